@@ -1,0 +1,351 @@
+"""Benchmark: exp(tA)v solves/s on the heat-equation workload (one GB300).
+
+Workload (default): A = 2D Dirichlet Laplacian / h^2 on a 2048 x 2048 grid
+(h = 1/2049, n = 4,194,304, nnz = 20,963,328, CSR int32/f64), v ~ U[0,1]
+(seed 1), t = 1e-5, m = 30, tol = 1e-6, run to convergence. Synthetic,
+seeded; the reference publishes no dataset for it.
+
+A step is one full solve y = exp(tA)v. `value` is solves/s of the chosen
+form (mixed precision when its result is within 1e-6 relative 2-norm error
+of the FP64 path on this workload, else FP64) with v and y resident in HBM;
+`e2e` is the same metric through the host-buffer C ABI call (mexk_expmv:
+H2D of v and D2H of y inside the timed region). The basis (>= 520 MB) and
+CSR (251 MB) exceed the 129 MB L2, so no extra flush runs between steps.
+
+    python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "matrix-exp-krylov_gb300"))
+
+METRIC = "exp(tA)v solves/s at <=1e-6 rel err, chosen vs plain FP64 (1 GB300); SpMV HBM GB/s"
+WORKLOAD = ("heat2048: A = 2D Dirichlet Laplacian / h^2 on a 2048^2 grid (h=1/2049), n=4194304, "
+            "nnz=20963328, CSR int32/f64; v ~ U[0,1] seed 1; t=1e-5, m=30, tol=1e-6, max_restarts=0")
+HEAT_GOLDEN = os.path.join(ROOT, "tests", "golden", "heat2048_reference.npz")
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ bytes model
+def kernel_bytes(kind, n, nnz, k, fp32):
+    """Algorithmic HBM bytes of one launch (per-kernel minimum traffic)."""
+    s = 4 if fp32 else 8
+    if kind == "spmv":
+        return nnz * (s + 4) + 4 * (n + 1) + 2 * n * s  # values+cols, row_ptr, x once, y
+    if kind == "gs_dot":
+        return k * n * s + n * s  # V_k, w
+    if kind in ("gs_upd_dot", "gs_upd_norm"):
+        return k * n * s + 2 * n * s  # V_k, w read + write
+    if kind == "normalize":
+        return 2 * n * s
+    if kind == "lift":
+        return k * n * s + 8 * n
+    return 0
+
+
+def profile_cycle(ctx, m, n, nnz, precision, iters=2):
+    """CUDA-event timing of every kernel kind of one Krylov cycle."""
+    fp32 = precision == "mixed"
+    kinds = ["spmv", "gs_dot", "gs_upd_dot", "gs_upd_norm", "normalize"]
+    per = {k: {"ms": 0.0, "bytes": 0.0, "launches": 0} for k in kinds + ["controller", "lift"]}
+    for j in range(m):
+        for kind in kinds:
+            ms = ctx.profile_kernel(kind, j, iters, precision)
+            per[kind]["ms"] += ms
+            per[kind]["bytes"] += kernel_bytes(kind, n, nnz, j + 1, fp32)
+            per[kind]["launches"] += 1
+    for kind in ("controller", "lift"):
+        ms = ctx.profile_kernel(kind, m - 1, iters, precision)
+        per[kind]["ms"] += ms
+        per[kind]["bytes"] += kernel_bytes(kind, n, nnz, m, fp32)
+        per[kind]["launches"] += 1
+    return per
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_cycle_seconds(A, v, t, m, cycles=1):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    if not os.path.exists(O.LIB_PATH):
+        O.build(with_reference=False)
+    t0 = time.perf_counter()
+    O.expmv(A, v, t, m, max_cycles=cycles)
+    return (time.perf_counter() - t0) / cycles
+
+
+def reference_attempts():
+    """Basis builds per solve of the reference: one per [STEP] attempt (it
+    rebuilds the basis on every reject), from its own full-size run."""
+    if os.path.exists(HEAT_GOLDEN):
+        d = np.load(HEAT_GOLDEN)
+        return int(len(d["step_lines"])), "reference run (tests/golden/heat2048_reference.npz)"
+    return None, None
+
+
+# ------------------------------------------------------------------ arms
+def make_problem():
+    from mexk import synthetic as S
+
+    return S.config1()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    P = make_problem()
+    attempts, src = reference_attempts()
+    for _ in range(args.warmup):
+        pass  # the CPU sample has no warm-up effect worth paying for
+    secs = []
+    for _ in range(max(1, args.steps)):
+        secs.append(cpu_cycle_seconds(P.A, P.v, P.t, P.m, 1))
+    t_cycle = statistics.median(secs)
+    if attempts is None:
+        attempts = 1
+        src = "unknown: one basis build counted as one solve"
+    value = 1.0 / (t_cycle * attempts)
+    sample = (f"{len(secs)} x one Arnoldi cycle (m=30, n=4194304) of the reference's CPU algorithm "
+              f"(oracle port, bit-identical to main_cpu.cpp), median {t_cycle:.2f}s; a solve = {attempts} "
+              f"basis builds ({src})")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_cycle * attempts * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "form": "reference CPU (FP64, 1 thread)"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    from mexk import synthetic as S  # noqa: F401
+    from mexk.api import Context
+
+    torch.cuda.set_device(local_rank)
+    P = make_problem()
+    n, nnz, m = P.A.n, P.A.nnz, P.m
+    ctx = Context(P.A, m_alloc=m, device=local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    v_d = torch.from_numpy(P.v).cuda()
+    y64 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    y32 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+
+    res64 = ctx.expmv_device(v_d.data_ptr(), y64.data_ptr(), P.t, m, precision="fp64")
+    steps64 = ctx.steps()
+    res32 = ctx.expmv_device(v_d.data_ptr(), y32.data_ptr(), P.t, m, precision="mixed")
+    torch.cuda.synchronize()
+    rel_err = float(torch.linalg.norm(y32 - y64) / torch.linalg.norm(y64))
+    form = args.precision if args.precision != "auto" else ("mixed" if rel_err <= 1e-6 else "fp64")
+
+    def timed(precision, K, W):
+        out = torch.zeros(n, dtype=torch.float64, device="cuda")
+        res = None
+        for _ in range(W):
+            res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), P.t, m, precision=precision)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        launches = 0
+        with ClockSampler(local_rank) as clk:
+            e0.record(stream)
+            for _ in range(K):
+                res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), P.t, m, precision=precision)
+                launches += 2 + res["cycles"] * (5 * m + 3)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            torch.distributed.barrier()
+            ms = float(t.item())
+        return ms, res, launches, clk.summary()
+
+    ms_c, res_c, launches, clocks = timed(form, args.steps, args.warmup)
+    value = world * args.steps / (ms_c / 1e3)
+    ms64, _, _, _ = timed("fp64", max(1, args.steps), 1) if form != "fp64" else (ms_c, None, None, None)
+    fp64_sps = world * max(1, args.steps) / (ms64 / 1e3)
+
+    # e2e: host buffers through mexk_expmv (H2D v, solve, D2H y each step)
+    v_pin = torch.from_numpy(P.v).pin_memory()
+    y_pin = torch.zeros(n, dtype=torch.float64).pin_memory()
+    import ctypes as C
+
+    from mexk._lib import Result, check, lib
+    from mexk.api import params as mkparams
+
+    pr = mkparams(m, P.t, precision=form)
+    r = Result()
+    vp = C.cast(v_pin.data_ptr(), C.POINTER(C.c_double))
+    yp = C.cast(y_pin.data_ptr(), C.POINTER(C.c_double))
+    check(lib().mexk_expmv(ctx.handle, C.byref(pr), vp, yp, C.byref(r)), "mexk_expmv")
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        check(lib().mexk_expmv(ctx.handle, C.byref(pr), vp, yp, C.byref(r)), "mexk_expmv")
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * args.steps / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": 8 * n,
+           "d2h_bytes_per_step": 8 * n}
+
+    # kernel roofline from live CUDA-event timings of each kernel kind
+    peak, peak_kind = measured_peaks()
+    per = profile_cycle(ctx, m, n, nnz, form)
+    tot_ms = sum(p["ms"] for p in per.values())
+    dom = max(per, key=lambda k: per[k]["ms"])
+    ach = per[dom]["bytes"] / (per[dom]["ms"] / 1e3) / 1e9
+    traffic = None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"}
+    sp = per["spmv"]
+    spmv_gbs = sp["bytes"] / (sp["ms"] / 1e3) / 1e9
+    per64 = profile_cycle(ctx, m, n, nnz, "fp64") if form != "fp64" else per
+    sp64 = per64["spmv"]
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        attempts, src = reference_attempts()
+        if attempts is None:
+            attempts, src = len(steps64), "this run's FP64 decision sequence"
+        t_cycle = cpu_cycle_seconds(P.A, P.v, P.t, m, 1)
+        cpu = {"value": 1.0 / (t_cycle * attempts), "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": (f"one Arnoldi cycle (m=30, n=4194304) of the oracle port of main_cpu.cpp on 1 core "
+                          f"took {t_cycle:.2f}s; a reference solve = {attempts} basis builds ({src})")}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_c / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if form == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": form, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (CSR 251 MB, basis >= 520 MB); no flush"},
+            "fp64_solves_per_s": fp64_sps, "chosen_rel_err_vs_fp64": rel_err,
+            "solve": {"attempts": res_c["attempts"], "cycles": res_c["cycles"],
+                      "restarts_done": res_c["restarts_done"], "converged": res_c["converged"],
+                      "fp64_attempts": res64["attempts"], "mixed_attempts": res32["attempts"]},
+            "spmv": {"gbs": spmv_gbs, "frac": spmv_gbs / peak, "precision": form,
+                     "fp64_gbs": sp64["bytes"] / (sp64["ms"] / 1e3) / 1e9},
+            "kernel_share": {k: round(p["ms"] / tot_ms, 4) for k, p in per.items()},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

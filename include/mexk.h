@@ -1,0 +1,170 @@
+/*
+ * mexk -- C ABI of the GB300 (sm_103a) restarted-Arnoldi exp(t*A)*v library.
+ *
+ * Plain pointers and sizes only. "Device" pointers are CUDA device addresses
+ * on the context's device; "host" pointers are ordinary host memory.
+ * Streams are passed as void* (a cudaStream_t; NULL = the context's own
+ * stream for context calls, the legacy default stream for the free kernel
+ * calls). Every function returns MEXK_OK or a MEXK_ERR_* code and never
+ * exits the process; mexk_error_string() explains a code and
+ * mexk_last_error_detail() gives the last failing CUDA call.
+ *
+ * The reference (kol-di/matrix-exp-krylov) has no library or FFI layer: its
+ * solver is C++ classes compiled into main.cu. Each entry point below names
+ * the reference code it replaces (file:line in that project).
+ */
+#ifndef MEXK_H
+#define MEXK_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MEXK_OK 0
+#define MEXK_ERR_INVALID 1     /* bad argument */
+#define MEXK_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define MEXK_ERR_ALLOC 3       /* device or pinned allocation failed */
+#define MEXK_ERR_NOT_READY 4   /* call order violated (e.g. expmv before upload) */
+#define MEXK_ERR_DEVICE 5      /* the device reported a failure status */
+#define MEXK_ERR_UNSUPPORTED 6 /* valid request this build does not handle */
+
+/* Arithmetic of the Krylov basis and matrix values. */
+#define MEXK_PREC_FP64 0  /* plain method: everything FP64 (the reference's path) */
+#define MEXK_PREC_MIXED 1 /* A values, basis V_m and SpMV/Gram-Schmidt in FP32;
+                             Hessenberg, norms, Pade and residual in FP64 */
+
+/* Largest Krylov dimension m this build supports. */
+#define MEXK_M_MAX 64
+
+/* Solver parameters. Mirrors ArnoldiParams (main.cu:1221-1230) plus the
+ * precision choice; the controller constants follow TimeSteppingParams
+ * defaults (main.cu:1292-1305). */
+typedef struct {
+    int m;               /* Krylov dimension, 1 <= m <= MEXK_M_MAX, m < n */
+    double t;            /* total time */
+    double tol;          /* per-step tolerance on the residual estimate */
+    int max_restarts;    /* > 0: dt_init = t/max_restarts and at most that many
+                            accepted steps; <= 0: dt_init = t, cap 1000 */
+    int reorthogonalize; /* nonzero: second Gram-Schmidt pass (CLI always on) */
+    int precision;       /* MEXK_PREC_* */
+} mexk_params_t;
+
+/* Outcome of one solve. converged / restarts_done / last_residual are the
+ * reference's ArnoldiRunner public fields (main.cu:1258-1260). */
+typedef struct {
+    int converged;
+    int restarts_done;    /* accepted time steps */
+    double last_residual;
+    int attempts;         /* accepted + rejected attempts ([STEP] lines) */
+    int cycles;           /* Arnoldi basis builds (rejected attempts reuse the basis) */
+    long long spmv_count; /* sparse products performed */
+    double t_done;        /* time reached */
+    int status;           /* device status bits, 0 = clean */
+} mexk_result_t;
+
+/* One accept/reject attempt: the fields of the reference's [STEP] line
+ * (main.cu:1471-1474). */
+typedef struct {
+    double t_done, dt, err;
+    int m_used, accepts, rejects;
+} mexk_step_t;
+
+typedef struct mexk_context_s* mexk_context_t;
+
+/* ---- library ---------------------------------------------------------- */
+const char* mexk_error_string(int code);
+/* Text of the last CUDA failure seen by this thread (empty if none). */
+const char* mexk_last_error_detail(void);
+/* Build identification, e.g. "mexk 0.1 sm_103a". */
+const char* mexk_version(void);
+/* Number of CUDA devices visible (cudaGetDeviceCount, main.cu:2146). */
+int mexk_device_count(int* count);
+
+/* ---- device context: replaces DeviceContext (main.cu:747-1125) -------- */
+/* DeviceContext(dev_id) + init_handles() + create_streams()
+ * (main.cu:806-868): selects the device and creates the context's stream. */
+int mexk_context_create(int device, mexk_context_t* out);
+
+/* DeviceContext::alloc_from + create_descriptors (main.cu:873-1067):
+ * copies the CSR matrix (rows x rows, int32 indices, FP64 values, host
+ * memory) to the device, allocates the basis for Krylov dimensions up to
+ * m_alloc_max and builds the SpMV row-block schedule. The reference's
+ * on/off-diagonal split and ghost buffers do not exist on one device.
+ * Call once per context. */
+int mexk_context_upload_csr(mexk_context_t ctx, int rows, long long nnz, const int* row_ptr,
+                            const int* col_idx, const double* values, int m_alloc_max);
+
+/* DeviceContext::destroy (main.cu:1069-1124). Safe on NULL. */
+int mexk_context_destroy(mexk_context_t ctx);
+
+/* The context's CUDA stream (a cudaStream_t). */
+void* mexk_context_stream(mexk_context_t ctx);
+
+/* ---- the hot path: ArnoldiRunner::compute_expmv (main.cu:1411-1571) ---- */
+/* y = exp(t*A)*v with host vectors of length rows. Copies v in, runs the
+ * whole restarted-Arnoldi solve on the device (basis build, fused
+ * Gram-Schmidt, Pade exponential, accept/reject control, lift, restart)
+ * and copies y out. result may be NULL. */
+int mexk_expmv(mexk_context_t ctx, const mexk_params_t* p, const double* v_host, double* y_host,
+               mexk_result_t* result);
+
+/* Same with device vectors (FP64, length rows) on `stream` (NULL = the
+ * context stream). Returns after the solve finished on the device. */
+int mexk_expmv_device(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev,
+                      double* y_dev, void* stream, mexk_result_t* result);
+
+/* Attempt log of the last solve ([STEP] lines). Writes up to cap entries,
+ * *count = number available (may exceed cap). */
+int mexk_get_steps(mexk_context_t ctx, mexk_step_t* steps, int cap, int* count);
+
+/* ---- individual kernels (device pointers), for tests and composition -- */
+/* w = A*x, CSR FP64 (replaces cusparseSpMV, main.cu:1722-1767). */
+int mexk_spmv_f64(int rows, const int* row_ptr, const int* col_idx, const double* values,
+                  const double* x, double* y, void* stream);
+/* w = A*x with FP32 values and vectors, FP32 products and accumulation. */
+int mexk_spmv_f32(int rows, const int* row_ptr, const int* col_idx, const float* values,
+                  const float* x, float* y, void* stream);
+
+/* One Arnoldi step j on the context's matrix: w = A*V[:,j], two
+ * Gram-Schmidt passes (replaces orthogonalize_mgs, main.cu:1769-1876) and
+ * normalisation with the breakdown test (normalize_new_vector,
+ * main.cu:1878-1942). V is the context's FP64 basis, set with
+ * mexk_context_set_basis. On return h[0..j] = H(0..j, j), *beta = H(j+1,j)
+ * (0 on breakdown), *ok = 1 unless breakdown. Host outputs. */
+int mexk_arnoldi_step(mexk_context_t ctx, int j, int reorthogonalize, int precision, double* h,
+                      double* beta, int* ok);
+/* Copy columns 0..ncols-1 of the context basis to/from host (column-major,
+ * leading dimension rows) in the given precision's storage. */
+int mexk_context_set_basis(mexk_context_t ctx, int precision, const double* V_host, int ncols);
+int mexk_context_get_basis(mexk_context_t ctx, int precision, double* V_host, int ncols);
+
+/* E = exp(A) for a k-by-k FP64 matrix (device pointers, column-major,
+ * leading dimensions lda/lde), single thread block Pade scaling-and-squaring
+ * (replaces Eigen's MatrixXd::exp at main.cu:33-36). k <= MEXK_M_MAX. */
+int mexk_expm_f64(int k, const double* A, int lda, double* E, int lde, void* stream);
+
+/* ---- measurement ------------------------------------------------------ */
+#define MEXK_KERNEL_SPMV 0
+#define MEXK_KERNEL_GS_DOT 1      /* pass-1 dots */
+#define MEXK_KERNEL_GS_UPD_DOT 2  /* pass-1 update fused with pass-2 dots */
+#define MEXK_KERNEL_GS_UPD_NORM 3 /* pass-2 update + norm */
+#define MEXK_KERNEL_NORMALIZE 4
+#define MEXK_KERNEL_LIFT 5
+#define MEXK_KERNEL_CONTROLLER 6
+#define MEXK_KERNEL_KINDS 7
+
+/* Times `iters` launches of one solver kernel for Arnoldi step j (k = j+1
+ * basis columns) on the context stream with a CUDA event pair around each
+ * launch, on the context's current basis and matrix (run a solve first).
+ * Each launch starts from a fresh running state. *ms_per_launch = mean
+ * launch duration in milliseconds. No reference counterpart (the reference
+ * times only the whole solve, METRIC total_compute_expmv_ms at main.cu:1570). */
+int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int iters, double* ms_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MEXK_H */

@@ -1,0 +1,451 @@
+// K3: exp(dt*H_k) on the device plus the accept/reject step controller.
+//
+// The reference computes the small exponential on the host with Eigen
+// (matrix_exp_stable, main.cu:33-36), twice per attempt (small_expm_and_lift
+// main.cu:1954-1978 and residual_estimate main.cu:2004-2020), after copying
+// every H entry to the host. Here one thread block holds the k-by-k matrices
+// in shared memory and evaluates the Pade scaling-and-squaring method of
+// N. J. Higham, SIAM J. Matrix Anal. Appl. 26(4), 2005 (the method Eigen
+// 3.4's MatrixExponential implements): degree 3/5/7/9/13 from the 1-norm,
+// 2^-s scaling before degree 13, an LU solve with partial pivoting for
+// (V-U)^{-1}(V+U), then s squarings. The same exponential feeds the lift
+// coefficients and the residual estimate |H(k,k-1) [exp(dt H_k) e1]_{k-1}| |v|.
+//
+// The controller (ArnoldiRunner::compute_expmv, main.cu:1431-1518) runs in
+// the same block with the reference's arithmetic: accept if err <= tol or
+// breakdown; grow dt by 1.5*0.8 when err < 0.1*tol (capped at dt_max);
+// otherwise shrink by 0.5*0.8 (floored at dt_min) and retry, aborting after
+// 20 rejects. The reference rebuilds the whole Arnoldi basis on every retry;
+// the basis depends only on A and the start vector, never on dt, so the
+// retry here reuses it and re-evaluates only the exponential: same decisions
+// and results, m SpMVs and Gram-Schmidt sweeps fewer per reject.
+#include "mexk_internal.cuh"
+
+#include <math.h>
+
+namespace mexk {
+
+namespace {
+
+constexpr int EXPM_THREADS = 512;
+
+__device__ void mm(int k, const double* X, const double* Y, double* Z) {
+    const int kk = k * k;
+    for (int e = threadIdx.x; e < kk; e += blockDim.x) {
+        const int i = e % k, j = e / k;
+        double s = 0.0;
+        for (int l = 0; l < k; ++l) s = fma(X[i + l * k], Y[l + j * k], s);
+        Z[e] = s;
+    }
+    __syncthreads();
+}
+
+// Z = c0*M0 + c1*M1 + c2*M2 + c3*M3 + cid*I, terms left to right (nt <= 4).
+__device__ void lincomb(int k, int nt, const double* c, const double* const* M, double cid, double* Z) {
+    const int kk = k * k;
+    for (int e = threadIdx.x; e < kk; e += blockDim.x) {
+        double s = c[0] * M[0][e];
+        for (int t = 1; t < nt; ++t) s = s + c[t] * M[t][e];
+        if (cid != 0.0 && (e % k) == (e / k)) s = s + cid;
+        Z[e] = s;
+    }
+    __syncthreads();
+}
+
+__device__ void lu_factor(int k, double* D, int* piv, int* status) {
+    for (int c = 0; c < k; ++c) {
+        if (threadIdx.x < 32) {
+            double best = -1.0;
+            int bi = k;
+            for (int i = c + threadIdx.x; i < k; i += 32) {
+                const double v = fabs(D[i + c * k]);
+                if (v > best) {
+                    best = v;
+                    bi = i;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) {
+                    best = ob;
+                    bi = oi;
+                }
+            }
+            if (threadIdx.x == 0) piv[c] = (bi < k) ? bi : c;
+        }
+        __syncthreads();
+        const int p = piv[c];
+        if (p != c) {
+            for (int j = threadIdx.x; j < k; j += blockDim.x) {
+                const double t = D[c + j * k];
+                D[c + j * k] = D[p + j * k];
+                D[p + j * k] = t;
+            }
+            __syncthreads();
+        }
+        const double d = D[c + c * k];
+        if (d != 0.0) {
+            for (int i = c + 1 + threadIdx.x; i < k; i += blockDim.x) D[i + c * k] /= d;
+            __syncthreads();
+            const int r = k - c - 1;
+            for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+                const int i = c + 1 + e % r, j = c + 1 + e / r;
+                D[i + j * k] -= D[i + c * k] * D[c + j * k];
+            }
+        } else if (threadIdx.x == 0) {
+            *status |= ST_LU_SINGULAR;
+        }
+        __syncthreads();
+    }
+}
+
+__device__ void lu_solve(int k, const double* LU, const int* piv, double* B) {
+    for (int i = 0; i < k; ++i) {
+        const int p = piv[i];
+        if (p != i) {
+            for (int c = threadIdx.x; c < k; c += blockDim.x) {
+                const double t = B[i + c * k];
+                B[i + c * k] = B[p + c * k];
+                B[p + c * k] = t;
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = 0; i < k - 1; ++i) {
+        const int r = k - i - 1;
+        for (int e = threadIdx.x; e < r * k; e += blockDim.x) {
+            const int l = i + 1 + e % r, c = e / r;
+            B[l + c * k] -= LU[l + i * k] * B[i + c * k];
+        }
+        __syncthreads();
+    }
+    for (int i = k - 1; i >= 0; --i) {
+        for (int c = threadIdx.x; c < k; c += blockDim.x) B[i + c * k] /= LU[i + i * k];
+        __syncthreads();
+        for (int e = threadIdx.x; e < i * k; e += blockDim.x) {
+            const int l = e % i, c = e / i;
+            B[l + c * k] -= LU[l + i * k] * B[i + c * k];
+        }
+        __syncthreads();
+    }
+}
+
+// Pade [m/m] coefficients b_j = (2m-j)! / (j! (m-j)!), exact integers.
+__device__ void pade_coefficients(int m, double* b) {
+    for (int j = 0; j <= m; ++j) {
+        unsigned long long num = 1ull, den = 1ull;
+        for (int i = m - j + 1; i <= 2 * m - j; ++i) num *= static_cast<unsigned long long>(i);
+        for (int i = 2; i <= j; ++i) den *= static_cast<unsigned long long>(i);
+        b[j] = static_cast<double>(num / den);
+    }
+}
+
+struct ExpmBuf {
+    double *A, *A2, *A4, *A6, *U, *T;
+    int* piv;
+    double* red;  // >= k doubles
+};
+
+// exp of the k-by-k matrix in B.A (ld k); returns the buffer holding the
+// result. All threads of the block must call it.
+__device__ double* expm_block(const ExpmBuf& B, int k, int* status) {
+    __shared__ int s_deg, s_sq;
+    __shared__ double s_b[14];
+    if (threadIdx.x < k) {
+        double cs = 0.0;
+        for (int i = 0; i < k; ++i) cs += fabs(B.A[i + threadIdx.x * k]);
+        B.red[threadIdx.x] = cs;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double l1 = 0.0;
+        for (int j = 0; j < k; ++j)
+            if (B.red[j] > l1) l1 = B.red[j];
+        int sq = 0, deg;
+        if (l1 < 1.495585217958292e-002) deg = 3;
+        else if (l1 < 2.539398330063230e-001) deg = 5;
+        else if (l1 < 9.504178996162932e-001) deg = 7;
+        else if (l1 < 2.097847961257068e+000) deg = 9;
+        else {
+            deg = 13;
+            (void)frexp(l1 / 5.371920351148152, &sq);
+            if (sq < 0) sq = 0;
+        }
+        s_deg = deg;
+        s_sq = sq;
+        pade_coefficients(deg, s_b);
+    }
+    __syncthreads();
+    const int deg = s_deg, sq = s_sq;
+    const int kk = k * k;
+    if (sq > 0) {
+        for (int e = threadIdx.x; e < kk; e += blockDim.x) B.A[e] = ldexp(B.A[e], -sq);
+        __syncthreads();
+    }
+    const double* b = s_b;
+    mm(k, B.A, B.A, B.A2);
+    if (deg >= 5) mm(k, B.A2, B.A2, B.A4);
+    if (deg >= 7) mm(k, B.A4, B.A2, B.A6);
+    double *pU, *pV;
+    if (deg <= 7) {
+        const double* M[3] = {deg == 3 ? B.A2 : (deg == 5 ? B.A4 : B.A6), deg == 7 ? B.A4 : B.A2, B.A2};
+        const int nt = deg == 3 ? 1 : (deg == 5 ? 2 : 3);
+        double cu[3], cv[3];
+        if (deg == 3) { cu[0] = b[3]; cv[0] = b[2]; }
+        if (deg == 5) { cu[0] = b[5]; cu[1] = b[3]; cv[0] = b[4]; cv[1] = b[2]; }
+        if (deg == 7) { cu[0] = b[7]; cu[1] = b[5]; cu[2] = b[3]; cv[0] = b[6]; cv[1] = b[4]; cv[2] = b[2]; }
+        lincomb(k, nt, cu, M, b[1], B.T);
+        mm(k, B.A, B.T, B.U);
+        lincomb(k, nt, cv, M, b[0], B.T);
+        pU = B.U;
+        pV = B.T;
+    } else if (deg == 9) {
+        mm(k, B.A6, B.A2, B.U);  // A8 in U
+        for (int e = threadIdx.x; e < kk; e += blockDim.x) {
+            const double a8 = B.U[e], a6 = B.A6[e], a4 = B.A4[e], a2 = B.A2[e];
+            const bool dg = (e % k) == (e / k);
+            double u = b[9] * a8 + b[7] * a6 + b[5] * a4 + b[3] * a2;
+            double v = b[8] * a8 + b[6] * a6 + b[4] * a4 + b[2] * a2;
+            if (dg) { u = u + b[1]; v = v + b[0]; }
+            B.T[e] = u;
+            B.U[e] = v;
+        }
+        __syncthreads();
+        mm(k, B.A, B.T, B.A2);
+        pU = B.A2;
+        pV = B.U;
+    } else {
+        const double* M[3] = {B.A6, B.A4, B.A2};
+        const double c1[3] = {b[13], b[11], b[9]};
+        lincomb(k, 3, c1, M, 0.0, B.T);
+        mm(k, B.A6, B.T, B.U);
+        for (int e = threadIdx.x; e < kk; e += blockDim.x) {
+            double s = b[7] * B.A6[e] + b[5] * B.A4[e] + b[3] * B.A2[e];
+            if ((e % k) == (e / k)) s = s + b[1];
+            B.U[e] = B.U[e] + s;
+        }
+        __syncthreads();
+        mm(k, B.A, B.U, B.T);  // U final in T
+        const double c3[3] = {b[12], b[10], b[8]};
+        lincomb(k, 3, c3, M, 0.0, B.U);
+        mm(k, B.A6, B.U, B.A);  // V in A
+        for (int e = threadIdx.x; e < kk; e += blockDim.x) {
+            double s = b[6] * B.A6[e] + b[4] * B.A4[e] + b[2] * B.A2[e];
+            if ((e % k) == (e / k)) s = s + b[0];
+            B.A[e] = B.A[e] + s;
+        }
+        __syncthreads();
+        pU = B.T;
+        pV = B.A;
+    }
+    // numer = U + V (into pU), denom = -U + V (into pV)
+    for (int e = threadIdx.x; e < kk; e += blockDim.x) {
+        const double u = pU[e], v = pV[e];
+        pU[e] = u + v;
+        pV[e] = -u + v;
+    }
+    __syncthreads();
+    lu_factor(k, pV, B.piv, status);
+    lu_solve(k, pV, B.piv, pU);
+    double* R = pU;
+    double* F = pV;
+    for (int s = 0; s < sq; ++s) {
+        mm(k, R, R, F);
+        double* t = R;
+        R = F;
+        F = t;
+    }
+    return R;
+}
+
+__device__ ExpmBuf carve(double* smem, int k) {
+    ExpmBuf B;
+    const size_t kk = static_cast<size_t>(k) * k;
+    B.A = smem;
+    B.A2 = B.A + kk;
+    B.A4 = B.A2 + kk;
+    B.A6 = B.A4 + kk;
+    B.U = B.A6 + kk;
+    B.T = B.U + kk;
+    B.red = B.T + kk;
+    B.piv = reinterpret_cast<int*>(B.red + MEXK_M_MAX);
+    return B;
+}
+
+size_t expm_smem_bytes(int k) {
+    return sizeof(double) * (6 * static_cast<size_t>(k) * k + MEXK_M_MAX) + sizeof(int) * MEXK_M_MAX;
+}
+
+__global__ void __launch_bounds__(EXPM_THREADS)
+    expm_standalone_kernel(int k, const double* __restrict__ A, int lda, double* __restrict__ E, int lde,
+                           int* status) {
+    extern __shared__ double smem[];
+    ExpmBuf B = carve(smem, k);
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = A[(e % k) + static_cast<size_t>(e / k) * lda];
+    __syncthreads();
+    double* R = expm_block(B, k, status);
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) E[(e % k) + static_cast<size_t>(e / k) * lde] = R[e];
+}
+
+enum : int { DEC_REJECT = 0, DEC_ACCEPT = 1, DEC_ABORT = 2 };
+
+__global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a, int m) {
+    extern __shared__ double smem[];
+    __shared__ int s_k, s_bd, s_dec;
+    __shared__ double s_dt;
+    DevState* st = a.st;
+    if (st->done) return;
+    if (threadIdx.x == 0) {
+        const int bd = st->breakdown;
+        int k = bd ? st->k_used : m;
+        if (k < 1 || k > m) {
+            st->status |= ST_BAD_K;
+            k = k < 1 ? 1 : m;
+        }
+        s_k = k;
+        s_bd = bd;
+        s_dt = st->dt;
+    }
+    __syncthreads();
+    const int k = s_k;
+    const bool bd = s_bd != 0;
+    const size_t ldh = static_cast<size_t>(a.ldh);
+    ExpmBuf B = carve(smem, k);
+    int rejects = 0;
+    double err = 0.0;
+    double* R = nullptr;
+    while (true) {
+        const double dt = s_dt;
+        for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = dt * a.H[(e % k) + (e / k) * ldh];
+        __syncthreads();
+        R = expm_block(B, k, &st->status);
+        if (threadIdx.x == 0) {
+            err = bd ? 0.0 : fabs(a.H[k + (k - 1) * ldh] * R[k - 1]) * st->v_norm;
+            if (st->nlog < st->log_cap && a.log != nullptr) {
+                mexk_step_t& L = a.log[st->nlog];
+                L.t_done = st->t_done;
+                L.dt = dt;
+                L.err = err;
+                L.m_used = k;
+                L.accepts = st->accepted;
+                L.rejects = rejects;
+            }
+            st->nlog += 1;
+            st->attempts += 1;
+            int dec;
+            if (err <= st->tol || bd) {
+                dec = DEC_ACCEPT;
+            } else {
+                ++rejects;
+                if (rejects >= st->max_rejects) {
+                    dec = DEC_ABORT;
+                } else {
+                    dec = DEC_REJECT;
+                    const double dt_new = dt * 0.5 * 0.8;
+                    s_dt = dt_new > st->dt_min ? dt_new : st->dt_min;
+                }
+            }
+            s_dec = dec;
+        }
+        __syncthreads();
+        if (s_dec != DEC_REJECT) break;
+    }
+    // Lift coefficients |v| * wH_i, zero where |wH_i| <= 1e-15 (main.cu:1993).
+    const double vn = st->v_norm;
+    for (int i = threadIdx.x; i <= k; i += blockDim.x) {
+        const double wi = (i < k) ? R[i] : 0.0;
+        a.coef[i] = (fabs(wi) > 1e-15) ? vn * wi : 0.0;
+    }
+    if (threadIdx.x == 0) {
+        double dt = s_dt;
+        if (s_dec == DEC_ACCEPT) {
+            st->t_done += dt;
+            st->accepted += 1;
+            st->last_residual = err;
+            if (st->t_done >= st->total_t) {
+                st->converged = 1;
+                st->done = 1;
+                st->restart = 0;
+            } else {
+                if (err < 0.1 * st->tol) {
+                    const double dt_new = dt * 1.5 * 0.8;
+                    dt = dt_new < st->dt_max ? dt_new : st->dt_max;
+                }
+                if (st->accepted >= st->max_steps) {
+                    st->done = 1;
+                    st->restart = 0;
+                } else {
+                    st->restart = 1;
+                }
+            }
+        } else {
+            st->converged = 0;
+            st->last_residual = err;
+            st->t_done = st->total_t;
+            st->done = 1;
+            st->restart = 0;
+        }
+        st->k_lift = k;
+        st->cycles += 1;
+        st->spmv_count += k;
+        st->lift = 1;
+        if (!st->done) {
+            st->breakdown = 0;
+            st->k_used = m;
+            const double rem = st->total_t - st->t_done;
+            dt = dt < rem ? dt : rem;
+        }
+        st->dt = dt;
+    }
+}
+
+}  // namespace
+
+int expm_init_attributes() {
+    const int bytes = static_cast<int>(expm_smem_bytes(MEXK_M_MAX));
+    MEXK_CK(cudaFuncSetAttribute(expm_standalone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    MEXK_CK(cudaFuncSetAttribute(controller_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    return MEXK_OK;
+}
+
+int launch_expm_standalone(int k, const double* A, int lda, double* E, int lde, int* status, cudaStream_t s) {
+    const size_t smem = expm_smem_bytes(k);
+    expm_standalone_kernel<<<1, EXPM_THREADS, smem, s>>>(k, A, lda, E, lde, status);
+    MEXK_CK_LAUNCH("expm_standalone_kernel");
+    return MEXK_OK;
+}
+
+int launch_controller(const ControlArgs& a, int m, cudaStream_t s) {
+    const size_t smem = expm_smem_bytes(m);
+    controller_kernel<<<1, EXPM_THREADS, smem, s>>>(a, m);
+    MEXK_CK_LAUNCH("controller_kernel");
+    return MEXK_OK;
+}
+
+}  // namespace mexk
+
+extern "C" int mexk_expm_f64(int k, const double* A, int lda, double* E, int lde, void* stream) {
+    if (k < 1 || k > MEXK_M_MAX || !A || !E || lda < k || lde < k) return MEXK_ERR_INVALID;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int rc0 = mexk::expm_init_attributes();
+    if (rc0 != MEXK_OK) return rc0;
+    int* d_status = nullptr;
+    MEXK_CK(cudaMallocAsync(reinterpret_cast<void**>(&d_status), sizeof(int), s));
+    MEXK_CK(cudaMemsetAsync(d_status, 0, sizeof(int), s));
+    int rc = mexk::launch_expm_standalone(k, A, lda, E, lde, d_status, s);
+    int h_status = 0;
+    if (rc == MEXK_OK) {
+        cudaError_t e = cudaMemcpyAsync(&h_status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            mexk::set_cuda_error(e, "expm status copy", __FILE__, __LINE__);
+            rc = MEXK_ERR_CUDA;
+        }
+    }
+    cudaFreeAsync(d_status, s);
+    cudaStreamSynchronize(s);
+    if (rc == MEXK_OK && (h_status & mexk::ST_LU_SINGULAR)) rc = MEXK_ERR_DEVICE;
+    return rc;
+}

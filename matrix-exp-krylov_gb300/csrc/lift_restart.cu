@@ -1,0 +1,142 @@
+// K4: lift y = |v| V_k w_H with the norm of y for the restart, the restart
+// q1 = y/|y| and the start vector q1 = v/|v|.
+//
+// The reference lifts with one pageable H2D copy of the coefficient and one
+// cublasDaxpy per basis column (small_expm_and_lift, main.cu:1980-2001),
+// rereading and rewriting y k times, then restart_from_y
+// (main.cu:2023-2073) runs Dnrm2, an allreduce, a host sync, Dscal and two
+// D2D copies; init_q1 (main.cu:1574-1633) does the same for v. Here the
+// lift reads each basis column once, accumulates every row in one FMA chain
+// in column order (the axpy order), writes y once and reduces |y|^2 in the
+// same pass; the restart is a single scale into V[:,0]. The norm guard
+// |x| > 1e-14 follows the CPU twin (main_cpu.cpp:480, 596).
+#include "mexk_internal.cuh"
+
+#include <math.h>
+
+namespace mexk {
+
+namespace {
+
+constexpr int LIFT_THREADS = 256;
+
+template <typename TV>
+__global__ void __launch_bounds__(LIFT_THREADS) lift_kernel(LiftArgs a) {
+    __shared__ double s_coef[MEXK_M_MAX + 1];
+    __shared__ double s_red[32];
+    __shared__ double s_out[1];
+    __shared__ double s_scratch[LIFT_THREADS];
+    __shared__ int s_flag;
+    DevState* st = a.st;
+    if (!st->lift) return;
+    const int k = st->k_lift;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) s_coef[i] = a.coef[i];
+    __syncthreads();
+    const TV* __restrict__ V = static_cast<const TV*>(a.V);
+    const size_t ldv = static_cast<size_t>(a.ldv);
+    double nacc = 0.0;
+    for (int r = blockIdx.x * LIFT_THREADS + threadIdx.x; r < a.n; r += gridDim.x * LIFT_THREADS) {
+        double s = 0.0;
+        for (int c = 0; c < k; ++c) s = fma(s_coef[c], static_cast<double>(V[c * ldv + r]), s);
+        a.y[r] = s;
+        nacc = fma(s, s, nacc);
+    }
+    nacc = warp_sum(nacc);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = nacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < LIFT_THREADS / 32; ++q) t += s_red[q];
+        a.partials[static_cast<size_t>(blockIdx.x) * RED_STRIDE] = t;
+    }
+    if (!grid_last_block(a.counter, &s_flag)) return;
+    reduce_partials(a.partials, gridDim.x, 1, s_out, s_scratch);
+    if (threadIdx.x == 0) {
+        const double nrm = sqrt(s_out[0]);
+        st->restart_scale = nrm > 1e-14 ? 1.0 / nrm : 1.0;
+        if (st->restart) st->v_norm = nrm;
+        st->lift = 0;
+    }
+}
+
+// |x|^2 of the start vector -> v_norm and restart_scale (init_q1).
+__global__ void __launch_bounds__(LIFT_THREADS)
+    start_norm_kernel(int n, const double* __restrict__ x, double* partials, unsigned int* counter,
+                      DevState* st) {
+    __shared__ double s_red[32];
+    __shared__ double s_out[1];
+    __shared__ double s_scratch[LIFT_THREADS];
+    __shared__ int s_flag;
+    double nacc = 0.0;
+    for (int r = blockIdx.x * LIFT_THREADS + threadIdx.x; r < n; r += gridDim.x * LIFT_THREADS)
+        nacc = fma(x[r], x[r], nacc);
+    nacc = warp_sum(nacc);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = nacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < LIFT_THREADS / 32; ++q) t += s_red[q];
+        partials[static_cast<size_t>(blockIdx.x) * RED_STRIDE] = t;
+    }
+    if (!grid_last_block(counter, &s_flag)) return;
+    reduce_partials(partials, gridDim.x, 1, s_out, s_scratch);
+    if (threadIdx.x == 0) {
+        const double nrm = sqrt(s_out[0]);
+        st->v_norm = nrm;
+        st->restart_scale = nrm > 1e-14 ? 1.0 / nrm : 1.0;
+    }
+}
+
+template <typename TV>
+__global__ void __launch_bounds__(256) restart_kernel(int n, const double* __restrict__ x, TV* __restrict__ V0,
+                                                      const DevState* st, int force) {
+    if (!force && !st->restart) return;
+    const double sc = st->restart_scale;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+        V0[r] = static_cast<TV>(x[r] * sc);
+}
+
+int elementwise_grid(int n) {
+    int g = (n + 255) / 256;
+    if (g > 8192) g = 8192;
+    return g < 1 ? 1 : g;
+}
+
+}  // namespace
+
+template <typename TV>
+int launch_lift(const LiftArgs& a, int grid, cudaStream_t s) {
+    lift_kernel<TV><<<grid, LIFT_THREADS, 0, s>>>(a);
+    MEXK_CK_LAUNCH("lift_kernel");
+    return MEXK_OK;
+}
+
+template <typename TV>
+int launch_restart(int n, int ldv, const double* y, TV* V, const DevState* st, cudaStream_t s) {
+    (void)ldv;
+    restart_kernel<TV><<<elementwise_grid(n), 256, 0, s>>>(n, y, V, st, 0);
+    MEXK_CK_LAUNCH("restart_kernel");
+    return MEXK_OK;
+}
+
+template <typename TV>
+int launch_init_start(int n, int ldv, const double* v, TV* V, double* partials, unsigned int* counter,
+                      DevState* st, int grid, cudaStream_t s) {
+    (void)ldv;
+    start_norm_kernel<<<grid, LIFT_THREADS, 0, s>>>(n, v, partials, counter, st);
+    MEXK_CK_LAUNCH("start_norm_kernel");
+    restart_kernel<TV><<<elementwise_grid(n), 256, 0, s>>>(n, v, V, st, 1);
+    MEXK_CK_LAUNCH("restart_kernel");
+    return MEXK_OK;
+}
+
+template int launch_lift<double>(const LiftArgs&, int, cudaStream_t);
+template int launch_lift<float>(const LiftArgs&, int, cudaStream_t);
+template int launch_restart<double>(int, int, const double*, double*, const DevState*, cudaStream_t);
+template int launch_restart<float>(int, int, const double*, float*, const DevState*, cudaStream_t);
+template int launch_init_start<double>(int, int, const double*, double*, double*, unsigned int*, DevState*,
+                                       int, cudaStream_t);
+template int launch_init_start<float>(int, int, const double*, float*, double*, unsigned int*, DevState*, int,
+                                      cudaStream_t);
+
+}  // namespace mexk

@@ -1,0 +1,226 @@
+// Internal declarations shared by the mexk CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "mexk.h"
+
+namespace mexk {
+
+// ------------------------------------------------------------ errors
+void set_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+void set_error_text(const std::string& s);
+
+#define MEXK_CK(call)                                                   \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) {                                        \
+            ::mexk::set_cuda_error(e_, #call, __FILE__, __LINE__);      \
+            return MEXK_ERR_CUDA;                                       \
+        }                                                               \
+    } while (0)
+
+#define MEXK_CK_LAUNCH(what)                                            \
+    do {                                                                \
+        cudaError_t e_ = cudaGetLastError();                            \
+        if (e_ != cudaSuccess) {                                        \
+            ::mexk::set_cuda_error(e_, what, __FILE__, __LINE__);       \
+            return MEXK_ERR_CUDA;                                       \
+        }                                                               \
+    } while (0)
+
+// ------------------------------------------------------------ device state
+// Scalar state of one solve, resident in device memory. The controller
+// fields follow ArnoldiRunner::compute_expmv (main.cu:1411-1571) and
+// TimeSteppingParams (main.cu:1237-1250).
+struct DevState {
+    double total_t, t_done, dt, dt_min, dt_max, tol;
+    double v_norm;        // |start vector| of the current segment
+    double last_residual;
+    double inv_beta;      // 1 / H(j+1, j) of the current Arnoldi step
+    double restart_scale; // 1 / |y| (or 1) for the restart
+    int m;
+    int max_steps;
+    int max_rejects;
+    int accepted;
+    int k_used;     // basis size of the cycle being built
+    int k_lift;     // basis size used by the lift of the finished cycle
+    int breakdown;  // set by the normalisation of the current cycle
+    int done;       // solve finished (converged or not)
+    int restart;    // the finished cycle was accepted and the solve goes on
+    int converged;
+    int status;     // error bits (0 = clean)
+    int attempts;
+    int cycles;
+    int nlog;
+    int log_cap;
+    int lift;       // the finished cycle's lift is pending
+    long long spmv_count;
+};
+
+// Status bits written by kernels.
+enum : int {
+    ST_LU_SINGULAR = 1,
+    ST_SMEM = 2,
+    ST_BAD_K = 4,
+};
+
+// ------------------------------------------------------------ constants
+constexpr int SPMV_THREADS = 256;
+constexpr int SPMV_TILE = 2048;     // nonzeros staged per row block
+constexpr int SPMV_TILE_ROWS = 512; // rows per row block
+constexpr int GS_THREADS = 256;
+constexpr int RED_STRIDE = 72;      // doubles per block partial (>= MEXK_M_MAX + 2)
+
+// ------------------------------------------------------------ helpers
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum, result valid in thread 0. `scratch` holds >= 32 values.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T* scratch) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    T s = 0;
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int i = 0; i < nw; ++i) s += scratch[i];
+    }
+    __syncthreads();
+    return s;
+}
+
+// Last-block-done handshake for grid reductions: every block has written its
+// partials; returns true in exactly one block (the last to arrive), which
+// then sees all partials. The counter is reset by that block.
+__device__ __forceinline__ bool grid_last_block(unsigned int* counter, int* smem_flag) {
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int ticket = atomicAdd(counter, 1u);
+        *smem_flag = (ticket == gridDim.x - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    const bool last = *smem_flag != 0;
+    if (last) {
+        __threadfence();
+        if (threadIdx.x == 0) *counter = 0u;
+    }
+    return last;
+}
+
+// Deterministic reduction of partials[b * RED_STRIDE + c] over blocks
+// b < nblocks for columns c < ncols by one block; out[c] in thread order.
+// Uses up to blockDim.x threads; scratch holds blockDim.x doubles.
+__device__ __forceinline__ void reduce_partials(const double* partials, int nblocks, int ncols,
+                                                double* out_smem, double* scratch) {
+    int groups = blockDim.x / (ncols > 0 ? ncols : 1);
+    if (groups < 1) groups = 1;
+    // power-of-two-free: thread t handles column c = t % ncols, group g = t / ncols
+    const int t = threadIdx.x;
+    const int c = t % ncols;
+    const int g = t / ncols;
+    double s = 0.0;
+    if (g < groups) {
+        for (int b = g; b < nblocks; b += groups) s += __ldcg(&partials[(size_t)b * RED_STRIDE + c]);
+    }
+    scratch[t] = s;
+    __syncthreads();
+    if (t < ncols) {
+        double tot = 0.0;
+        for (int q = 0; q < groups; ++q) tot += scratch[q * ncols + t];
+        out_smem[t] = tot;
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------ SpMV
+// Row-block schedule: rows [blocks[b], blocks[b+1]) form block b. A block
+// holds <= SPMV_TILE nonzeros and <= SPMV_TILE_ROWS rows, or one longer row.
+std::vector<int> build_row_blocks(int n, const int* row_ptr);
+
+template <typename TA, typename TX>
+int launch_spmv(int n, int nblocks, const int* blocks, const int* row_ptr, const int* col_idx,
+                const TA* values, const TX* x, TX* y, const int* skip_flag, cudaStream_t s);
+
+// ------------------------------------------------------------ Gram-Schmidt
+enum GsMode : int { GS_DOT = 0, GS_UPD_DOT = 1, GS_UPD_NORM = 2 };
+
+struct GsArgs {
+    int n;
+    int k;            // number of basis columns involved (j+1)
+    int j;            // Arnoldi step (column of H)
+    int ldv;          // basis leading dimension (elements)
+    int ldh;          // H leading dimension
+    int reortho;      // second pass enabled
+    const void* V;    // basis, column-major, TV elements
+    void* w;          // work vector, TV elements
+    double* H;        // Hessenberg, column-major ldh x m
+    double* h1;       // first-pass coefficients (k)
+    double* h2;       // second-pass coefficients (k)
+    double* partials; // grid partials
+    unsigned int* counter;
+    DevState* st;     // may be null (standalone use): no flags read/written
+    double* beta_out; // standalone use: |w| after the last pass
+};
+
+template <typename TV>
+int launch_gs(GsMode mode, const GsArgs& a, int grid, cudaStream_t s);
+int gs_grid_size(int n, int k, bool fp32);
+
+template <typename TV>
+int launch_normalize(int n, int j, int ldv, const TV* w, TV* V, const DevState* st,
+                     const double* inv_beta, cudaStream_t s);
+
+// ------------------------------------------------------------ expm / control
+// Raises the dynamic shared-memory limits of the expm kernels; call once
+// per device before any launch or stream capture.
+int expm_init_attributes();
+int launch_expm_standalone(int k, const double* A, int lda, double* E, int lde, int* status,
+                           cudaStream_t s);
+
+struct ControlArgs {
+    DevState* st;
+    const double* H;
+    int ldh;
+    double* coef;       // lift coefficients (k+1)
+    mexk_step_t* log;   // attempt log (log_cap entries)
+};
+int launch_controller(const ControlArgs& a, int m, cudaStream_t s);
+
+// ------------------------------------------------------------ lift / restart
+struct LiftArgs {
+    int n, ldv;
+    const void* V;
+    const double* coef;
+    double* y;
+    double* partials;
+    unsigned int* counter;
+    DevState* st;
+};
+template <typename TV>
+int launch_lift(const LiftArgs& a, int grid, cudaStream_t s);
+template <typename TV>
+int launch_restart(int n, int ldv, const double* y, TV* V, const DevState* st, cudaStream_t s);
+
+// Start vector: |v| by grid reduction, then V[:,0] = v * scale. The first
+// kernel also initialises the controller fields.
+template <typename TV>
+int launch_init_start(int n, int ldv, const double* v, TV* V, double* partials,
+                      unsigned int* counter, DevState* st, int grid, cudaStream_t s);
+
+}  // namespace mexk

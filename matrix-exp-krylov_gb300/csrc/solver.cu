@@ -1,0 +1,734 @@
+// Device context and the restarted-Arnoldi driver behind the C ABI.
+//
+// Replaces DeviceContext (reference main.cu:747-1125) and
+// ArnoldiRunner::compute_expmv (main.cu:1411-1571) for one device. The
+// reference drives every Arnoldi step from the host (about 10(j+1)+12
+// launches and 3 blocking syncs per step, H held on the host). Here a whole
+// Krylov cycle -- m x (SpMV, three Gram-Schmidt sweeps, normalise), the
+// exponential + controller, the lift and the restart -- is one CUDA graph
+// whose kernels read and write a device-resident state block, so the host
+// launches one graph per accepted step and syncs once to read `done`.
+//
+// HBM layout per context (n rows, m_alloc maximum Krylov dimension):
+//   CSR        row_ptr int32[n+1], col_idx int32[nnz], values f64[nnz]
+//              (+ f32 copy of values for the mixed-precision form)
+//   row blocks int32[nblocks+1] SpMV schedule
+//   basis V    column-major, leading dimension ldv = n rounded up to 64,
+//              m_alloc+1 columns, f64 (+ f32 basis for the mixed form)
+//   w, y       work vector (basis precision) and result (f64)
+//   H          f64 (m_alloc+1) x m_alloc column-major; h1, h2, coef f64
+//   partials   f64[4096 x RED_STRIDE] grid-reduction scratch + counter
+//   state      DevState (device) mirrored into pinned host memory
+#include "mexk_internal.cuh"
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+namespace mexk {
+
+static thread_local std::string g_err;
+
+void set_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    g_err = buf;
+}
+
+void set_error_text(const std::string& s) { g_err = s; }
+
+constexpr int PARTIAL_BLOCKS = 4096;
+constexpr int LOG_CAP = 8192;
+
+}  // namespace mexk
+
+using namespace mexk;
+
+struct GraphEntry {
+    int m, prec, reortho;
+    cudaGraphExec_t exec;
+};
+
+struct mexk_context_s {
+    int device = 0;
+    int sms = 1;
+    cudaStream_t stream = nullptr;
+    int n = 0;
+    long long nnz = 0;
+    int m_alloc = 0;
+    int ldv = 0;
+    int ldh = 0;
+    int nblocks = 0;
+    int* d_row_ptr = nullptr;
+    int* d_col = nullptr;
+    double* d_val = nullptr;
+    float* d_val32 = nullptr;
+    int* d_blocks = nullptr;
+    double* d_V = nullptr;
+    float* d_V32 = nullptr;
+    double* d_w = nullptr;
+    float* d_w32 = nullptr;
+    double* d_y = nullptr;
+    double* d_H = nullptr;
+    double* d_h1 = nullptr;
+    double* d_h2 = nullptr;
+    double* d_coef = nullptr;
+    double* d_partials = nullptr;
+    unsigned int* d_counter = nullptr;
+    DevState* d_state = nullptr;
+    DevState* h_state = nullptr;
+    mexk_step_t* d_log = nullptr;
+    bool uploaded = false;
+    bool use_graph = true;
+    std::vector<GraphEntry> graphs;
+};
+
+namespace {
+
+template <typename T>
+int dalloc(T** p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "cudaMalloc", __FILE__, __LINE__);
+        return MEXK_ERR_ALLOC;
+    }
+    return MEXK_OK;
+}
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+int check_params(const mexk_context_t ctx, const mexk_params_t* p) {
+    if (!ctx || !p) return MEXK_ERR_INVALID;
+    if (!ctx->uploaded) return MEXK_ERR_NOT_READY;
+    if (p->m < 1 || p->m > ctx->m_alloc || p->m > MEXK_M_MAX) {
+        set_error_text("Krylov dimension m out of range (1..m_alloc_max)");
+        return MEXK_ERR_INVALID;
+    }
+    // main.cu:1322-1326: m must be smaller than the number of rows.
+    if (p->m >= ctx->n) {
+        set_error_text("Requested Arnoldi m must be less than the number of rows");
+        return MEXK_ERR_INVALID;
+    }
+    if (p->precision != MEXK_PREC_FP64 && p->precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
+    return MEXK_OK;
+}
+
+int ensure_mixed(mexk_context_t ctx) {
+    if (ctx->d_V32) return MEXK_OK;
+    int rc;
+    if ((rc = dalloc(&ctx->d_V32, static_cast<size_t>(ctx->ldv) * (ctx->m_alloc + 1)))) return rc;
+    if ((rc = dalloc(&ctx->d_w32, static_cast<size_t>(ctx->ldv)))) return rc;
+    if ((rc = dalloc(&ctx->d_val32, static_cast<size_t>(ctx->nnz) + 4))) return rc;
+    // FP32 copy of the matrix values (device conversion).
+    std::vector<double> tmp;
+    // Convert on the host in slices to bound memory.
+    const size_t slice = 1u << 24;
+    std::vector<double> hv(std::min<size_t>(slice, static_cast<size_t>(ctx->nnz) + 1));
+    std::vector<float> hf(hv.size());
+    for (size_t off = 0; off < static_cast<size_t>(ctx->nnz); off += slice) {
+        const size_t cnt = std::min<size_t>(slice, static_cast<size_t>(ctx->nnz) - off);
+        MEXK_CK(cudaMemcpy(hv.data(), ctx->d_val + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < cnt; ++i) hf[i] = static_cast<float>(hv[i]);
+        MEXK_CK(cudaMemcpy(ctx->d_val32 + off, hf.data(), sizeof(float) * cnt, cudaMemcpyHostToDevice));
+    }
+    return MEXK_OK;
+}
+
+// One Krylov cycle: the unit that is captured into a graph.
+template <typename TV>
+int enqueue_cycle(mexk_context_t ctx, int m, int reortho, cudaStream_t s) {
+    const bool fp32 = sizeof(TV) == 4;
+    TV* V = fp32 ? reinterpret_cast<TV*>(ctx->d_V32) : reinterpret_cast<TV*>(ctx->d_V);
+    TV* w = fp32 ? reinterpret_cast<TV*>(ctx->d_w32) : reinterpret_cast<TV*>(ctx->d_w);
+    const TV* A = fp32 ? reinterpret_cast<const TV*>(ctx->d_val32) : reinterpret_cast<const TV*>(ctx->d_val);
+    const size_t ldv = static_cast<size_t>(ctx->ldv);
+    int rc;
+    for (int j = 0; j < m; ++j) {
+        rc = launch_spmv<TV, TV>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col, A,
+                                 V + j * ldv, w, &ctx->d_state->breakdown, s);
+        if (rc) return rc;
+        GsArgs g;
+        g.n = ctx->n;
+        g.k = j + 1;
+        g.j = j;
+        g.ldv = ctx->ldv;
+        g.ldh = ctx->ldh;
+        g.reortho = reortho;
+        g.V = V;
+        g.w = w;
+        g.H = ctx->d_H;
+        g.h1 = ctx->d_h1;
+        g.h2 = ctx->d_h2;
+        g.partials = ctx->d_partials;
+        g.counter = ctx->d_counter;
+        g.st = ctx->d_state;
+        g.beta_out = nullptr;
+        const int grid = gs_grid_size(ctx->n, j + 1, fp32);
+        if ((rc = launch_gs<TV>(GS_DOT, g, grid, s))) return rc;
+        if (reortho && (rc = launch_gs<TV>(GS_UPD_DOT, g, grid, s))) return rc;
+        if ((rc = launch_gs<TV>(GS_UPD_NORM, g, grid, s))) return rc;
+        if ((rc = launch_normalize<TV>(ctx->n, j, ctx->ldv, w, V, ctx->d_state, nullptr, s))) return rc;
+    }
+    ControlArgs c;
+    c.st = ctx->d_state;
+    c.H = ctx->d_H;
+    c.ldh = ctx->ldh;
+    c.coef = ctx->d_coef;
+    c.log = ctx->d_log;
+    if ((rc = launch_controller(c, m, s))) return rc;
+    LiftArgs l;
+    l.n = ctx->n;
+    l.ldv = ctx->ldv;
+    l.V = V;
+    l.coef = ctx->d_coef;
+    l.y = ctx->d_y;
+    l.partials = ctx->d_partials;
+    l.counter = ctx->d_counter;
+    l.st = ctx->d_state;
+    if ((rc = launch_lift<TV>(l, gs_grid_size(ctx->n, 1, false), s))) return rc;
+    return launch_restart<TV>(ctx->n, ctx->ldv, ctx->d_y, V, ctx->d_state, s);
+}
+
+int enqueue_cycle_any(mexk_context_t ctx, int m, int prec, int reortho, cudaStream_t s) {
+    return prec == MEXK_PREC_MIXED ? enqueue_cycle<float>(ctx, m, reortho, s)
+                                   : enqueue_cycle<double>(ctx, m, reortho, s);
+}
+
+int get_graph(mexk_context_t ctx, int m, int prec, int reortho, cudaGraphExec_t* out) {
+    for (auto& g : ctx->graphs) {
+        if (g.m == m && g.prec == prec && g.reortho == reortho) {
+            *out = g.exec;
+            return MEXK_OK;
+        }
+    }
+    cudaGraph_t graph = nullptr;
+    MEXK_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_cycle_any(ctx, m, prec, reortho, ctx->stream);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (rc != MEXK_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
+    ctx->graphs.push_back({m, prec, reortho, exec});
+    *out = exec;
+    return MEXK_OK;
+}
+
+void init_state(DevState* st, const mexk_params_t* p, int log_cap) {
+    memset(st, 0, sizeof(*st));
+    // ArnoldiRunner constructor (main.cu:1292-1305).
+    st->total_t = p->t;
+    st->dt_max = p->t;
+    st->dt_min = std::max(1e-12, p->t * 1e-6);
+    const double denom = (p->max_restarts > 0) ? p->max_restarts : 1;
+    const double dt_init = p->t / denom;
+    st->tol = p->tol;
+    st->max_steps = (p->max_restarts > 0) ? p->max_restarts : 1000;
+    st->max_rejects = 20;
+    st->m = p->m;
+    // compute_expmv (main.cu:1426-1434): clamp, then the first outer iteration's min.
+    double dt = std::min(std::max(dt_init, st->dt_min), st->dt_max);
+    st->t_done = 0.0;
+    st->done = !(st->t_done < st->total_t && 0 < st->max_steps);
+    dt = std::min(dt, st->total_t - st->t_done);
+    st->dt = dt;
+    st->k_used = p->m;
+    st->log_cap = log_cap;
+}
+
+int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, double* y_dev, cudaStream_t s,
+          mexk_result_t* result) {
+    int rc = check_params(ctx, p);
+    if (rc) return rc;
+    if (p->precision == MEXK_PREC_MIXED && (rc = ensure_mixed(ctx))) return rc;
+    if (s == nullptr) s = ctx->stream;
+    init_state(ctx->h_state, p, LOG_CAP);
+    MEXK_CK(cudaMemcpyAsync(ctx->d_state, ctx->h_state, sizeof(DevState), cudaMemcpyHostToDevice, s));
+    if (ctx->h_state->done) {
+        // The reference never lifts when no step runs: y stays zero (main_cpu.cpp:467).
+        MEXK_CK(cudaMemsetAsync(ctx->d_y, 0, sizeof(double) * ctx->n, s));
+    } else {
+        const int grid = gs_grid_size(ctx->n, 1, false);
+        if (p->precision == MEXK_PREC_MIXED)
+            rc = launch_init_start<float>(ctx->n, ctx->ldv, v_dev, ctx->d_V32, ctx->d_partials, ctx->d_counter,
+                                          ctx->d_state, grid, s);
+        else
+            rc = launch_init_start<double>(ctx->n, ctx->ldv, v_dev, ctx->d_V, ctx->d_partials, ctx->d_counter,
+                                           ctx->d_state, grid, s);
+        if (rc) return rc;
+        cudaGraphExec_t exec = nullptr;
+        if (ctx->use_graph) {
+            // Capture happens on the context stream; order it after `s`.
+            if (s != ctx->stream) MEXK_CK(cudaStreamSynchronize(s));
+            if ((rc = get_graph(ctx, p->m, p->precision, p->reorthogonalize ? 1 : 0, &exec))) return rc;
+        }
+        // Every cycle ends with an accepted step or an abort, so the loop is
+        // bounded by max_steps; the extra margin only guards corrupt state.
+        const int max_cycles = ctx->h_state->max_steps + 2;
+        for (int cyc = 0; cyc < max_cycles; ++cyc) {
+            if (exec) {
+                MEXK_CK(cudaGraphLaunch(exec, s));
+            } else if ((rc = enqueue_cycle_any(ctx, p->m, p->precision, p->reorthogonalize ? 1 : 0, s))) {
+                return rc;
+            }
+            MEXK_CK(cudaMemcpyAsync(ctx->h_state, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+            MEXK_CK(cudaStreamSynchronize(s));
+            if (ctx->h_state->done) break;
+        }
+        if (!ctx->h_state->done) {
+            set_error_text("solve did not finish within max_steps cycles");
+            return MEXK_ERR_DEVICE;
+        }
+    }
+    if (y_dev != ctx->d_y)
+        MEXK_CK(cudaMemcpyAsync(y_dev, ctx->d_y, sizeof(double) * ctx->n, cudaMemcpyDeviceToDevice, s));
+    MEXK_CK(cudaMemcpyAsync(ctx->h_state, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    MEXK_CK(cudaStreamSynchronize(s));
+    const DevState* st = ctx->h_state;
+    if (result) {
+        result->converged = st->converged;
+        result->restarts_done = st->accepted;
+        result->last_residual = st->last_residual;
+        result->attempts = st->attempts;
+        result->cycles = st->cycles;
+        result->spmv_count = st->spmv_count;
+        result->t_done = st->t_done;
+        result->status = st->status;
+    }
+    return MEXK_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* mexk_error_string(int code) {
+    switch (code) {
+        case MEXK_OK: return "ok";
+        case MEXK_ERR_INVALID: return "invalid argument";
+        case MEXK_ERR_CUDA: return "CUDA runtime error";
+        case MEXK_ERR_ALLOC: return "allocation failed";
+        case MEXK_ERR_NOT_READY: return "context not ready (upload the matrix first)";
+        case MEXK_ERR_DEVICE: return "device reported a failure";
+        case MEXK_ERR_UNSUPPORTED: return "unsupported request";
+    }
+    return "unknown error";
+}
+
+const char* mexk_last_error_detail(void) { return g_err.c_str(); }
+
+const char* mexk_version(void) { return "mexk 0.1 sm_103a"; }
+
+int mexk_device_count(int* count) {
+    if (!count) return MEXK_ERR_INVALID;
+    *count = 0;
+    MEXK_CK(cudaGetDeviceCount(count));
+    return MEXK_OK;
+}
+
+int mexk_context_create(int device, mexk_context_t* out) {
+    if (!out) return MEXK_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    MEXK_CK(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(device));
+    mexk_context_t c = new mexk_context_s();
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    const char* ng = getenv("MEXK_NO_GRAPH");
+    c->use_graph = !(ng && ng[0] == '1');
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "cudaStreamCreate", __FILE__, __LINE__);
+        delete c;
+        return MEXK_ERR_CUDA;
+    }
+    int rc = expm_init_attributes();
+    if (rc) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return MEXK_OK;
+}
+
+int mexk_context_upload_csr(mexk_context_t ctx, int rows, long long nnz, const int* row_ptr, const int* col_idx,
+                            const double* values, int m_alloc_max) {
+    if (!ctx || rows < 1 || nnz < 0 || !row_ptr || (nnz > 0 && (!col_idx || !values))) return MEXK_ERR_INVALID;
+    if (ctx->uploaded) return MEXK_ERR_NOT_READY;
+    if (m_alloc_max < 1 || m_alloc_max > MEXK_M_MAX) return MEXK_ERR_INVALID;
+    if (row_ptr[0] != 0 || row_ptr[rows] != nnz) {
+        set_error_text("row_ptr must start at 0 and end at nnz");
+        return MEXK_ERR_INVALID;
+    }
+    for (int r = 0; r < rows; ++r)
+        if (row_ptr[r] > row_ptr[r + 1]) {
+            set_error_text("row_ptr must be non-decreasing");
+            return MEXK_ERR_INVALID;
+        }
+    for (long long e = 0; e < nnz; ++e)
+        if (col_idx[e] < 0 || col_idx[e] >= rows) {
+            set_error_text("column index out of range");
+            return MEXK_ERR_INVALID;
+        }
+    MEXK_CK(cudaSetDevice(ctx->device));
+    ctx->n = rows;
+    ctx->nnz = nnz;
+    ctx->m_alloc = m_alloc_max;
+    ctx->ldv = (rows + 63) / 64 * 64;
+    ctx->ldh = m_alloc_max + 1;
+    int rc;
+    if ((rc = dalloc(&ctx->d_row_ptr, rows + 1))) return rc;
+    if ((rc = dalloc(&ctx->d_col, static_cast<size_t>(nnz) + 4))) return rc;
+    if ((rc = dalloc(&ctx->d_val, static_cast<size_t>(nnz) + 4))) return rc;
+    MEXK_CK(cudaMemcpy(ctx->d_row_ptr, row_ptr, sizeof(int) * (rows + 1), cudaMemcpyHostToDevice));
+    if (nnz > 0) {
+        MEXK_CK(cudaMemcpy(ctx->d_col, col_idx, sizeof(int) * nnz, cudaMemcpyHostToDevice));
+        MEXK_CK(cudaMemcpy(ctx->d_val, values, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+    }
+    std::vector<int> blocks = build_row_blocks(rows, row_ptr);
+    ctx->nblocks = static_cast<int>(blocks.size()) - 1;
+    if ((rc = dalloc(&ctx->d_blocks, blocks.size()))) return rc;
+    MEXK_CK(cudaMemcpy(ctx->d_blocks, blocks.data(), sizeof(int) * blocks.size(), cudaMemcpyHostToDevice));
+    const size_t vcount = static_cast<size_t>(ctx->ldv) * (m_alloc_max + 1);
+    if ((rc = dalloc(&ctx->d_V, vcount))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_V, 0, sizeof(double) * vcount));
+    if ((rc = dalloc(&ctx->d_w, ctx->ldv))) return rc;
+    if ((rc = dalloc(&ctx->d_y, ctx->ldv))) return rc;
+    const size_t hcount = static_cast<size_t>(ctx->ldh) * m_alloc_max;
+    if ((rc = dalloc(&ctx->d_H, hcount))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_H, 0, sizeof(double) * hcount));
+    if ((rc = dalloc(&ctx->d_h1, MEXK_M_MAX + 2))) return rc;
+    if ((rc = dalloc(&ctx->d_h2, MEXK_M_MAX + 2))) return rc;
+    if ((rc = dalloc(&ctx->d_coef, MEXK_M_MAX + 2))) return rc;
+    if ((rc = dalloc(&ctx->d_partials, static_cast<size_t>(PARTIAL_BLOCKS) * RED_STRIDE))) return rc;
+    if ((rc = dalloc(&ctx->d_counter, 4))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_counter, 0, sizeof(unsigned int) * 4));
+    if ((rc = dalloc(&ctx->d_state, 1))) return rc;
+    if ((rc = dalloc(&ctx->d_log, LOG_CAP))) return rc;
+    cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&ctx->h_state), sizeof(DevState));
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "cudaMallocHost", __FILE__, __LINE__);
+        return MEXK_ERR_ALLOC;
+    }
+    memset(ctx->h_state, 0, sizeof(DevState));
+    MEXK_CK(cudaMemcpy(ctx->d_state, ctx->h_state, sizeof(DevState), cudaMemcpyHostToDevice));
+    ctx->uploaded = true;
+    return MEXK_OK;
+}
+
+int mexk_context_destroy(mexk_context_t ctx) {
+    if (!ctx) return MEXK_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto& g : ctx->graphs) cudaGraphExecDestroy(g.exec);
+    dfree(ctx->d_row_ptr);
+    dfree(ctx->d_col);
+    dfree(ctx->d_val);
+    dfree(ctx->d_val32);
+    dfree(ctx->d_blocks);
+    dfree(ctx->d_V);
+    dfree(ctx->d_V32);
+    dfree(ctx->d_w);
+    dfree(ctx->d_w32);
+    dfree(ctx->d_y);
+    dfree(ctx->d_H);
+    dfree(ctx->d_h1);
+    dfree(ctx->d_h2);
+    dfree(ctx->d_coef);
+    dfree(ctx->d_partials);
+    dfree(ctx->d_counter);
+    dfree(ctx->d_state);
+    dfree(ctx->d_log);
+    if (ctx->h_state) cudaFreeHost(ctx->h_state);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MEXK_OK;
+}
+
+void* mexk_context_stream(mexk_context_t ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+
+int mexk_expmv_device(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, double* y_dev,
+                      void* stream, mexk_result_t* result) {
+    if (!ctx || !v_dev || !y_dev) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    return solve(ctx, p, v_dev, y_dev, static_cast<cudaStream_t>(stream), result);
+}
+
+int mexk_expmv(mexk_context_t ctx, const mexk_params_t* p, const double* v_host, double* y_host,
+               mexk_result_t* result) {
+    if (!ctx || !v_host || !y_host) return MEXK_ERR_INVALID;
+    int rc = check_params(ctx, p);
+    if (rc) return rc;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    const size_t bytes = sizeof(double) * ctx->n;
+    // v goes through the work vector slot w (FP64, length >= n) as staging.
+    MEXK_CK(cudaMemcpyAsync(ctx->d_w, v_host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    // The start-vector kernels read v before any cycle overwrites w.
+    rc = solve(ctx, p, ctx->d_w, ctx->d_y, ctx->stream, result);
+    if (rc) return rc;
+    MEXK_CK(cudaMemcpyAsync(y_host, ctx->d_y, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    MEXK_CK(cudaStreamSynchronize(ctx->stream));
+    return MEXK_OK;
+}
+
+int mexk_get_steps(mexk_context_t ctx, mexk_step_t* steps, int cap, int* count) {
+    if (!ctx || !ctx->uploaded || cap < 0 || (cap > 0 && !steps)) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    const int avail = std::min(ctx->h_state->nlog, LOG_CAP);
+    if (count) *count = ctx->h_state->nlog;
+    const int ncopy = std::min(avail, cap);
+    if (ncopy > 0)
+        MEXK_CK(cudaMemcpy(steps, ctx->d_log, sizeof(mexk_step_t) * ncopy, cudaMemcpyDeviceToHost));
+    return MEXK_OK;
+}
+
+int mexk_context_set_basis(mexk_context_t ctx, int precision, const double* V_host, int ncols) {
+    if (!ctx || !ctx->uploaded || !V_host || ncols < 1 || ncols > ctx->m_alloc + 1) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    const size_t n = static_cast<size_t>(ctx->n);
+    if (precision == MEXK_PREC_FP64) {
+        MEXK_CK(cudaMemcpy2D(ctx->d_V, sizeof(double) * ctx->ldv, V_host, sizeof(double) * n, sizeof(double) * n,
+                             ncols, cudaMemcpyHostToDevice));
+        return MEXK_OK;
+    }
+    int rc = ensure_mixed(ctx);
+    if (rc) return rc;
+    std::vector<float> f(n * ncols);
+    for (size_t i = 0; i < f.size(); ++i) f[i] = static_cast<float>(V_host[i]);
+    MEXK_CK(cudaMemcpy2D(ctx->d_V32, sizeof(float) * ctx->ldv, f.data(), sizeof(float) * n, sizeof(float) * n,
+                         ncols, cudaMemcpyHostToDevice));
+    return MEXK_OK;
+}
+
+int mexk_context_get_basis(mexk_context_t ctx, int precision, double* V_host, int ncols) {
+    if (!ctx || !ctx->uploaded || !V_host || ncols < 1 || ncols > ctx->m_alloc + 1) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    const size_t n = static_cast<size_t>(ctx->n);
+    if (precision == MEXK_PREC_FP64) {
+        MEXK_CK(cudaMemcpy2D(V_host, sizeof(double) * n, ctx->d_V, sizeof(double) * ctx->ldv, sizeof(double) * n,
+                             ncols, cudaMemcpyDeviceToHost));
+        return MEXK_OK;
+    }
+    if (!ctx->d_V32) return MEXK_ERR_NOT_READY;
+    std::vector<float> f(n * ncols);
+    MEXK_CK(cudaMemcpy2D(f.data(), sizeof(float) * n, ctx->d_V32, sizeof(float) * ctx->ldv, sizeof(float) * n,
+                         ncols, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < f.size(); ++i) V_host[i] = static_cast<double>(f[i]);
+    return MEXK_OK;
+}
+
+int mexk_arnoldi_step(mexk_context_t ctx, int j, int reorthogonalize, int precision, double* h, double* beta,
+                      int* ok) {
+    if (!ctx || !ctx->uploaded || !h || !beta || !ok) return MEXK_ERR_INVALID;
+    if (j < 0 || j >= ctx->m_alloc) return MEXK_ERR_INVALID;
+    if (precision != MEXK_PREC_FP64 && precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    int rc;
+    if (precision == MEXK_PREC_MIXED && (rc = ensure_mixed(ctx))) return rc;
+    cudaStream_t s = ctx->stream;
+    DevState* hs = ctx->h_state;
+    memset(hs, 0, sizeof(DevState));
+    hs->m = ctx->m_alloc;
+    hs->k_used = ctx->m_alloc;
+    MEXK_CK(cudaMemcpyAsync(ctx->d_state, hs, sizeof(DevState), cudaMemcpyHostToDevice, s));
+    const bool fp32 = precision == MEXK_PREC_MIXED;
+    GsArgs g;
+    g.n = ctx->n;
+    g.k = j + 1;
+    g.j = j;
+    g.ldv = ctx->ldv;
+    g.ldh = ctx->ldh;
+    g.reortho = reorthogonalize ? 1 : 0;
+    g.H = ctx->d_H;
+    g.h1 = ctx->d_h1;
+    g.h2 = ctx->d_h2;
+    g.partials = ctx->d_partials;
+    g.counter = ctx->d_counter;
+    g.st = ctx->d_state;
+    g.beta_out = nullptr;
+    const int grid = gs_grid_size(ctx->n, j + 1, fp32);
+    const size_t ldv = static_cast<size_t>(ctx->ldv);
+    if (fp32) {
+        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
+                                            ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr, s)))
+            return rc;
+        g.V = ctx->d_V32;
+        g.w = ctx->d_w32;
+        if ((rc = launch_gs<float>(GS_DOT, g, grid, s))) return rc;
+        if (g.reortho && (rc = launch_gs<float>(GS_UPD_DOT, g, grid, s))) return rc;
+        if ((rc = launch_gs<float>(GS_UPD_NORM, g, grid, s))) return rc;
+        if ((rc = launch_normalize<float>(ctx->n, j, ctx->ldv, ctx->d_w32, ctx->d_V32, ctx->d_state, nullptr, s)))
+            return rc;
+    } else {
+        if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
+                                              ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, nullptr, s)))
+            return rc;
+        g.V = ctx->d_V;
+        g.w = ctx->d_w;
+        if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
+        if (g.reortho && (rc = launch_gs<double>(GS_UPD_DOT, g, grid, s))) return rc;
+        if ((rc = launch_gs<double>(GS_UPD_NORM, g, grid, s))) return rc;
+        if ((rc = launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s)))
+            return rc;
+    }
+    std::vector<double> col(static_cast<size_t>(ctx->ldh));
+    MEXK_CK(cudaMemcpyAsync(col.data(), ctx->d_H + static_cast<size_t>(j) * ctx->ldh, sizeof(double) * ctx->ldh,
+                            cudaMemcpyDeviceToHost, s));
+    MEXK_CK(cudaMemcpyAsync(hs, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    MEXK_CK(cudaStreamSynchronize(s));
+    for (int i = 0; i <= j; ++i) h[i] = col[i];
+    *beta = col[j + 1];
+    *ok = hs->breakdown ? 0 : 1;
+    return MEXK_OK;
+}
+
+int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int iters, double* ms_per_launch) {
+    if (!ctx || !ctx->uploaded || !ms_per_launch || iters < 1) return MEXK_ERR_INVALID;
+    if (kind < 0 || kind >= MEXK_KERNEL_KINDS || j < 0 || j >= ctx->m_alloc) return MEXK_ERR_INVALID;
+    if (precision != MEXK_PREC_FP64 && precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    int rc;
+    if (precision == MEXK_PREC_MIXED && (rc = ensure_mixed(ctx))) return rc;
+    const bool fp32 = precision == MEXK_PREC_MIXED;
+    cudaStream_t s = ctx->stream;
+    // A running state: k = j+1 basis columns, lift pending, nothing finished.
+    DevState run;
+    memset(&run, 0, sizeof(run));
+    run.total_t = 1.0;
+    run.dt = 1e-3;
+    run.dt_max = 1.0;
+    run.dt_min = 1e-12;
+    run.tol = 1e-6;
+    run.v_norm = 1.0;
+    run.m = j + 1;
+    run.max_steps = 1 << 30;
+    run.max_rejects = 20;
+    run.k_used = j + 1;
+    run.k_lift = j + 1;
+    run.lift = 1;
+    run.inv_beta = 1.0;
+    run.log_cap = 0;
+    DevState* h_run = nullptr;
+    MEXK_CK(cudaMallocHost(reinterpret_cast<void**>(&h_run), sizeof(DevState)));
+    *h_run = run;
+    cudaEvent_t e0, e1;
+    MEXK_CK(cudaEventCreate(&e0));
+    MEXK_CK(cudaEventCreate(&e1));
+    const size_t ldv = static_cast<size_t>(ctx->ldv);
+    GsArgs g;
+    g.n = ctx->n;
+    g.k = j + 1;
+    g.j = j;
+    g.ldv = ctx->ldv;
+    g.ldh = ctx->ldh;
+    g.reortho = 1;
+    g.V = fp32 ? static_cast<const void*>(ctx->d_V32) : static_cast<const void*>(ctx->d_V);
+    g.w = fp32 ? static_cast<void*>(ctx->d_w32) : static_cast<void*>(ctx->d_w);
+    g.H = ctx->d_H;
+    g.h1 = ctx->d_h1;
+    g.h2 = ctx->d_h2;
+    g.partials = ctx->d_partials;
+    g.counter = ctx->d_counter;
+    g.st = ctx->d_state;
+    g.beta_out = nullptr;
+    const int grid = gs_grid_size(ctx->n, j + 1, fp32);
+    double total = 0.0;
+    rc = MEXK_OK;
+    for (int it = 0; it < iters && rc == MEXK_OK; ++it) {
+        cudaError_t ce = cudaMemcpyAsync(ctx->d_state, h_run, sizeof(DevState), cudaMemcpyHostToDevice, s);
+        if (ce == cudaSuccess) ce = cudaEventRecord(e0, s);
+        if (ce != cudaSuccess) {
+            set_cuda_error(ce, "profile setup", __FILE__, __LINE__);
+            rc = MEXK_ERR_CUDA;
+            break;
+        }
+        switch (kind) {
+            case MEXK_KERNEL_SPMV:
+                rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
+                                                      ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr, s)
+                          : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr,
+                                                        ctx->d_col, ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, nullptr,
+                                                        s);
+                break;
+            case MEXK_KERNEL_GS_DOT:
+            case MEXK_KERNEL_GS_UPD_DOT:
+            case MEXK_KERNEL_GS_UPD_NORM: {
+                const GsMode mode = kind == MEXK_KERNEL_GS_DOT ? GS_DOT
+                                    : kind == MEXK_KERNEL_GS_UPD_DOT ? GS_UPD_DOT
+                                                                       : GS_UPD_NORM;
+                rc = fp32 ? launch_gs<float>(mode, g, grid, s) : launch_gs<double>(mode, g, grid, s);
+                break;
+            }
+            case MEXK_KERNEL_NORMALIZE:
+                rc = fp32 ? launch_normalize<float>(ctx->n, j, ctx->ldv, ctx->d_w32, ctx->d_V32, ctx->d_state, nullptr, s)
+                          : launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s);
+                break;
+            case MEXK_KERNEL_LIFT: {
+                LiftArgs l;
+                l.n = ctx->n;
+                l.ldv = ctx->ldv;
+                l.V = g.V;
+                l.coef = ctx->d_coef;
+                l.y = ctx->d_y;
+                l.partials = ctx->d_partials;
+                l.counter = ctx->d_counter;
+                l.st = ctx->d_state;
+                rc = fp32 ? launch_lift<float>(l, gs_grid_size(ctx->n, 1, false), s)
+                          : launch_lift<double>(l, gs_grid_size(ctx->n, 1, false), s);
+                break;
+            }
+            case MEXK_KERNEL_CONTROLLER: {
+                ControlArgs c;
+                c.st = ctx->d_state;
+                c.H = ctx->d_H;
+                c.ldh = ctx->ldh;
+                c.coef = ctx->d_coef;
+                c.log = nullptr;
+                rc = launch_controller(c, j + 1, s);
+                break;
+            }
+        }
+        if (rc != MEXK_OK) break;
+        ce = cudaEventRecord(e1, s);
+        if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+        if (ce != cudaSuccess) {
+            set_cuda_error(ce, "profile timing", __FILE__, __LINE__);
+            rc = MEXK_ERR_CUDA;
+            break;
+        }
+        total += ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeHost(h_run);
+    if (rc == MEXK_OK) *ms_per_launch = total / iters;
+    return rc;
+}
+
+}  // extern "C"

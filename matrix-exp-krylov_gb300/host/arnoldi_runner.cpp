@@ -1,0 +1,171 @@
+// DeviceContext and ArnoldiRunner on top of the mexk C ABI.
+//
+// Mirrors the reference classes (kol-di/matrix-exp-krylov main.cu:747-1125
+// and 1253-2081) for one device. compute_expmv hands the whole solve to
+// mexk_expmv, then prints the attempt log in the reference's [STEP] format,
+// the [FLOPs] model (main.cu:1539-1565) and the METRIC line.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <iostream>
+#include <vector>
+
+#include "matrix_exp_krylov.hpp"
+
+namespace {
+
+[[noreturn]] void die(const char* what, int rc) {
+    std::cerr << "mexk Error: " << what << ": " << mexk_error_string(rc);
+    const char* d = mexk_last_error_detail();
+    if (d && d[0]) std::cerr << " (" << d << ")";
+    std::cerr << std::endl;
+    std::exit(EXIT_FAILURE);
+}
+
+}  // namespace
+
+void DeviceContext::init_handles() {}
+
+void DeviceContext::create_streams() {
+    if (handle) return;
+    int rc = mexk_context_create(device_id, &handle);
+    if (rc != MEXK_OK) die("mexk_context_create", rc);
+}
+
+void DeviceContext::alloc_from(const CSRHost& part, int global_cols, int m_alloc_max) {
+    (void)global_cols;
+    if (!handle) create_streams();
+    local_rows = part.rows;
+    local_nnz = static_cast<int>(part.nnz);
+    std::cout << "GPU " << device_id << " allocating: local_rows=" << local_rows << ", local_nnz=" << local_nnz
+              << std::endl;
+    allocated_m_max = std::max(1, std::min(m_alloc_max, MEXK_M_MAX));
+    int rc = mexk_context_upload_csr(handle, part.rows, part.nnz, part.row_ptr.data(), part.col_idx.data(),
+                                     part.values.data(), allocated_m_max);
+    if (rc != MEXK_OK) die("mexk_context_upload_csr", rc);
+}
+
+void DeviceContext::create_descriptors(const CSRHost&, int, const CSRHost::GhostMap&, int, int) {}
+
+void DeviceContext::destroy() {
+    if (handle) mexk_context_destroy(handle);
+    handle = nullptr;
+}
+
+ArnoldiRunner::ArnoldiRunner(int n_gpus, const ArnoldiParams& arnoldi_params, int total_rows, int total_cols,
+                             long long total_nnz)
+    : num_gpus(n_gpus), params(arnoldi_params), global_rows(total_rows), global_cols(total_cols),
+      global_nnz(total_nnz) {
+    device_contexts.reserve(static_cast<size_t>(std::max(1, num_gpus)));
+    for (int i = 0; i < std::max(1, num_gpus); ++i) device_contexts.emplace_back(i);
+    // Derived time-stepping parameters (main.cu:1292-1305); the device
+    // controller computes the same values from ArnoldiParams.
+    ts_params.dt_max = params.t;
+    ts_params.dt_min = std::max(1e-12, params.t * 1e-6);
+    const double denom = (params.max_restarts > 0) ? params.max_restarts : 1;
+    ts_params.dt_init = params.t / denom;
+    ts_params.tol_step = params.tol;
+    ts_params.max_steps = (params.max_restarts > 0) ? params.max_restarts : 1000;
+    ts_params.max_rejects = 20;
+    ts_params.safety = 0.8;
+    ts_params.grow = 1.5;
+    ts_params.shrink = 0.5;
+    ts_params.adapt_m = false;
+    ts_params.m_max = params.m;
+    ts_params.m_step = 0;
+}
+
+void ArnoldiRunner::init_all_devices(const std::vector<CSRHost>& partitions, const std::vector<int>& device_ids,
+                                     const std::vector<CSRHost::GhostMap>& ghost_maps_in) {
+    ghost_maps = ghost_maps_in;
+    if (static_cast<int>(device_ids.size()) != num_gpus) {
+        std::cerr << "ERROR: device_ids size (" << device_ids.size() << ") must match num_gpus (" << num_gpus << ")"
+                  << std::endl;
+        std::exit(EXIT_FAILURE);
+    }
+    if (params.m >= global_rows) {
+        std::cerr << "ERROR: Requested Arnoldi m=" << params.m << " must be less than global_rows=" << global_rows
+                  << std::endl;
+        std::exit(EXIT_FAILURE);
+    }
+    if (global_rows != global_cols) {
+        std::cerr << "ERROR: Matrix must be square. rows=" << global_rows << " cols=" << global_cols << std::endl;
+        std::exit(EXIT_FAILURE);
+    }
+    if (params.m > MEXK_M_MAX) {
+        std::cerr << "ERROR: Requested Arnoldi m=" << params.m << " exceeds the supported maximum " << MEXK_M_MAX
+                  << std::endl;
+        std::exit(EXIT_FAILURE);
+    }
+    // Row partitions hold global column indices: stacking them restores A.
+    CSRHost full;
+    full.rows = 0;
+    full.cols = global_cols;
+    full.row_ptr.assign(1, 0);
+    for (const CSRHost& p : partitions) {
+        const int base = full.row_ptr.back();
+        for (int r = 0; r < p.rows; ++r) full.row_ptr.push_back(base + p.row_ptr[r + 1]);
+        full.col_idx.insert(full.col_idx.end(), p.col_idx.begin(), p.col_idx.begin() + p.nnz);
+        full.values.insert(full.values.end(), p.values.begin(), p.values.begin() + p.nnz);
+        full.rows += p.rows;
+    }
+    full.nnz = static_cast<long long>(full.col_idx.size());
+    DeviceContext& dc = device_contexts[0];
+    dc.device_id = device_ids.empty() ? 0 : device_ids[0];
+    dc.init_handles();
+    dc.create_streams();
+    const int alloc_m = std::max(params.m, ts_params.m_max > 0 ? ts_params.m_max : params.m);
+    dc.alloc_from(full, global_cols, alloc_m);
+    dc.create_descriptors(full, global_cols, CSRHost::GhostMap(), 0, alloc_m);
+}
+
+void ArnoldiRunner::compute_expmv(const std::vector<double>& v_host, std::vector<double>& y_host) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (mode != ExpmvMode::AdaptiveTimeStepping) {
+        std::cerr << "Expmv mode not implemented" << std::endl;
+        return;
+    }
+    DeviceContext& dc = device_contexts[0];
+    mexk_params_t p;
+    p.m = params.m;
+    p.t = params.t;
+    p.tol = params.tol;
+    p.max_restarts = params.max_restarts;
+    p.reorthogonalize = params.reorthogonalize ? 1 : 0;
+    p.precision = precision;
+    int rc = mexk_expmv(dc.handle, &p, v_host.data(), y_host.data(), &last_result);
+    if (rc != MEXK_OK) die("mexk_expmv", rc);
+    converged = last_result.converged != 0;
+    restarts_done = last_result.restarts_done;
+    last_residual = last_result.last_residual;
+    int count = 0;
+    mexk_get_steps(dc.handle, nullptr, 0, &count);
+    last_steps.resize(static_cast<size_t>(count));
+    if (count > 0) mexk_get_steps(dc.handle, last_steps.data(), count, &count);
+    if (verbose) {
+        for (const mexk_step_t& s : last_steps)
+            std::cout << "[STEP] t=" << s.t_done << " dt=" << s.dt << " err=" << s.err << " m_used=" << s.m_used
+                      << " accepts=" << s.accepts << " rejects=" << s.rejects << std::endl;
+        // An abort (20 rejects) is the only way to finish unconverged at t_done = t.
+        if (!converged && last_result.t_done >= params.t && params.t > 0)
+            std::cerr << "[STEP] rejected too many times, aborting" << std::endl;
+        const double N = static_cast<double>(global_rows);
+        const double nnz = static_cast<double>(global_nnz);
+        const double m = static_cast<double>(params.m);
+        const double S = static_cast<double>(restarts_done);
+        const double seg = 2.0 * nnz * m + 4.0 * N * m * (m + 1.0) + 5.0 * N * m + 2.0 * N;
+        const double gpu_total = 3.0 * N * S + S * seg;
+        const double cpu_seg = 2.0 * 1.0 * m * m * m + 2.0 * m * m;
+        std::cout << "[FLOPs] N=" << N << " nnz=" << nnz << " m=" << m << " steps=" << S << std::endl;
+        std::cout << "[FLOPs] GPU segment: " << seg << " | GPU total: " << gpu_total << std::endl;
+        std::cout << "[FLOPs] CPU segment: " << cpu_seg << " | CPU total: " << S * cpu_seg << " (C_exp=" << 1.0 << ")"
+                  << std::endl;
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        std::cout << "METRIC total_compute_expmv_ms=" << ms << std::endl;
+    }
+}
+
+void ArnoldiRunner::destroy() {
+    for (DeviceContext& dc : device_contexts) dc.destroy();
+}

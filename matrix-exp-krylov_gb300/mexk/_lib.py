@@ -1,0 +1,107 @@
+"""ctypes binding of the mexk C ABI (include/mexk.h).
+
+Loads ``_build/libmexk.so`` (built in-tree by ``mexk.build`` /
+``__graft_entry__.build()``). There is no fallback: if the library is
+missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ROOT = os.path.dirname(PKG)
+BUILD = os.path.join(PKG, "_build")
+LIB_PATH = os.path.join(BUILD, "libmexk.so")
+HOST_LIB_PATH = os.path.join(BUILD, "libmexk_host.so")
+HEADER = os.path.join(ROOT, "include", "mexk.h")
+
+MEXK_OK = 0
+PREC_FP64 = 0
+PREC_MIXED = 1
+M_MAX = 64
+
+
+class MexkError(RuntimeError):
+    pass
+
+
+class Params(C.Structure):
+    _fields_ = [("m", C.c_int), ("t", C.c_double), ("tol", C.c_double), ("max_restarts", C.c_int),
+                ("reorthogonalize", C.c_int), ("precision", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("converged", C.c_int), ("restarts_done", C.c_int), ("last_residual", C.c_double),
+                ("attempts", C.c_int), ("cycles", C.c_int), ("spmv_count", C.c_longlong),
+                ("t_done", C.c_double), ("status", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Step(C.Structure):
+    _fields_ = [("t_done", C.c_double), ("dt", C.c_double), ("err", C.c_double), ("m_used", C.c_int),
+                ("accepts", C.c_int), ("rejects", C.c_int)]
+
+
+_VP = C.c_void_p
+_IP = C.POINTER(C.c_int)
+_DP = C.POINTER(C.c_double)
+
+_PROTOS = {
+    "mexk_error_string": ([C.c_int], C.c_char_p),
+    "mexk_last_error_detail": ([], C.c_char_p),
+    "mexk_version": ([], C.c_char_p),
+    "mexk_device_count": ([_IP], C.c_int),
+    "mexk_context_create": ([C.c_int, C.POINTER(_VP)], C.c_int),
+    "mexk_context_upload_csr": ([_VP, C.c_int, C.c_longlong, _IP, _IP, _DP, C.c_int], C.c_int),
+    "mexk_context_destroy": ([_VP], C.c_int),
+    "mexk_context_stream": ([_VP], _VP),
+    "mexk_expmv": ([_VP, C.POINTER(Params), _DP, _DP, C.POINTER(Result)], C.c_int),
+    "mexk_expmv_device": ([_VP, C.POINTER(Params), _VP, _VP, _VP, C.POINTER(Result)], C.c_int),
+    "mexk_get_steps": ([_VP, C.POINTER(Step), C.c_int, _IP], C.c_int),
+    "mexk_spmv_f64": ([C.c_int, _VP, _VP, _VP, _VP, _VP, _VP], C.c_int),
+    "mexk_spmv_f32": ([C.c_int, _VP, _VP, _VP, _VP, _VP, _VP], C.c_int),
+    "mexk_arnoldi_step": ([_VP, C.c_int, C.c_int, C.c_int, _DP, _DP, _IP], C.c_int),
+    "mexk_context_set_basis": ([_VP, C.c_int, _DP, C.c_int], C.c_int),
+    "mexk_context_get_basis": ([_VP, C.c_int, _DP, C.c_int], C.c_int),
+    "mexk_expm_f64": ([C.c_int, _VP, C.c_int, _VP, C.c_int, _VP], C.c_int),
+    "mexk_profile_kernel": ([_VP, C.c_int, C.c_int, C.c_int, C.c_int, _DP], C.c_int),
+}
+
+KERNELS = {"spmv": 0, "gs_dot": 1, "gs_upd_dot": 2, "gs_upd_norm": 3, "normalize": 4, "lift": 5, "controller": 6}
+
+_lib = None
+
+
+def header_functions(path: str = HEADER):
+    """Names of the functions declared in a C header."""
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(mexk_\w+)\s*\(", text, flags=re.M)))
+
+
+def lib():
+    """The loaded libmexk.so; raises MexkError when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise MexkError(f"CUDA library {LIB_PATH} is not built; run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (args, res) in _PROTOS.items():
+            if hasattr(L, name):
+                f = getattr(L, name)
+                f.argtypes = args
+                f.restype = res
+        _lib = L
+    return _lib
+
+
+def check(rc: int, what: str = "mexk call") -> None:
+    if rc != MEXK_OK:
+        L = lib()
+        msg = L.mexk_error_string(rc).decode()
+        det = L.mexk_last_error_detail().decode()
+        raise MexkError(f"{what}: {msg} (code {rc}){': ' + det if det else ''}")

@@ -1,0 +1,137 @@
+"""Python mirror of the reference's solver interface, over the mexk C ABI.
+
+``Context`` plays the reference's DeviceContext + ArnoldiRunner
+(main.cu:747-1125, 1253-2081): upload a CSR matrix once, then call
+``expmv`` (host vectors, like ArnoldiRunner::compute_expmv) or
+``expmv_device`` (device pointers). Results carry the reference's
+``converged`` / ``restarts_done`` / ``last_residual`` fields.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import PREC_FP64, PREC_MIXED, M_MAX, Params, Result, Step, check, lib
+
+PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def params(m, t, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64") -> Params:
+    prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    return Params(int(m), float(t), float(tol), int(max_restarts), int(bool(reorthogonalize)), prec)
+
+
+class Context:
+    """One device's copy of A plus basis and work buffers."""
+
+    def __init__(self, A, m_alloc: int = 30, device: int = 0):
+        self._h = C.c_void_p()
+        check(lib().mexk_context_create(device, C.byref(self._h)), "mexk_context_create")
+        self.n = int(A.n)
+        self.nnz = int(A.nnz)
+        self.m_alloc = int(m_alloc)
+        rp = np.ascontiguousarray(A.row_ptr, dtype=np.int32)
+        ci = np.ascontiguousarray(A.col_idx, dtype=np.int32)
+        va = np.ascontiguousarray(A.values, dtype=np.float64)
+        try:
+            check(lib().mexk_context_upload_csr(self._h, self.n, self.nnz, _ptr(rp, C.c_int), _ptr(ci, C.c_int),
+                                                _ptr(va, C.c_double), self.m_alloc), "mexk_context_upload_csr")
+        except Exception:
+            self.close()
+            raise
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return lib().mexk_context_stream(self._h) or 0
+
+    def close(self):
+        if self._h:
+            lib().mexk_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def expmv(self, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64"):
+        """y = exp(t A) v with host vectors. Returns (y, result dict)."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        if v.shape != (self.n,):
+            raise ValueError("v must have length n")
+        y = np.zeros(self.n)
+        p = params(m, t, tol, max_restarts, reorthogonalize, precision)
+        r = Result()
+        check(lib().mexk_expmv(self._h, C.byref(p), _ptr(v, C.c_double), _ptr(y, C.c_double), C.byref(r)),
+              "mexk_expmv")
+        return y, r.as_dict()
+
+    def expmv_device(self, v_ptr: int, y_ptr: int, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True,
+                     precision="fp64", stream: int = 0):
+        p = params(m, t, tol, max_restarts, reorthogonalize, precision)
+        r = Result()
+        check(lib().mexk_expmv_device(self._h, C.byref(p), C.c_void_p(v_ptr), C.c_void_p(y_ptr),
+                                      C.c_void_p(stream), C.byref(r)), "mexk_expmv_device")
+        return r.as_dict()
+
+    def steps(self):
+        cnt = C.c_int(0)
+        check(lib().mexk_get_steps(self._h, None, 0, C.byref(cnt)), "mexk_get_steps")
+        n = cnt.value
+        buf = (Step * max(n, 1))()
+        check(lib().mexk_get_steps(self._h, buf, n, C.byref(cnt)), "mexk_get_steps")
+        return [(s.t_done, s.dt, s.err, s.m_used, s.accepts, s.rejects) for s in buf[: min(n, len(buf))]]
+
+    def set_basis(self, V_cols: np.ndarray, precision="fp64"):
+        """V_cols: (ncols, n) array, row i = basis column i."""
+        V = np.ascontiguousarray(V_cols, dtype=np.float64)
+        check(lib().mexk_context_set_basis(self._h, PRECISIONS[precision], _ptr(V, C.c_double), V.shape[0]),
+              "mexk_context_set_basis")
+
+    def get_basis(self, ncols: int, precision="fp64") -> np.ndarray:
+        V = np.zeros((ncols, self.n))
+        check(lib().mexk_context_get_basis(self._h, PRECISIONS[precision], _ptr(V, C.c_double), ncols),
+              "mexk_context_get_basis")
+        return V
+
+    def profile_kernel(self, kind: str, j: int, iters: int = 3, precision="fp64") -> float:
+        """Mean CUDA-event duration (ms) of one solver kernel at Arnoldi step j."""
+        from ._lib import KERNELS
+
+        ms = C.c_double(0.0)
+        check(lib().mexk_profile_kernel(self._h, KERNELS[kind], PRECISIONS[precision], j, iters, C.byref(ms)),
+              "mexk_profile_kernel")
+        return ms.value
+
+    def arnoldi_step(self, j: int, reorthogonalize=True, precision="fp64"):
+        h = np.zeros(j + 1)
+        beta = C.c_double(0.0)
+        ok = C.c_int(0)
+        check(lib().mexk_arnoldi_step(self._h, j, int(reorthogonalize), PRECISIONS[precision], _ptr(h, C.c_double),
+                                      C.byref(beta), C.byref(ok)), "mexk_arnoldi_step")
+        return bool(ok.value), h, beta.value
+
+
+def device_count() -> int:
+    c = C.c_int(0)
+    check(lib().mexk_device_count(C.byref(c)), "mexk_device_count")
+    return c.value
+
+
+__all__ = ["Context", "params", "device_count", "PRECISIONS", "M_MAX"]

@@ -1,0 +1,299 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and the
+reference's golden fixtures. Needs a GB300 and the built libmexk.so.
+
+Tolerances: the FP64 path must agree with the reference's FP64 output to a
+relative 2-norm error of 1e-12 and take the same accept/reject decisions;
+the mixed-precision path must stay within 1e-6 of FP64.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_NAMES, load_golden
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+MIXED_TOL = 1e-6
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    return torch
+
+
+def _dev(torch, a, dtype):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device="cuda", dtype=dtype)
+
+
+# ------------------------------------------------------------------ SpMV
+@pytest.mark.parametrize("case", ["cfg0_random_n2000", "powerlaw_n2048", "heat_N32", "convdiff_N8_pe100"])
+def test_spmv_f64_bitwise(torch_cuda, oracle_mod, case):
+    from mexk._lib import check, lib
+
+    torch = torch_cuda
+    A, _ = load_golden(case)
+    x = np.random.default_rng(7).standard_normal(A.n)
+    rp, ci = _dev(torch, A.row_ptr, torch.int32), _dev(torch, A.col_idx, torch.int32)
+    va, xd = _dev(torch, A.values, torch.float64), _dev(torch, x, torch.float64)
+    yd = torch.empty(A.n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    check(lib().mexk_spmv_f64(A.n, rp.data_ptr(), ci.data_ptr(), va.data_ptr(), xd.data_ptr(), yd.data_ptr(), None))
+    y = yd.cpu().numpy()
+    y_ref = oracle_mod.spmv(A, x)
+    lens = np.diff(A.row_ptr)
+    short = lens <= 2048
+    # Rows that fit one tile: one rounded product per nonzero, summed in order.
+    assert np.array_equal(y[short], y_ref[short])
+    assert np.allclose(y[~short], y_ref[~short], rtol=1e-13, atol=0)
+
+
+def test_spmv_long_rows_and_empty_rows(torch_cuda, oracle_mod):
+    """Rows longer than a tile (block reduction), empty rows, one huge row."""
+    from mexk import synthetic as S
+    from mexk._lib import check, lib
+
+    torch = torch_cuda
+    n = 6000
+    rng = np.random.default_rng(3)
+    lens = rng.integers(0, 6, size=n)
+    lens[10] = 5000
+    lens[11] = 0
+    lens[4000] = 2049
+    lens[4001] = 2048
+    rows = np.repeat(np.arange(n), lens)
+    cols = np.concatenate([np.sort(rng.choice(n, size=l, replace=False)) for l in lens])
+    rp = np.zeros(n + 1, dtype=np.int32)
+    np.cumsum(lens, out=rp[1:])
+    A = S.CSR(n, rp, cols.astype(np.int32), rng.standard_normal(rows.size))
+    x = rng.standard_normal(n)
+    d = [_dev(torch, a, t) for a, t in ((A.row_ptr, torch.int32), (A.col_idx, torch.int32),
+                                        (A.values, torch.float64), (x, torch.float64))]
+    yd = torch.full((n,), np.nan, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    check(lib().mexk_spmv_f64(n, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(),
+                              yd.data_ptr(), None))
+    y = yd.cpu().numpy()
+    y_ref = oracle_mod.spmv(A, x)
+    assert np.allclose(y, y_ref, rtol=1e-13, atol=1e-13)
+    assert y[11] == 0.0
+
+
+def test_spmv_f32(torch_cuda):
+    from mexk import synthetic as S
+    from mexk._lib import check, lib
+
+    torch = torch_cuda
+    A = S.power_law(20000, seed=9)
+    x = np.random.default_rng(1).standard_normal(A.n).astype(np.float32)
+    d = [_dev(torch, a, t) for a, t in ((A.row_ptr, torch.int32), (A.col_idx, torch.int32),
+                                        (A.values.astype(np.float32), torch.float32), (x, torch.float32))]
+    yd = torch.empty(A.n, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    check(lib().mexk_spmv_f32(A.n, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), d[3].data_ptr(),
+                              yd.data_ptr(), None))
+    ref = A.to_dense().astype(np.float64) @ x.astype(np.float64) if A.n <= 4000 else None
+    # float64 reference of the float32 data
+    rows = np.repeat(np.arange(A.n), np.diff(A.row_ptr))
+    prod = A.values.astype(np.float32).astype(np.float64) * x.astype(np.float64)[A.col_idx]
+    ref = np.bincount(rows, weights=prod, minlength=A.n)
+    assert rel(yd.cpu().numpy().astype(np.float64), ref) < 1e-5
+
+
+# ------------------------------------------------------------------ expm
+@pytest.mark.parametrize("k", [1, 2, 5, 17, 30, 40, 64])
+@pytest.mark.parametrize("scale", [1e-3, 0.2, 0.9, 2.0, 8.0, 150.0])
+def test_expm_f64_vs_oracle(torch_cuda, oracle_mod, k, scale):
+    from mexk._lib import check, lib
+
+    torch = torch_cuda
+    rng = np.random.default_rng(k * 1000 + int(scale * 10))
+    M = rng.standard_normal((k, k)) * scale / max(1.0, np.sqrt(k))
+    E_ref = oracle_mod.expm(M)
+    Md = torch.from_numpy(np.asfortranarray(M).ravel(order="F")).cuda()
+    Ed = torch.zeros(k * k, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    check(lib().mexk_expm_f64(k, Md.data_ptr(), k, Ed.data_ptr(), k, None))
+    E = Ed.cpu().numpy().reshape(k, k, order="F")
+    tol = 1e-13 * max(10.0, np.abs(M).sum(axis=0).max())
+    assert np.abs(E - E_ref).max() <= tol * max(1.0, np.abs(E_ref).max())
+
+
+# ------------------------------------------------------------------ Arnoldi step
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_arnoldi_steps_vs_oracle(oracle_mod, precision):
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    A = S.power_law(3000, seed=4)
+    m = 24
+    v = np.random.default_rng(5).standard_normal(A.n)
+    V = np.zeros((m + 1, A.n))
+    V[0] = v / np.linalg.norm(v)
+    with Context(A, m_alloc=m) as ctx:
+        ctx.set_basis(V[:1], precision=precision)
+        for j in range(m):
+            ok_o, h_o, beta_o, _ = oracle_mod.arnoldi_step(A, V, j)
+            ok, h, beta = ctx.arnoldi_step(j, precision=precision)
+            assert ok and ok_o
+            scale = np.abs(h_o).max()
+            tol = 1e-13 if precision == "fp64" else 2e-5
+            assert np.abs(h - h_o).max() <= tol * scale, (j, np.abs(h - h_o).max() / scale)
+            assert abs(beta - beta_o) <= tol * scale
+        Vg = ctx.get_basis(m + 1, precision=precision)
+    tolv = 1e-12 if precision == "fp64" else 1e-4
+    assert np.abs(Vg - V).max() < tolv
+    # orthonormality of the device basis
+    G = Vg @ Vg.T
+    assert np.abs(G - np.eye(m + 1)).max() < (1e-13 if precision == "fp64" else 1e-6)
+
+
+def test_arnoldi_breakdown_detected():
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    n = 90
+    A = S.CSR(n, np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32), np.tile([-1.0, -2.0, -3.0], 30))
+    v = np.random.default_rng(1).uniform(0, 1, n)
+    V = np.zeros((4, n))
+    V[0] = v / np.linalg.norm(v)
+    with Context(A, m_alloc=10) as ctx:
+        ctx.set_basis(V[:1])
+        oks = [ctx.arnoldi_step(j)[0] for j in range(3)]
+    assert oks == [True, True, False]
+
+
+# ------------------------------------------------------------------ full solves
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_expmv_fp64_matches_reference(name):
+    from mexk.api import Context
+
+    A, d = load_golden(name)
+    if name.startswith("heat2048"):
+        pytest.skip("full-size record, covered separately")
+    m = int(d["m"])
+    with Context(A, m_alloc=m) as ctx:
+        y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), max_restarts=int(d["max_restarts"]))
+        steps = ctx.steps()
+    assert rel(y, d["y"]) <= FP64_TOL, rel(y, d["y"])
+    assert res["restarts_done"] == int(d["restarts_done"])
+    assert res["converged"] == int(d["converged"])
+    ref_steps = [ln.split() for ln in d["step_lines"]]
+    assert len(steps) == len(ref_steps)
+    for s, r in zip(steps, ref_steps):
+        # m_used / accepts / rejects exact; t, dt and err to printed precision
+        assert f"m_used={s[3]}" == r[4] and f"accepts={s[4]}" == r[5] and f"rejects={s[5]}" == r[6]
+        assert f"dt={s[1]:g}" == r[2]
+        ref_err = float(r[3].split("=")[1])
+        assert abs(s[2] - ref_err) <= 1e-5 * abs(ref_err) + 1e-20
+
+
+@pytest.mark.parametrize("name", ["cfg0_random_n2000", "heat_N32", "powerlaw_n2048", "convdiff_N8_pe100",
+                                  "diag_n1000_kat", "rejects_skew_n300_t20_m8"])
+def test_expmv_mixed_within_tolerance(name):
+    from mexk.api import Context
+
+    A, d = load_golden(name)
+    m = int(d["m"])
+    with Context(A, m_alloc=m) as ctx:
+        y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), max_restarts=int(d["max_restarts"]),
+                           precision="mixed")
+    assert rel(y, d["y"]) <= MIXED_TOL, rel(y, d["y"])
+
+
+def test_expmv_device_pointers(torch_cuda):
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    torch = torch_cuda
+    P = S.config0()
+    v = torch.from_numpy(P.v).cuda()
+    y = torch.zeros(P.A.n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    with Context(P.A, m_alloc=30) as ctx:
+        res = ctx.expmv_device(v.data_ptr(), y.data_ptr(), P.t, P.m)
+        y_host, _ = ctx.expmv(P.v, P.t, P.m)
+    assert res["converged"] == 1
+    assert np.array_equal(y.cpu().numpy(), y_host)
+
+
+def test_t_zero_and_zero_vector():
+    """Edge cases the reference defines: t = 0 runs no step (y = 0); v = 0
+    breaks down at once and returns 0."""
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    A = S.random_diag_dominant(200, 4, seed=1)
+    with Context(A, m_alloc=10) as ctx:
+        y, res = ctx.expmv(np.ones(200), 0.0, 10)
+        assert not y.any() and res["restarts_done"] == 0 and res["converged"] == 0
+        y, res = ctx.expmv(np.zeros(200), 1.0, 10)
+        assert not y.any() and res["converged"] == 1
+
+
+def test_invalid_arguments_rejected():
+    from mexk import MexkError
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    A = S.random_diag_dominant(50, 3, seed=2)
+    with Context(A, m_alloc=10) as ctx:
+        with pytest.raises(MexkError):
+            ctx.expmv(np.ones(50), 1.0, 11)  # m > m_alloc
+        with pytest.raises(MexkError):
+            ctx.expmv(np.ones(50), 1.0, 0)
+    with pytest.raises(MexkError):
+        Context(S.random_diag_dominant(20, 3, seed=2), m_alloc=65)
+
+
+# ------------------------------------------------------------------ full size
+def test_heat2048_modes_known_answer():
+    """Full 2048^2 heat workload with v = a combination of three Laplacian
+    eigenmodes: exp(tA)v = sum c_i exp(t lambda_i) u_i exactly, and the
+    Krylov space closes after three vectors (breakdown at j = 2)."""
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    N = 2048
+    A = S.laplacian_2d(N)
+    modes = [(1, 1, 1.0), (3, 2, 0.5), (40, 7, -0.25)]
+    v = np.zeros(A.n)
+    exact = np.zeros(A.n)
+    t = 1e-5
+    for p, q, c in modes:
+        u, lam = S.laplacian_2d_mode(N, p, q)
+        v += c * u
+        exact += c * np.exp(t * lam) * u
+    with Context(A, m_alloc=30) as ctx:
+        y, res = ctx.expmv(v, t, 30)
+        assert res["converged"] == 1
+        assert rel(y, exact) < 1e-11, rel(y, exact)
+        y32, _ = ctx.expmv(v, t, 30, precision="mixed")
+        assert rel(y32, exact) < MIXED_TOL, rel(y32, exact)
+
+
+def test_cli_diagonal_known_answer(tmp_path):
+    """The matrix_exp program on its built-in diagonal matrix (main.cu:2196)."""
+    import os
+    import subprocess
+
+    from mexk._lib import BUILD
+
+    out = tmp_path / "y.txt"
+    env = dict(os.environ, OUTPUT_Y_FILE=str(out))
+    p = subprocess.run([os.path.join(BUILD, "matrix_exp"), "1000"], env=env, capture_output=True, text=True,
+                       timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert "converged=yes" in p.stdout
+    y = np.loadtxt(out)
+    exact = 0.1 * np.exp(1.0 + np.arange(1000) / 1000)
+    assert rel(y, exact) < 1e-13
