@@ -211,6 +211,7 @@ def run_ours(args, rank, world, local_rank):
     res64 = ctx.expmv_device(v_d.data_ptr(), y64.data_ptr(), P.t, m, precision="fp64")
     steps64 = ctx.steps()
     res32 = ctx.expmv_device(v_d.data_ptr(), y32.data_ptr(), P.t, m, precision="mixed")
+    steps32 = ctx.steps()
     torch.cuda.synchronize()
     rel_err = float(torch.linalg.norm(y32 - y64) / torch.linalg.norm(y64))
     form = args.precision if args.precision != "auto" else ("mixed" if rel_err <= 1e-6 else "fp64")
@@ -312,10 +313,30 @@ def run_ours(args, rank, world, local_rank):
             "spmv": {"gbs": spmv_gbs, "frac": spmv_gbs / peak, "precision": form,
                      "fp64_gbs": sp64["bytes"] / (sp64["ms"] / 1e3) / 1e9},
             "kernel_share": {k: round(p["ms"] / tot_ms, 4) for k, p in per.items()},
+            "kernels": {f: {k: {"ms_per_cycle": round(p["ms"], 4),
+                                "gbs": round(p["bytes"] / (p["ms"] / 1e3) / 1e9, 1) if p["bytes"] else None}
+                            for k, p in pp.items()} for f, pp in (("chosen", per), ("fp64", per64))},
+            "trace": {"fp64": [(round(s[1], 12), float(f"{s[2]:.3g}")) for s in steps64],
+                      "mixed": [(round(s[1], 12), float(f"{s[2]:.3g}")) for s in steps32]},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def run_solve_once(local_rank):
+    """One FP64 and one mixed solve of the workload, untimed: the command
+    that ncu captures (profiles/ summaries name it)."""
+    import torch
+
+    from mexk.api import Context
+
+    torch.cuda.set_device(local_rank)
+    P = make_problem()
+    with Context(P.A, m_alloc=P.m, device=local_rank) as ctx:
+        for prec in ("fp64", "mixed"):
+            _, res = ctx.expmv(P.v, P.t, P.m, precision=prec)
+            print(prec, res, flush=True)
 
 
 def main():
@@ -326,7 +347,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--solve-once", action="store_true", help="one untimed FP64 + mixed solve (for ncu)")
     args = ap.parse_args()
+    if args.solve_once:
+        run_solve_once(int(os.environ.get("LOCAL_RANK", "0")))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -52,7 +52,10 @@ def rebuild_matrix(name, desc):
     raise KeyError(desc)
 
 
-GOLDEN_NAMES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+# Small fixtures with stored inputs; the full-size heat2048 record only holds
+# a decision sequence and a fingerprint of y.
+GOLDEN_NAMES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                      if not os.path.basename(p).startswith("heat2048"))
 
 
 def format_step(s):

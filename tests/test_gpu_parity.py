@@ -146,7 +146,9 @@ def test_arnoldi_steps_vs_oracle(oracle_mod, precision):
             ok, h, beta = ctx.arnoldi_step(j, precision=precision)
             assert ok and ok_o
             scale = np.abs(h_o).max()
-            tol = 1e-13 if precision == "fp64" else 2e-5
+            # Two independently built bases (CGS2 on the device, MGS2 in the
+            # oracle) drift apart by rounding as j grows.
+            tol = 1e-12 if precision == "fp64" else 2e-5
             assert np.abs(h - h_o).max() <= tol * scale, (j, np.abs(h - h_o).max() / scale)
             assert abs(beta - beta_o) <= tol * scale
         Vg = ctx.get_basis(m + 1, precision=precision)
@@ -178,8 +180,6 @@ def test_expmv_fp64_matches_reference(name):
     from mexk.api import Context
 
     A, d = load_golden(name)
-    if name.startswith("heat2048"):
-        pytest.skip("full-size record, covered separately")
     m = int(d["m"])
     with Context(A, m_alloc=m) as ctx:
         y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), max_restarts=int(d["max_restarts"]))
@@ -193,8 +193,10 @@ def test_expmv_fp64_matches_reference(name):
         # m_used / accepts / rejects exact; t, dt and err to printed precision
         assert f"m_used={s[3]}" == r[4] and f"accepts={s[4]}" == r[5] and f"rejects={s[5]}" == r[6]
         assert f"dt={s[1]:g}" == r[2]
+        # err near the rounding floor differs in its last digits; the
+        # decisions (checked above) are what must match.
         ref_err = float(r[3].split("=")[1])
-        assert abs(s[2] - ref_err) <= 1e-5 * abs(ref_err) + 1e-20
+        assert abs(s[2] - ref_err) <= 1e-5 * abs(ref_err) + 1e-3 * float(d["tol"])
 
 
 @pytest.mark.parametrize("name", ["cfg0_random_n2000", "heat_N32", "powerlaw_n2048", "convdiff_N8_pe100",
@@ -297,3 +299,34 @@ def test_cli_diagonal_known_answer(tmp_path):
     y = np.loadtxt(out)
     exact = 0.1 * np.exp(1.0 + np.arange(1000) / 1000)
     assert rel(y, exact) < 1e-13
+
+
+def test_heat2048_fp64_matches_reference_run():
+    """Full-size workload (n = 4,194,304) against the reference's own run:
+    the same accept/reject sequence and y to 1e-12 (norm, sum and entries at
+    seeded positions)."""
+    import os
+
+    from conftest import GOLDEN
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    d = np.load(os.path.join(GOLDEN, "heat2048_reference.npz"))
+    P = S.config1()
+    assert P.A.nnz == int(d["nnz"])
+    with Context(P.A, m_alloc=P.m) as ctx:
+        y, res = ctx.expmv(P.v, P.t, P.m)
+        steps = ctx.steps()
+        y32, res32 = ctx.expmv(P.v, P.t, P.m, precision="mixed")
+    ref_steps = [ln.split() for ln in d["step_lines"]]
+    assert len(steps) == len(ref_steps)
+    for s, r in zip(steps, ref_steps):
+        assert f"m_used={s[3]}" == r[4] and f"accepts={s[4]}" == r[5] and f"rejects={s[5]}" == r[6]
+        assert f"dt={s[1]:g}" == r[2] and f"t={s[0]:g}" == r[1]
+    assert res["restarts_done"] == int(d["restarts_done"]) and res["converged"] == int(d["converged"])
+    assert abs(np.linalg.norm(y) - float(d["y_norm"])) <= 1e-12 * float(d["y_norm"])
+    assert abs(y.sum() - float(d["y_sum"])) <= 1e-12 * np.abs(y).sum()
+    pos = d["positions"]
+    assert rel(y[pos], d["y_at"]) <= FP64_TOL and rel(y[:16], d["y_head"]) <= FP64_TOL
+    # mixed precision: within 1e-6 of the FP64 result
+    assert rel(y32, y) <= MIXED_TOL, rel(y32, y)
