@@ -145,6 +145,29 @@ int mexk_context_get_basis(mexk_context_t ctx, int precision, double* V_host, in
  * (replaces Eigen's MatrixXd::exp at main.cu:33-36). k <= MEXK_M_MAX. */
 int mexk_expm_f64(int k, const double* A, int lda, double* E, int lde, void* stream);
 
+/* ---- allocation-free variant ------------------------------------------- */
+/* Orthonormalises w against the k orthonormal FP64 columns of V (column-major,
+ * leading dimension ldv) with the solver's Gram-Schmidt sweeps (two passes if
+ * reorthogonalize, else one) and normalises it, without allocating anything:
+ * for callers that cannot call cudaMalloc (a host that owns all device memory
+ * through its own pool, an FFI runtime that only passes buffers, a request
+ * path that must not allocate). All pointers are device memory of the current
+ * device: on return (in stream order) h[0..k-1] = V^T w summed over the
+ * passes, *beta = |w - V h| (0 on breakdown: norm < 1e-14, NaN or Inf),
+ * q[0..n-1] = (w - V h) / beta (left untouched on breakdown), and w holds the
+ * orthogonalised, unnormalised vector. Limits: 1 <= k <= 64; the kernels'
+ * reduction scratch is a fixed 592 KB array in the library's device memory,
+ * sized for grids of up to 1024 thread blocks; larger sizes are refused with
+ * MEXK_ERR_INVALID. That array is shared by all calls on a device and keeps
+ * the last call's contents (each call clears what must start at zero), so
+ * calls that overlap on the GPU race and must be serialised. The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture. No counterpart in the
+ * reference: it orthogonalises only inside orthogonalize_mgs with cuBLAS. */
+int mexk_gram_schmidt_f64_noalloc(int n, int k, const double* V, int ldv, double* w,
+                                  int reorthogonalize, double* h, double* beta, double* q,
+                                  void* stream);
+
 /* ---- measurement ------------------------------------------------------ */
 #define MEXK_KERNEL_SPMV 0
 #define MEXK_KERNEL_GS_DOT 1      /* pass-1 dots */

@@ -69,6 +69,8 @@ _PROTOS = {
     "mexk_context_get_basis": ([_VP, C.c_int, _DP, C.c_int], C.c_int),
     "mexk_expm_f64": ([C.c_int, _VP, C.c_int, _VP, C.c_int, _VP], C.c_int),
     "mexk_profile_kernel": ([_VP, C.c_int, C.c_int, C.c_int, C.c_int, _DP], C.c_int),
+    "mexk_gram_schmidt_f64_noalloc": ([C.c_int, C.c_int, _VP, C.c_int, _VP, C.c_int, _VP, _VP, _VP, _VP],
+                                      C.c_int),
 }
 
 KERNELS = {"spmv": 0, "gs_dot": 1, "gs_upd_dot": 2, "gs_upd_norm": 3, "normalize": 4, "lift": 5, "controller": 6}
