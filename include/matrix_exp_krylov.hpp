@@ -135,10 +135,11 @@ struct ArnoldiRunner {
     int global_cols;
     long long global_nnz;
 
-    // Extensions (defaults reproduce the reference): arithmetic form, whether
-    // compute_expmv prints the [STEP]/[FLOPs]/METRIC lines, and the
-    // statistics of the last solve.
+    // Extensions (defaults reproduce the reference): arithmetic form, step
+    // controller, whether compute_expmv prints the [STEP]/[FLOPs]/METRIC
+    // lines, and the statistics of the last solve.
     int precision = MEXK_PREC_FP64;
+    int controller = MEXK_CTRL_REFERENCE;
     bool verbose = true;
     mexk_result_t last_result{};
     std::vector<mexk_step_t> last_steps;

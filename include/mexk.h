@@ -35,6 +35,15 @@ extern "C" {
 #define MEXK_PREC_MIXED 1 /* A values, basis V_m and SpMV/Gram-Schmidt in FP32;
                              Hessenberg, norms, Pade and residual in FP64 */
 
+/* Step-size control. */
+#define MEXK_CTRL_REFERENCE 0 /* the reference's accept/reject heuristic (main.cu:1476-1516) */
+#define MEXK_CTRL_SEARCH 1    /* per basis, the largest of 32 candidate steps whose
+                                 residual estimate passes; reference heuristic if none.
+                                 With MEXK_PREC_MIXED the per-step tolerance is
+                                 max(tol, 2^-24 |v|): the FP32 basis precision */
+#define MEXK_CTRL_LEARNED 2   /* SEARCH centred on an MLP's step prediction, with the
+                                 MLP also choosing the next cycle's Krylov dimension */
+
 /* Largest Krylov dimension m this build supports. */
 #define MEXK_M_MAX 64
 
@@ -49,6 +58,7 @@ typedef struct {
                             accepted steps; <= 0: dt_init = t, cap 1000 */
     int reorthogonalize; /* nonzero: second Gram-Schmidt pass (CLI always on) */
     int precision;       /* MEXK_PREC_* */
+    int controller;      /* MEXK_CTRL_*: step-size control (0 = the reference's) */
 } mexk_params_t;
 
 /* Outcome of one solve. converged / restarts_done / last_residual are the

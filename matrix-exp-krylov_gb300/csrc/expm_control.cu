@@ -401,12 +401,187 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
     }
 }
 
+// Shared accept bookkeeping of both controllers (main.cu:1476-1516): accepted
+// step tau with estimate err, or an abort after too many rejects.
+__device__ void finish_cycle(DevState* st, bool accept, double tau, double err, int k, int m_next,
+                             double next_center, bool grow_reference) {
+    double dt = tau;
+    if (accept) {
+        st->t_done += tau;
+        st->accepted += 1;
+        st->last_residual = err;
+        if (st->t_done >= st->total_t) {
+            st->converged = 1;
+            st->done = 1;
+            st->restart = 0;
+        } else {
+            if (grow_reference) {
+                if (err < 0.1 * st->tol) {
+                    const double dt_new = dt * 1.5 * 0.8;
+                    dt = dt_new < st->dt_max ? dt_new : st->dt_max;
+                }
+            } else {
+                dt = next_center < st->dt_max ? next_center : st->dt_max;
+            }
+            if (st->accepted >= st->max_steps) {
+                st->done = 1;
+                st->restart = 0;
+            } else {
+                st->restart = 1;
+            }
+        }
+    } else {
+        st->converged = 0;
+        st->last_residual = err;
+        st->t_done = st->total_t;
+        st->done = 1;
+        st->restart = 0;
+    }
+    st->k_lift = k;
+    st->cycles += 1;
+    st->spmv_count += k;
+    st->lift = 1;
+    st->tau_prev = tau;
+    st->err_prev = err;
+    if (!st->done) {
+        st->breakdown = 0;
+        st->m_next = m_next;
+        st->k_used = m_next;
+        const double rem = st->total_t - st->t_done;
+        dt = dt < rem ? dt : rem;
+    }
+    st->dt = dt;
+}
+
+__device__ void write_log(DevState* st, mexk_step_t* log, double dt, double err, int k, int rejects) {
+    if (log != nullptr && st->nlog < st->log_cap) {
+        mexk_step_t& L = log[st->nlog];
+        L.t_done = st->t_done;
+        L.dt = dt;
+        L.err = err;
+        L.m_used = k;
+        L.accepts = st->accepted;
+        L.rejects = rejects;
+    }
+    st->nlog += 1;
+    st->attempts += 1;
+}
+
+// Candidate steps tau_g = center * 2^((g - 24)/4), g = 0..31 (1/64 .. 3.4 x the
+// centre), each clamped to the remaining time. Every block evaluates one
+// candidate's exponential and residual estimate; the last block to finish
+// takes the largest passing step (its exponential is reused for the lift),
+// or, if none passes, continues below the smallest candidate with the
+// reference's shrink rule.
+__global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchArgs a, int m) {
+    extern __shared__ double smem[];
+    __shared__ int s_k, s_bd, s_flag, s_best, s_dec;
+    __shared__ double s_tau, s_center;
+    DevState* st = a.st;
+    if (st->done) return;
+    if (threadIdx.x == 0) {
+        const int bd = st->breakdown;
+        int k = bd ? st->k_used : m;
+        if (k < 1 || k > m) k = k < 1 ? 1 : m;
+        s_k = k;
+        s_bd = bd;
+        s_center = st->dt;
+    }
+    __syncthreads();
+    const int k = s_k;
+    const bool bd = s_bd != 0;
+    const size_t ldh = static_cast<size_t>(a.ldh);
+    const double rem = st->total_t - st->t_done;
+    const double tol_eff = fmax(st->tol, st->tol_floor_rel * st->v_norm);
+    ExpmBuf B = carve(smem, k);
+    {
+        double tau = s_center * exp2(0.25 * (static_cast<int>(blockIdx.x) - 24));
+        tau = tau < rem ? tau : rem;
+        for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = tau * a.H[(e % k) + (e / k) * ldh];
+        __syncthreads();
+        double* R = expm_block(B, k, &st->status);
+        double* c = a.cand + static_cast<size_t>(blockIdx.x) * CAND_STRIDE;
+        for (int i = threadIdx.x; i < k; i += blockDim.x) c[2 + i] = R[i];
+        if (threadIdx.x == 0) {
+            c[0] = bd ? 0.0 : fabs(a.H[k + (k - 1) * ldh] * R[k - 1]) * st->v_norm;
+            c[1] = tau;
+        }
+    }
+    if (!grid_last_block(a.counter, &s_flag)) return;
+    if (threadIdx.x == 0) {
+        int best = -1;
+        for (int g = 0; g < static_cast<int>(gridDim.x); ++g) {
+            const double* c = a.cand + static_cast<size_t>(g) * CAND_STRIDE;
+            if (__ldcg(&c[0]) <= tol_eff && (best < 0 || __ldcg(&c[1]) > __ldcg(&a.cand[best * CAND_STRIDE + 1])))
+                best = g;
+        }
+        s_best = best;
+    }
+    __syncthreads();
+    const double vn = st->v_norm;
+    if (s_best >= 0) {
+        const double* c = a.cand + static_cast<size_t>(s_best) * CAND_STRIDE;
+        for (int i = threadIdx.x; i <= k; i += blockDim.x) {
+            const double wi = (i < k) ? __ldcg(&c[2 + i]) : 0.0;
+            a.coef[i] = (fabs(wi) > 1e-15) ? vn * wi : 0.0;
+        }
+        if (threadIdx.x == 0) {
+            const double tau = __ldcg(&c[1]), err = __ldcg(&c[0]);
+            write_log(st, a.log, tau, err, k, 0);
+            // next centre: double the step (the grid reaches 1/64 of it)
+            finish_cycle(st, true, tau, err, k, m, 2.0 * tau, false);
+        }
+        return;
+    }
+    // No candidate passed: the reference heuristic below the smallest one.
+    if (threadIdx.x == 0) s_tau = __ldcg(&a.cand[1]);
+    __syncthreads();
+    int rejects = 1;  // the failed candidate round counts as one reject
+    double err = 0.0;
+    double* R = nullptr;
+    while (true) {
+        if (threadIdx.x == 0) {
+            const double dt_new = s_tau * 0.5 * 0.8;
+            s_tau = dt_new > st->dt_min ? dt_new : st->dt_min;
+        }
+        __syncthreads();
+        const double dt = s_tau;
+        for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = dt * a.H[(e % k) + (e / k) * ldh];
+        __syncthreads();
+        R = expm_block(B, k, &st->status);
+        if (threadIdx.x == 0) {
+            err = bd ? 0.0 : fabs(a.H[k + (k - 1) * ldh] * R[k - 1]) * st->v_norm;
+            write_log(st, a.log, dt, err, k, rejects);
+            if (err <= tol_eff || bd) {
+                s_dec = DEC_ACCEPT;
+            } else {
+                ++rejects;
+                s_dec = rejects >= st->max_rejects ? DEC_ABORT : DEC_REJECT;
+            }
+        }
+        __syncthreads();
+        if (s_dec != DEC_REJECT) break;
+    }
+    for (int i = threadIdx.x; i <= k; i += blockDim.x) {
+        const double wi = (i < k) ? R[i] : 0.0;
+        a.coef[i] = (fabs(wi) > 1e-15) ? vn * wi : 0.0;
+    }
+    if (threadIdx.x == 0) finish_cycle(st, s_dec == DEC_ACCEPT, s_tau, err, k, m, 2.0 * s_tau, false);
+}
+
 }  // namespace
+
+int launch_controller_search(const SearchArgs& a, int m, cudaStream_t s) {
+    controller_search_kernel<<<SEARCH_CAND, EXPM_THREADS, expm_smem_bytes(m), s>>>(a, m);
+    MEXK_CK_LAUNCH("controller_search_kernel");
+    return MEXK_OK;
+}
 
 int expm_init_attributes() {
     const int bytes = static_cast<int>(expm_smem_bytes(MEXK_M_MAX));
     MEXK_CK(cudaFuncSetAttribute(expm_standalone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     MEXK_CK(cudaFuncSetAttribute(controller_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    MEXK_CK(cudaFuncSetAttribute(controller_search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     return MEXK_OK;
 }
 

@@ -85,8 +85,193 @@ __device__ __forceinline__ double transpose_reduce(double (&a)[K], int lane) {
     return v;
 }
 
-template <int KMAX, int MODE, typename TV>
-__global__ void __launch_bounds__(GS_THREADS) gs_kernel(GsArgs a) {
+// 16-byte row-group loads: RPT consecutive rows of one basis column.
+template <int RPT, typename TV>
+struct RowIO;
+template <>
+struct RowIO<1, double> {
+    static __device__ __forceinline__ void ld(const double* p, double (&o)[1]) { o[0] = *p; }
+    static __device__ __forceinline__ void ldg(const double* p, double (&o)[1]) { o[0] = __ldg(p); }
+    static __device__ __forceinline__ void ldcs(const double* p, double (&o)[1]) { o[0] = __ldcs(p); }
+    static __device__ __forceinline__ void st(double* p, const double (&o)[1]) { *p = o[0]; }
+};
+template <>
+struct RowIO<2, double> {
+    static __device__ __forceinline__ void put(const double2 t, double (&o)[2]) {
+        o[0] = t.x;
+        o[1] = t.y;
+    }
+    static __device__ __forceinline__ void ld(const double* p, double (&o)[2]) {
+        put(*reinterpret_cast<const double2*>(p), o);
+    }
+    static __device__ __forceinline__ void ldg(const double* p, double (&o)[2]) {
+        put(__ldg(reinterpret_cast<const double2*>(p)), o);
+    }
+    static __device__ __forceinline__ void ldcs(const double* p, double (&o)[2]) {
+        put(__ldcs(reinterpret_cast<const double2*>(p)), o);
+    }
+    static __device__ __forceinline__ void st(double* p, const double (&o)[2]) {
+        *reinterpret_cast<double2*>(p) = make_double2(o[0], o[1]);
+    }
+};
+template <>
+struct RowIO<1, float> {
+    static __device__ __forceinline__ void ld(const float* p, float (&o)[1]) { o[0] = *p; }
+    static __device__ __forceinline__ void ldg(const float* p, float (&o)[1]) { o[0] = __ldg(p); }
+    static __device__ __forceinline__ void ldcs(const float* p, float (&o)[1]) { o[0] = __ldcs(p); }
+    static __device__ __forceinline__ void st(float* p, const float (&o)[1]) { *p = o[0]; }
+};
+template <>
+struct RowIO<4, float> {
+    static __device__ __forceinline__ void put(const float4 t, float (&o)[4]) {
+        o[0] = t.x;
+        o[1] = t.y;
+        o[2] = t.z;
+        o[3] = t.w;
+    }
+    static __device__ __forceinline__ void ld(const float* p, float (&o)[4]) {
+        put(*reinterpret_cast<const float4*>(p), o);
+    }
+    static __device__ __forceinline__ void ldg(const float* p, float (&o)[4]) {
+        put(__ldg(reinterpret_cast<const float4*>(p)), o);
+    }
+    static __device__ __forceinline__ void ldcs(const float* p, float (&o)[4]) {
+        put(__ldcs(reinterpret_cast<const float4*>(p)), o);
+    }
+    static __device__ __forceinline__ void st(float* p, const float (&o)[4]) {
+        *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
+    }
+};
+
+// Dot of RPT row values into an accumulator: FP64 chains DFMAs; FP32 sums the
+// RPT products in FP32 and adds the group sum with compensation.
+template <int RPT>
+__device__ __forceinline__ void acc_dot(Acc<double>& a, const double (&v)[RPT], const double (&w)[RPT]) {
+#pragma unroll
+    for (int i = 0; i < RPT; ++i) a.fma_add(v[i], w[i]);
+}
+template <int RPT>
+__device__ __forceinline__ void acc_dot(Acc<float>& a, const float (&v)[RPT], const float (&w)[RPT]) {
+    float p = v[0] * w[0];
+#pragma unroll
+    for (int i = 1; i < RPT; ++i) p = __fmaf_rn(v[i], w[i], p);
+    a.fma_add(p, 1.0f);
+}
+
+// One row group (RPT rows starting at r0) of a sweep. Columns are read in
+// chunks of CH so that only the accumulators stay live across the loop.
+template <int KMAX, int MODE, typename TV, int RPT>
+__device__ __forceinline__ void gs_rows(const TV* __restrict__ V, size_t ldv, TV* __restrict__ w, size_t r0,
+                                       int k, const typename Compute<TV>::type* s_h, Acc<TV> (&acc)[KMAX],
+                                       Acc<TV>& nacc) {
+    using TC = typename Compute<TV>::type;
+    using IO = RowIO<RPT, TV>;
+    constexpr int CH = 8;
+    constexpr bool KEEP = KMAX * RPT * sizeof(TV) <= 128;
+    TV wv[RPT];
+    IO::ld(w + r0, wv);
+    TC wr[RPT];
+#pragma unroll
+    for (int i = 0; i < RPT; ++i) wr[i] = static_cast<TC>(wv[i]);
+    if constexpr (KEEP) {
+        TV vv[KMAX][RPT];
+#pragma unroll
+        for (int c = 0; c < KMAX; ++c)
+            if (c < k) IO::ldcs(V + c * ldv + r0, vv[c]);
+        if (MODE != GS_DOT) {
+            TC s[RPT];
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) s[i] = TC(0);
+#pragma unroll
+            for (int c = 0; c < KMAX; ++c)
+                if (c < k) {
+                    const TC h = s_h[c];
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i) s[i] = fma(static_cast<TC>(vv[c][i]), h, s[i]);
+                }
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                wr[i] = wr[i] - s[i];
+                wv[i] = static_cast<TV>(wr[i]);
+            }
+            IO::st(w + r0, wv);
+        }
+        if (MODE != GS_UPD_NORM) {
+#pragma unroll
+            for (int c = 0; c < KMAX; ++c)
+                if (c < k) {
+                    TC vc[RPT];
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i) vc[i] = static_cast<TC>(vv[c][i]);
+                    acc_dot<RPT>(acc[c], vc, wr);
+                }
+        } else {
+            acc_dot<RPT>(nacc, wr, wr);
+        }
+    } else {
+        if (MODE != GS_DOT) {
+            TC s[RPT];
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) s[i] = TC(0);
+#pragma unroll
+            for (int cb = 0; cb < KMAX; cb += CH) {
+                if (cb < k) {
+                    TV vv[CH][RPT];
+#pragma unroll
+                    for (int cc = 0; cc < CH; ++cc)
+                        if (cb + cc < k) IO::ld(V + (cb + cc) * ldv + r0, vv[cc]);
+#pragma unroll
+                    for (int cc = 0; cc < CH; ++cc)
+                        if (cb + cc < k) {
+                            const TC h = s_h[cb + cc];
+#pragma unroll
+                            for (int i = 0; i < RPT; ++i) s[i] = fma(static_cast<TC>(vv[cc][i]), h, s[i]);
+                        }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                wr[i] = wr[i] - s[i];
+                wv[i] = static_cast<TV>(wr[i]);
+            }
+            IO::st(w + r0, wv);
+        }
+        if (MODE != GS_UPD_NORM) {
+#pragma unroll
+            for (int cb = 0; cb < KMAX; cb += CH) {
+                if (cb < k) {
+                    TV vv[CH][RPT];
+#pragma unroll
+                    for (int cc = 0; cc < CH; ++cc)
+                        if (cb + cc < k) {
+                            if (MODE == GS_UPD_DOT) IO::ldg(V + (cb + cc) * ldv + r0, vv[cc]);
+                            else IO::ldcs(V + (cb + cc) * ldv + r0, vv[cc]);
+                        }
+#pragma unroll
+                    for (int cc = 0; cc < CH; ++cc)
+                        if (cb + cc < k) {
+                            TC vc[RPT];
+#pragma unroll
+                            for (int i = 0; i < RPT; ++i) vc[i] = static_cast<TC>(vv[cc][i]);
+                            acc_dot<RPT>(acc[cb + cc], vc, wr);
+                        }
+                }
+            }
+        } else {
+            acc_dot<RPT>(nacc, wr, wr);
+        }
+    }
+}
+
+// Register cap per width so that 3 / 2 / 1 blocks of 256 threads stay resident.
+// The fused update+dot sweep keeps more values live: one block fewer.
+template <int KMAX, int MODE>
+constexpr int gs_min_blocks() {
+    return KMAX <= 16 ? (MODE == GS_UPD_DOT ? 2 : 3) : (KMAX <= 32 ? 2 : 1);
+}
+
+template <int KMAX, int MODE, typename TV, int RPT>
+__global__ void __launch_bounds__(GS_THREADS, (gs_min_blocks<KMAX, MODE>())) gs_kernel(GsArgs a) {
     using TC = typename Compute<TV>::type;
     constexpr int NW = GS_THREADS / 32;
     constexpr int KR = KMAX < 32 ? KMAX : 32;  // width of one butterfly
@@ -94,6 +279,7 @@ __global__ void __launch_bounds__(GS_THREADS) gs_kernel(GsArgs a) {
     __shared__ double s_red[NW][KMAX + 1];
     __shared__ double s_out[KMAX + 1];
     __shared__ double s_scratch[GS_THREADS];
+    __shared__ TC s_h[KMAX];
     __shared__ int s_flag;
 
     DevState* st = a.st;
@@ -106,11 +292,10 @@ __global__ void __launch_bounds__(GS_THREADS) gs_kernel(GsArgs a) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
 
-    TC hreg[KMAX];
     if (MODE != GS_DOT) {
         const double* hin = (MODE == GS_UPD_DOT || !a.reortho) ? a.h1 : a.h2;
-#pragma unroll
-        for (int c = 0; c < KMAX; ++c) hreg[c] = (c < k) ? static_cast<TC>(hin[c]) : TC(0);
+        if (threadIdx.x < KMAX) s_h[threadIdx.x] = (threadIdx.x < k) ? static_cast<TC>(hin[threadIdx.x]) : TC(0);
+        __syncthreads();
     }
 
     Acc<TV> acc[KMAX];
@@ -120,23 +305,12 @@ __global__ void __launch_bounds__(GS_THREADS) gs_kernel(GsArgs a) {
     nacc.zero();
 
     const int stride = gridDim.x * GS_THREADS;
-    for (int r = blockIdx.x * GS_THREADS + threadIdx.x; r < n; r += stride) {
-        TC wr = static_cast<TC>(w[r]);
-        if (MODE != GS_DOT) {
-            TC s = TC(0);
-#pragma unroll
-            for (int c = 0; c < KMAX; ++c)
-                if (c < k) s = fma(static_cast<TC>(V[c * ldv + r]), hreg[c], s);
-            wr = wr - s;
-            w[r] = static_cast<TV>(wr);
-        }
-        if (MODE != GS_UPD_NORM) {
-#pragma unroll
-            for (int c = 0; c < KMAX; ++c)
-                if (c < k) acc[c].fma_add(static_cast<TC>(__ldg(&V[c * ldv + r])), wr);
-        } else {
-            nacc.fma_add(wr, wr);
-        }
+    const int ngroups = n / RPT;
+    for (int g = blockIdx.x * GS_THREADS + threadIdx.x; g < ngroups; g += stride)
+        gs_rows<KMAX, MODE, TV, RPT>(V, ldv, w, static_cast<size_t>(g) * RPT, k, s_h, acc, nacc);
+    if (RPT > 1) {
+        for (int r = ngroups * RPT + blockIdx.x * GS_THREADS + threadIdx.x; r < n; r += stride)
+            gs_rows<KMAX, MODE, TV, 1>(V, ldv, w, static_cast<size_t>(r), k, s_h, acc, nacc);
     }
 
     // ---- block reduction
@@ -196,36 +370,102 @@ __global__ void __launch_bounds__(GS_THREADS) gs_kernel(GsArgs a) {
     }
 }
 
+// V[:,j+1] = w * (1/beta) in the storage precision (FP64: the reference's
+// w * reciprocal; FP32: one conversion of 1/beta, then FP32 multiplies --
+// float<->double conversions run on the scarce FP64 pipe).
 template <typename TV>
 __global__ void __launch_bounds__(256) normalize_kernel(int n, int j, int ldv, const TV* __restrict__ w,
                                                         TV* __restrict__ V, const DevState* st,
                                                         const double* inv_beta_ptr) {
     if (st != nullptr && (st->breakdown || st->done)) return;
-    const double inv = st != nullptr ? st->inv_beta : *inv_beta_ptr;
+    const TV inv = static_cast<TV>(st != nullptr ? st->inv_beta : *inv_beta_ptr);
     TV* q = V + static_cast<size_t>(j + 1) * ldv;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
-        q[r] = static_cast<TV>(static_cast<double>(w[r]) * inv);
+    constexpr int RPT = 16 / sizeof(TV);
+    const bool vec = (reinterpret_cast<uintptr_t>(q) % 16 == 0) && (reinterpret_cast<uintptr_t>(w) % 16 == 0);
+    const int stride = gridDim.x * blockDim.x;
+    int r0 = 0;
+    if (vec) {
+        const int ng = n / RPT;
+        for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += stride) {
+            TV t[RPT];
+            RowIO<RPT, TV>::ldcs(w + static_cast<size_t>(g) * RPT, t);
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) t[i] = t[i] * inv;
+            RowIO<RPT, TV>::st(q + static_cast<size_t>(g) * RPT, t);
+        }
+        r0 = ng * RPT;
+    }
+    for (int r = r0 + blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) q[r] = w[r] * inv;
 }
 
-template <int KMAX, int MODE, typename TV>
+template <int KMAX, int MODE, typename TV, int RPT>
 int launch_one(const GsArgs& a, int grid, cudaStream_t s) {
-    gs_kernel<KMAX, MODE, TV><<<grid, GS_THREADS, 0, s>>>(a);
+    gs_kernel<KMAX, MODE, TV, RPT><<<grid, GS_THREADS, 0, s>>>(a);
     MEXK_CK_LAUNCH("gs_kernel");
     return MEXK_OK;
 }
 
+// 16-byte row groups need 16-byte aligned columns: every column start
+// (V + c*ldv) and w. Otherwise one row per thread.
+template <typename TV>
+bool vector_ok(const GsArgs& a) {
+    constexpr int RPT = 16 / sizeof(TV);
+    return (reinterpret_cast<uintptr_t>(a.V) % 16 == 0) && (reinterpret_cast<uintptr_t>(a.w) % 16 == 0) &&
+           (a.ldv % RPT == 0);
+}
+
+template <int KMAX, int MODE, typename TV>
+int launch_k(const GsArgs& a, int grid, cudaStream_t s) {
+    constexpr int RPT = 16 / sizeof(TV);
+    if (vector_ok<TV>(a)) return launch_one<KMAX, MODE, TV, RPT>(a, grid, s);
+    return launch_one<KMAX, MODE, TV, 1>(a, grid, s);
+}
+
 template <int MODE, typename TV>
 int launch_mode(const GsArgs& a, int grid, cudaStream_t s) {
-    if (a.k <= 8) return launch_one<8, MODE, TV>(a, grid, s);
-    if (a.k <= 16) return launch_one<16, MODE, TV>(a, grid, s);
-    if (a.k <= 32) return launch_one<32, MODE, TV>(a, grid, s);
-    if (a.k <= 64) return launch_one<64, MODE, TV>(a, grid, s);
+    if (a.k <= 8) return launch_k<8, MODE, TV>(a, grid, s);
+    if (a.k <= 16) return launch_k<16, MODE, TV>(a, grid, s);
+    if (a.k <= 32) return launch_k<32, MODE, TV>(a, grid, s);
+    if (a.k <= 64) return launch_k<64, MODE, TV>(a, grid, s);
     return MEXK_ERR_UNSUPPORTED;
 }
 
 }  // namespace
 
-int gs_grid_size(int n, int k, bool fp32) {
+namespace {
+
+template <int KMAX, int MODE, typename TV, int RPT>
+int occupancy_of() {
+    static int occ = -1;
+    if (occ < 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, gs_kernel<KMAX, MODE, TV, RPT>, GS_THREADS, 0) !=
+            cudaSuccess)
+            b = 1;
+        occ = b > 0 ? b : 1;
+    }
+    return occ;
+}
+
+// Resident blocks per SM shared by the three sweeps of one width.
+template <int KMAX, typename TV>
+int occupancy_k() {
+    constexpr int RPT = 16 / sizeof(TV);
+    int o = occupancy_of<KMAX, GS_DOT, TV, RPT>();
+    o = min(o, occupancy_of<KMAX, GS_UPD_DOT, TV, RPT>());
+    o = min(o, occupancy_of<KMAX, GS_UPD_NORM, TV, RPT>());
+    return o;
+}
+
+template <typename TV>
+int occupancy_for(int k) {
+    if (k <= 8) return occupancy_k<8, TV>();
+    if (k <= 16) return occupancy_k<16, TV>();
+    if (k <= 32) return occupancy_k<32, TV>();
+    return occupancy_k<64, TV>();
+}
+
+int num_sms() {
     static int sms = 0;
     if (sms == 0) {
         int dev = 0;
@@ -233,16 +473,29 @@ int gs_grid_size(int n, int k, bool fp32) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }
-    // Wide accumulator sets cost registers: fewer resident blocks per SM.
-    int per_sm = 4;
-    if (!fp32 && k > 32) per_sm = 1;
-    else if (!fp32 && k > 16) per_sm = 2;
-    else if (fp32 && k > 32) per_sm = 2;
-    const long long need = (static_cast<long long>(n) + GS_THREADS - 1) / GS_THREADS;
-    long long g = static_cast<long long>(sms) * per_sm;
+    return sms;
+}
+
+}  // namespace
+
+// One wave of resident blocks (at most 4 per SM), fewer for short vectors.
+int gs_grid_size(int n, int k, bool fp32) {
+    int per_sm = fp32 ? occupancy_for<float>(k) : occupancy_for<double>(k);
+    if (per_sm > 4) per_sm = 4;
+    const int rpt = fp32 ? 4 : 2;
+    const long long need = (static_cast<long long>(n) + rpt * GS_THREADS - 1) / (rpt * GS_THREADS);
+    long long g = static_cast<long long>(num_sms()) * per_sm;
     if (need < g) g = need;
     if (g < 1) g = 1;
     return static_cast<int>(g);
+}
+
+// Resolves every occupancy query once, outside any stream capture.
+void gs_prepare() {
+    for (int k : {8, 16, 32, 64}) {
+        (void)gs_grid_size(1 << 20, k, false);
+        (void)gs_grid_size(1 << 20, k, true);
+    }
 }
 
 template <typename TV>
@@ -259,8 +512,8 @@ int launch_gs(GsMode mode, const GsArgs& a, int grid, cudaStream_t s) {
 template <typename TV>
 int launch_normalize(int n, int j, int ldv, const TV* w, TV* V, const DevState* st,
                      const double* inv_beta, cudaStream_t s) {
-    int grid = (n + 255) / 256;
-    if (grid > 4096) grid = 4096;
+    int grid = (n / (16 / static_cast<int>(sizeof(TV))) + 255) / 256;
+    if (grid > 2048) grid = 2048;
     if (grid < 1) grid = 1;
     normalize_kernel<TV><<<grid, 256, 0, s>>>(n, j, ldv, w, V, st, inv_beta);
     MEXK_CK_LAUNCH("normalize_kernel");

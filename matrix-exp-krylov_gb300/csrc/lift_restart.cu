@@ -20,9 +20,36 @@ namespace {
 
 constexpr int LIFT_THREADS = 256;
 
+// One row of y = sum_c coef_c V_c. FP64 basis: a DFMA chain in column order
+// (the axpy order). FP32 basis: FP32 products summed with compensation and
+// widened once per row, so the FP64 pipe does O(1) work per row, not O(k).
+template <typename TV>
+__device__ __forceinline__ double lift_row(const TV* __restrict__ V, size_t ldv, int r, int k, const double* c64,
+                                           const float* c32);
+template <>
+__device__ __forceinline__ double lift_row<double>(const double* __restrict__ V, size_t ldv, int r, int k,
+                                                   const double* c64, const float*) {
+    double s = 0.0;
+    for (int c = 0; c < k; ++c) s = fma(c64[c], __ldcs(&V[c * ldv + r]), s);
+    return s;
+}
+template <>
+__device__ __forceinline__ double lift_row<float>(const float* __restrict__ V, size_t ldv, int r, int k,
+                                                  const double*, const float* c32) {
+    float s = 0.f, comp = 0.f;
+    for (int c = 0; c < k; ++c) {
+        const float y = __fmaf_rn(c32[c], __ldcs(&V[c * ldv + r]), -comp);
+        const float t = __fadd_rn(s, y);
+        comp = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    return static_cast<double>(s) - static_cast<double>(comp);
+}
+
 template <typename TV>
 __global__ void __launch_bounds__(LIFT_THREADS) lift_kernel(LiftArgs a) {
     __shared__ double s_coef[MEXK_M_MAX + 1];
+    __shared__ float s_coef32[MEXK_M_MAX + 1];
     __shared__ double s_red[32];
     __shared__ double s_out[1];
     __shared__ double s_scratch[LIFT_THREADS];
@@ -30,14 +57,16 @@ __global__ void __launch_bounds__(LIFT_THREADS) lift_kernel(LiftArgs a) {
     DevState* st = a.st;
     if (!st->lift) return;
     const int k = st->k_lift;
-    for (int i = threadIdx.x; i < k; i += blockDim.x) s_coef[i] = a.coef[i];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        s_coef[i] = a.coef[i];
+        s_coef32[i] = static_cast<float>(a.coef[i]);
+    }
     __syncthreads();
     const TV* __restrict__ V = static_cast<const TV*>(a.V);
     const size_t ldv = static_cast<size_t>(a.ldv);
     double nacc = 0.0;
     for (int r = blockIdx.x * LIFT_THREADS + threadIdx.x; r < a.n; r += gridDim.x * LIFT_THREADS) {
-        double s = 0.0;
-        for (int c = 0; c < k; ++c) s = fma(s_coef[c], static_cast<double>(V[c * ldv + r]), s);
+        const double s = lift_row<TV>(V, ldv, r, k, s_coef, s_coef32);
         a.y[r] = s;
         nacc = fma(s, s, nacc);
     }
@@ -87,13 +116,15 @@ __global__ void __launch_bounds__(LIFT_THREADS)
     }
 }
 
+// V[:,0] = x * scale. FP64: the reference's x * (1/|x|). FP32 basis: one
+// narrowing conversion per element, then an FP32 multiply.
 template <typename TV>
 __global__ void __launch_bounds__(256) restart_kernel(int n, const double* __restrict__ x, TV* __restrict__ V0,
                                                       const DevState* st, int force) {
     if (!force && !st->restart) return;
-    const double sc = st->restart_scale;
+    const TV sc = static_cast<TV>(st->restart_scale);
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
-        V0[r] = static_cast<TV>(x[r] * sc);
+        V0[r] = static_cast<TV>(__ldcs(&x[r])) * sc;
 }
 
 int elementwise_grid(int n) {

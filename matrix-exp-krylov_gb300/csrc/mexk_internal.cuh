@@ -60,6 +60,14 @@ struct DevState {
     int log_cap;
     int lift;       // the finished cycle's lift is pending
     long long spmv_count;
+    // step-size search / learned controller
+    int ctrl;       // MEXK_CTRL_* of this solve
+    int m_next;     // Krylov dimension of the next cycle
+    double tau_prev;
+    double err_prev;
+    // Candidate-step control in FP32 storage does not resolve the truncation
+    // error below the basis precision: tol_eff = max(tol, tol_floor_rel*|v|).
+    double tol_floor_rel;
 };
 
 // Status bits written by kernels.
@@ -181,6 +189,7 @@ struct GsArgs {
 template <typename TV>
 int launch_gs(GsMode mode, const GsArgs& a, int grid, cudaStream_t s);
 int gs_grid_size(int n, int k, bool fp32);
+void gs_prepare();
 
 template <typename TV>
 int launch_normalize(int n, int j, int ldv, const TV* w, TV* V, const DevState* st,
@@ -201,6 +210,21 @@ struct ControlArgs {
     mexk_step_t* log;   // attempt log (log_cap entries)
 };
 int launch_controller(const ControlArgs& a, int m, cudaStream_t s);
+
+// Candidate-step controller: one thread block per candidate step.
+constexpr int SEARCH_CAND = 32;
+constexpr int CAND_STRIDE = MEXK_M_MAX + 2;  // err, tau, w_0..w_{k-1}
+struct SearchArgs {
+    DevState* st;
+    const double* H;
+    int ldh;
+    double* coef;
+    mexk_step_t* log;
+    double* cand;           // SEARCH_CAND x CAND_STRIDE
+    unsigned int* counter;
+    const float* mlp;       // controller network weights, or null
+};
+int launch_controller_search(const SearchArgs& a, int m, cudaStream_t s);
 
 // ------------------------------------------------------------ lift / restart
 struct LiftArgs {

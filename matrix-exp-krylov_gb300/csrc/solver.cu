@@ -49,7 +49,7 @@ constexpr int LOG_CAP = 8192;
 using namespace mexk;
 
 struct GraphEntry {
-    int m, prec, reortho;
+    int m, prec, reortho, ctrl;
     cudaGraphExec_t exec;
 };
 
@@ -77,6 +77,8 @@ struct mexk_context_s {
     double* d_h1 = nullptr;
     double* d_h2 = nullptr;
     double* d_coef = nullptr;
+    double* d_cand = nullptr;
+    float* d_mlp = nullptr;
     double* d_partials = nullptr;
     unsigned int* d_counter = nullptr;
     DevState* d_state = nullptr;
@@ -119,6 +121,11 @@ int check_params(const mexk_context_t ctx, const mexk_params_t* p) {
         return MEXK_ERR_INVALID;
     }
     if (p->precision != MEXK_PREC_FP64 && p->precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
+    if (p->controller < MEXK_CTRL_REFERENCE || p->controller > MEXK_CTRL_LEARNED) return MEXK_ERR_INVALID;
+    if (p->controller == MEXK_CTRL_LEARNED && ctx->d_mlp == nullptr) {
+        set_error_text("learned controller requested but no controller network is loaded");
+        return MEXK_ERR_NOT_READY;
+    }
     return MEXK_OK;
 }
 
@@ -127,6 +134,9 @@ int ensure_mixed(mexk_context_t ctx) {
     int rc;
     if ((rc = dalloc(&ctx->d_V32, static_cast<size_t>(ctx->ldv) * (ctx->m_alloc + 1)))) return rc;
     if ((rc = dalloc(&ctx->d_w32, static_cast<size_t>(ctx->ldv)))) return rc;
+    // Rows n..ldv-1 stay zero: the vectorised sweeps read and write them.
+    MEXK_CK(cudaMemset(ctx->d_V32, 0, sizeof(float) * static_cast<size_t>(ctx->ldv) * (ctx->m_alloc + 1)));
+    MEXK_CK(cudaMemset(ctx->d_w32, 0, sizeof(float) * static_cast<size_t>(ctx->ldv)));
     if ((rc = dalloc(&ctx->d_val32, static_cast<size_t>(ctx->nnz) + 4))) return rc;
     // FP32 copy of the matrix values (device conversion).
     std::vector<double> tmp;
@@ -145,7 +155,7 @@ int ensure_mixed(mexk_context_t ctx) {
 
 // One Krylov cycle: the unit that is captured into a graph.
 template <typename TV>
-int enqueue_cycle(mexk_context_t ctx, int m, int reortho, cudaStream_t s) {
+int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, cudaStream_t s) {
     const bool fp32 = sizeof(TV) == 4;
     TV* V = fp32 ? reinterpret_cast<TV*>(ctx->d_V32) : reinterpret_cast<TV*>(ctx->d_V);
     TV* w = fp32 ? reinterpret_cast<TV*>(ctx->d_w32) : reinterpret_cast<TV*>(ctx->d_w);
@@ -178,13 +188,26 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, cudaStream_t s) {
         if ((rc = launch_gs<TV>(GS_UPD_NORM, g, grid, s))) return rc;
         if ((rc = launch_normalize<TV>(ctx->n, j, ctx->ldv, w, V, ctx->d_state, nullptr, s))) return rc;
     }
-    ControlArgs c;
-    c.st = ctx->d_state;
-    c.H = ctx->d_H;
-    c.ldh = ctx->ldh;
-    c.coef = ctx->d_coef;
-    c.log = ctx->d_log;
-    if ((rc = launch_controller(c, m, s))) return rc;
+    if (ctrl == MEXK_CTRL_REFERENCE) {
+        ControlArgs c;
+        c.st = ctx->d_state;
+        c.H = ctx->d_H;
+        c.ldh = ctx->ldh;
+        c.coef = ctx->d_coef;
+        c.log = ctx->d_log;
+        if ((rc = launch_controller(c, m, s))) return rc;
+    } else {
+        SearchArgs c;
+        c.st = ctx->d_state;
+        c.H = ctx->d_H;
+        c.ldh = ctx->ldh;
+        c.coef = ctx->d_coef;
+        c.log = ctx->d_log;
+        c.cand = ctx->d_cand;
+        c.counter = ctx->d_counter + 1;
+        c.mlp = ctrl == MEXK_CTRL_LEARNED ? ctx->d_mlp : nullptr;
+        if ((rc = launch_controller_search(c, m, s))) return rc;
+    }
     LiftArgs l;
     l.n = ctx->n;
     l.ldv = ctx->ldv;
@@ -198,21 +221,21 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, cudaStream_t s) {
     return launch_restart<TV>(ctx->n, ctx->ldv, ctx->d_y, V, ctx->d_state, s);
 }
 
-int enqueue_cycle_any(mexk_context_t ctx, int m, int prec, int reortho, cudaStream_t s) {
-    return prec == MEXK_PREC_MIXED ? enqueue_cycle<float>(ctx, m, reortho, s)
-                                   : enqueue_cycle<double>(ctx, m, reortho, s);
+int enqueue_cycle_any(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, cudaStream_t s) {
+    return prec == MEXK_PREC_MIXED ? enqueue_cycle<float>(ctx, m, reortho, ctrl, s)
+                                   : enqueue_cycle<double>(ctx, m, reortho, ctrl, s);
 }
 
-int get_graph(mexk_context_t ctx, int m, int prec, int reortho, cudaGraphExec_t* out) {
+int get_graph(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, cudaGraphExec_t* out) {
     for (auto& g : ctx->graphs) {
-        if (g.m == m && g.prec == prec && g.reortho == reortho) {
+        if (g.m == m && g.prec == prec && g.reortho == reortho && g.ctrl == ctrl) {
             *out = g.exec;
             return MEXK_OK;
         }
     }
     cudaGraph_t graph = nullptr;
     MEXK_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_cycle_any(ctx, m, prec, reortho, ctx->stream);
+    int rc = enqueue_cycle_any(ctx, m, prec, reortho, ctrl, ctx->stream);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
     if (rc != MEXK_OK) {
         if (graph) cudaGraphDestroy(graph);
@@ -229,7 +252,7 @@ int get_graph(mexk_context_t ctx, int m, int prec, int reortho, cudaGraphExec_t*
         set_cuda_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
         return MEXK_ERR_CUDA;
     }
-    ctx->graphs.push_back({m, prec, reortho, exec});
+    ctx->graphs.push_back({m, prec, reortho, ctrl, exec});
     *out = exec;
     return MEXK_OK;
 }
@@ -253,6 +276,11 @@ void init_state(DevState* st, const mexk_params_t* p, int log_cap) {
     dt = std::min(dt, st->total_t - st->t_done);
     st->dt = dt;
     st->k_used = p->m;
+    st->m_next = p->m;
+    st->ctrl = p->controller;
+    st->tol_floor_rel = (p->controller != MEXK_CTRL_REFERENCE && p->precision == MEXK_PREC_MIXED)
+                            ? 5.9604644775390625e-08  // 2^-24, the FP32 unit roundoff
+                            : 0.0;
     st->log_cap = log_cap;
 }
 
@@ -276,24 +304,26 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
             rc = launch_init_start<double>(ctx->n, ctx->ldv, v_dev, ctx->d_V, ctx->d_partials, ctx->d_counter,
                                            ctx->d_state, grid, s);
         if (rc) return rc;
-        cudaGraphExec_t exec = nullptr;
-        if (ctx->use_graph) {
-            // Capture happens on the context stream; order it after `s`.
-            if (s != ctx->stream) MEXK_CK(cudaStreamSynchronize(s));
-            if ((rc = get_graph(ctx, p->m, p->precision, p->reorthogonalize ? 1 : 0, &exec))) return rc;
-        }
+        if (ctx->use_graph && s != ctx->stream) MEXK_CK(cudaStreamSynchronize(s));
         // Every cycle ends with an accepted step or an abort, so the loop is
         // bounded by max_steps; the extra margin only guards corrupt state.
         const int max_cycles = ctx->h_state->max_steps + 2;
+        const int reortho = p->reorthogonalize ? 1 : 0;
+        int m_cycle = p->m;
         for (int cyc = 0; cyc < max_cycles; ++cyc) {
-            if (exec) {
+            if (ctx->use_graph) {
+                // Graphs are captured on the context stream and launched on `s`.
+                cudaGraphExec_t exec = nullptr;
+                if ((rc = get_graph(ctx, m_cycle, p->precision, reortho, p->controller, &exec))) return rc;
                 MEXK_CK(cudaGraphLaunch(exec, s));
-            } else if ((rc = enqueue_cycle_any(ctx, p->m, p->precision, p->reorthogonalize ? 1 : 0, s))) {
+            } else if ((rc = enqueue_cycle_any(ctx, m_cycle, p->precision, reortho, p->controller, s))) {
                 return rc;
             }
             MEXK_CK(cudaMemcpyAsync(ctx->h_state, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
             MEXK_CK(cudaStreamSynchronize(s));
             if (ctx->h_state->done) break;
+            const int mn = ctx->h_state->m_next;
+            if (mn >= 1 && mn <= ctx->m_alloc && mn < ctx->n) m_cycle = mn;
         }
         if (!ctx->h_state->done) {
             set_error_text("solve did not finish within max_steps cycles");
@@ -366,6 +396,7 @@ int mexk_context_create(int device, mexk_context_t* out) {
         return MEXK_ERR_CUDA;
     }
     int rc = expm_init_attributes();
+    gs_prepare();
     if (rc) {
         cudaStreamDestroy(c->stream);
         delete c;
@@ -418,12 +449,15 @@ int mexk_context_upload_csr(mexk_context_t ctx, int rows, long long nnz, const i
     MEXK_CK(cudaMemset(ctx->d_V, 0, sizeof(double) * vcount));
     if ((rc = dalloc(&ctx->d_w, ctx->ldv))) return rc;
     if ((rc = dalloc(&ctx->d_y, ctx->ldv))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_w, 0, sizeof(double) * ctx->ldv));
+    MEXK_CK(cudaMemset(ctx->d_y, 0, sizeof(double) * ctx->ldv));
     const size_t hcount = static_cast<size_t>(ctx->ldh) * m_alloc_max;
     if ((rc = dalloc(&ctx->d_H, hcount))) return rc;
     MEXK_CK(cudaMemset(ctx->d_H, 0, sizeof(double) * hcount));
     if ((rc = dalloc(&ctx->d_h1, MEXK_M_MAX + 2))) return rc;
     if ((rc = dalloc(&ctx->d_h2, MEXK_M_MAX + 2))) return rc;
     if ((rc = dalloc(&ctx->d_coef, MEXK_M_MAX + 2))) return rc;
+    if ((rc = dalloc(&ctx->d_cand, static_cast<size_t>(SEARCH_CAND) * CAND_STRIDE))) return rc;
     if ((rc = dalloc(&ctx->d_partials, static_cast<size_t>(PARTIAL_BLOCKS) * RED_STRIDE))) return rc;
     if ((rc = dalloc(&ctx->d_counter, 4))) return rc;
     MEXK_CK(cudaMemset(ctx->d_counter, 0, sizeof(unsigned int) * 4));
@@ -459,6 +493,8 @@ int mexk_context_destroy(mexk_context_t ctx) {
     dfree(ctx->d_h1);
     dfree(ctx->d_h2);
     dfree(ctx->d_coef);
+    dfree(ctx->d_cand);
+    dfree(ctx->d_mlp);
     dfree(ctx->d_partials);
     dfree(ctx->d_counter);
     dfree(ctx->d_state);
@@ -618,12 +654,14 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
     // A running state: k = j+1 basis columns, lift pending, nothing finished.
     DevState run;
     memset(&run, 0, sizeof(run));
+    // The last solve's step size and norm (its H is still in place when the
+    // controller is profiled before the Gram-Schmidt kernels).
     run.total_t = 1.0;
-    run.dt = 1e-3;
+    run.dt = (ctx->h_state->dt > 0.0) ? ctx->h_state->dt : 1e-3;
     run.dt_max = 1.0;
     run.dt_min = 1e-12;
     run.tol = 1e300;  // every controller launch accepts its first attempt: one exponential
-    run.v_norm = 1.0;
+    run.v_norm = (ctx->h_state->v_norm > 0.0) ? ctx->h_state->v_norm : 1.0;
     run.m = j + 1;
     run.max_steps = 1 << 30;
     run.max_rejects = 20;

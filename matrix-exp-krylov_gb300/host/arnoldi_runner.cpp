@@ -134,6 +134,7 @@ void ArnoldiRunner::compute_expmv(const std::vector<double>& v_host, std::vector
     p.max_restarts = params.max_restarts;
     p.reorthogonalize = params.reorthogonalize ? 1 : 0;
     p.precision = precision;
+    p.controller = controller;
     int rc = mexk_expmv(dc.handle, &p, v_host.data(), y_host.data(), &last_result);
     if (rc != MEXK_OK) die("mexk_expmv", rc);
     converged = last_result.converged != 0;

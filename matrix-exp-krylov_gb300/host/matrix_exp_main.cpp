@@ -4,7 +4,8 @@
 // matrix, t clamp to 10/max|A_ij|, m default min(30, max(5, n-1)),
 // tolerance 1e-6, v = 0.1, OUTPUT_Y_FILE dump and summary lines. It runs on
 // one GPU. Extra flags: --precision fp64|mixed (default fp64, the
-// reference's arithmetic) and --quiet (no [STEP]/[FLOPs] lines).
+// reference's arithmetic), --controller reference|search|learned (default
+// the reference's heuristic) and --quiet (no [STEP]/[FLOPs] lines).
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -43,6 +44,7 @@ int main(int argc, char* argv[]) {
     int max_restarts_cli = MAX_RESTARTS;
     double t_cli = 1.0;
     int precision = MEXK_PREC_FP64;
+    int controller = MEXK_CTRL_REFERENCE;
     bool quiet = false;
 
     std::vector<std::string> args(argv + 1, argv + argc);
@@ -67,6 +69,17 @@ int main(int argc, char* argv[]) {
             else if (v == "fp64") precision = MEXK_PREC_FP64;
             else {
                 std::cerr << "Error: --precision must be fp64 or mixed" << std::endl;
+                return EXIT_FAILURE;
+            }
+            continue;
+        }
+        if (a == "--controller" && i + 1 < args.size()) {
+            const std::string v = args[++i];
+            if (v == "reference") controller = MEXK_CTRL_REFERENCE;
+            else if (v == "search") controller = MEXK_CTRL_SEARCH;
+            else if (v == "learned") controller = MEXK_CTRL_LEARNED;
+            else {
+                std::cerr << "Error: --controller must be reference, search or learned" << std::endl;
                 return EXIT_FAILURE;
             }
             continue;
@@ -174,6 +187,7 @@ int main(int argc, char* argv[]) {
 
     ArnoldiRunner runner(gpus_used, params, A.rows, A.cols, A.nnz);
     runner.precision = precision;
+    runner.controller = controller;
     runner.verbose = !quiet;
     runner.init_all_devices(parts, std::vector<int>{0}, ghosts);
     std::vector<double> v(static_cast<size_t>(A.rows), 0.1);

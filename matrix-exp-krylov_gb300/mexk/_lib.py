@@ -21,6 +21,9 @@ MEXK_OK = 0
 PREC_FP64 = 0
 PREC_MIXED = 1
 M_MAX = 64
+CTRL_REFERENCE = 0
+CTRL_SEARCH = 1
+CTRL_LEARNED = 2
 
 
 class MexkError(RuntimeError):
@@ -29,7 +32,7 @@ class MexkError(RuntimeError):
 
 class Params(C.Structure):
     _fields_ = [("m", C.c_int), ("t", C.c_double), ("tol", C.c_double), ("max_restarts", C.c_int),
-                ("reorthogonalize", C.c_int), ("precision", C.c_int)]
+                ("reorthogonalize", C.c_int), ("precision", C.c_int), ("controller", C.c_int)]
 
 
 class Result(C.Structure):

@@ -21,9 +21,14 @@ def _ptr(a, ct):
     return a.ctypes.data_as(C.POINTER(ct))
 
 
-def params(m, t, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64") -> Params:
+CONTROLLERS = {"reference": 0, "search": 1, "learned": 2}
+
+
+def params(m, t, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64",
+           controller="reference") -> Params:
     prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
-    return Params(int(m), float(t), float(tol), int(max_restarts), int(bool(reorthogonalize)), prec)
+    ctrl = CONTROLLERS[controller] if isinstance(controller, str) else int(controller)
+    return Params(int(m), float(t), float(tol), int(max_restarts), int(bool(reorthogonalize)), prec, ctrl)
 
 
 class Context:
@@ -70,21 +75,22 @@ class Context:
         except Exception:
             pass
 
-    def expmv(self, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64"):
+    def expmv(self, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64",
+              controller="reference"):
         """y = exp(t A) v with host vectors. Returns (y, result dict)."""
         v = np.ascontiguousarray(v, dtype=np.float64)
         if v.shape != (self.n,):
             raise ValueError("v must have length n")
         y = np.zeros(self.n)
-        p = params(m, t, tol, max_restarts, reorthogonalize, precision)
+        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller)
         r = Result()
         check(lib().mexk_expmv(self._h, C.byref(p), _ptr(v, C.c_double), _ptr(y, C.c_double), C.byref(r)),
               "mexk_expmv")
         return y, r.as_dict()
 
     def expmv_device(self, v_ptr: int, y_ptr: int, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True,
-                     precision="fp64", stream: int = 0):
-        p = params(m, t, tol, max_restarts, reorthogonalize, precision)
+                     precision="fp64", stream: int = 0, controller="reference"):
+        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller)
         r = Result()
         check(lib().mexk_expmv_device(self._h, C.byref(p), C.c_void_p(v_ptr), C.c_void_p(y_ptr),
                                       C.c_void_p(stream), C.byref(r)), "mexk_expmv_device")

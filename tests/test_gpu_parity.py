@@ -330,3 +330,46 @@ def test_heat2048_fp64_matches_reference_run():
     assert rel(y[pos], d["y_at"]) <= FP64_TOL and rel(y[:16], d["y_head"]) <= FP64_TOL
     # mixed precision: within 1e-6 of the FP64 result
     assert rel(y32, y) <= MIXED_TOL, rel(y32, y)
+
+
+# ------------------------------------------------------------------ step controllers
+@pytest.mark.parametrize("name", ["cfg0_random_n2000", "heat_N32", "powerlaw_n2048", "convdiff_N8_pe100",
+                                  "diag_n1000_kat", "rejects_skew_n300_t20_m8", "breakdown_j2_diag3"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_search_controller_accuracy(name, precision):
+    """Candidate-step control: every accepted step passes the same residual
+    test, so the result stays within the tolerance of the reference's."""
+    from mexk.api import Context
+
+    A, d = load_golden(name)
+    m = int(d["m"])
+    with Context(A, m_alloc=m) as ctx:
+        y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), max_restarts=int(d["max_restarts"]),
+                           precision=precision, controller="search")
+    assert res["converged"] == 1
+    diff = np.linalg.norm(y - d["y"])
+    bound = max(MIXED_TOL * np.linalg.norm(d["y"]), (res["restarts_done"] + int(d["restarts_done"])) * float(d["tol"]))
+    assert diff <= bound, (diff, bound)
+
+
+def test_search_controller_takes_fewer_cycles():
+    from mexk.api import Context
+
+    A, d = load_golden("heat_N32")
+    with Context(A, m_alloc=30) as ctx:
+        _, r_ref = ctx.expmv(d["v"], float(d["t"]), 30)
+        _, r_s = ctx.expmv(d["v"], float(d["t"]), 30, controller="search")
+    assert r_s["cycles"] < r_ref["cycles"], (r_s, r_ref)
+
+
+def test_search_controller_abort_path():
+    """m = 1 can never pass the residual test: candidates fail, the
+    reference shrink rule takes over and aborts after 20 rejects."""
+    from mexk.api import Context
+
+    A, d = load_golden("abort_m1_n100")
+    with Context(A, m_alloc=4) as ctx:
+        _, res = ctx.expmv(d["v"], float(d["t"]), 1, controller="search")
+        steps = ctx.steps()
+    assert res["converged"] == 0 and res["restarts_done"] == 0
+    assert steps[-1][5] == 19 and len(steps) == 19
