@@ -202,7 +202,8 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     P = make_problem()
     n, nnz, m = P.A.n, P.A.nnz, P.m
-    ctx = Context(P.A, m_alloc=m, device=local_rank)
+    # room for the Krylov dimensions the learned controller may choose (<= 60)
+    ctx = Context(P.A, m_alloc=60, device=local_rank)
     stream = torch.cuda.ExternalStream(ctx.stream)
     v_d = torch.from_numpy(P.v).cuda()
     y64 = torch.zeros(n, dtype=torch.float64, device="cuda")
@@ -213,7 +214,7 @@ def run_ours(args, rank, world, local_rank):
     # chosen form is the fastest candidate within 1e-6 of it.
     res64 = ctx.expmv_device(v_d.data_ptr(), y64.data_ptr(), P.t, m, precision="fp64")
     steps64 = ctx.steps()
-    candidates = [("mixed", "search"), ("mixed", "reference"), ("fp64", "search")]
+    candidates = [("mixed", "learned"), ("mixed", "search"), ("mixed", "reference"), ("fp64", "search")]
     if args.precision != "auto":
         candidates = [(args.precision, args.controller)]
     checked = []

@@ -140,6 +140,7 @@ struct ArnoldiRunner {
     // lines, and the statistics of the last solve.
     int precision = MEXK_PREC_FP64;
     int controller = MEXK_CTRL_REFERENCE;
+    bool net_loaded = false;
     bool verbose = true;
     mexk_result_t last_result{};
     std::vector<mexk_step_t> last_steps;

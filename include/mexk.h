@@ -155,6 +155,52 @@ int mexk_context_get_basis(mexk_context_t ctx, int precision, double* V_host, in
  * (replaces Eigen's MatrixXd::exp at main.cu:33-36). k <= MEXK_M_MAX. */
 int mexk_expm_f64(int k, const double* A, int lda, double* E, int lde, void* stream);
 
+/* ---- stepping: one cycle's pieces driven from the host ----------------- */
+/* These expose the solve's steps for callers that choose steps themselves
+ * (the learned controller's training sweeps). Host vectors/matrices.
+ * start:   V[:,0] = v/|v| (init_q1, main.cu:1574); *beta = |v|.
+ * build:   m Arnoldi steps from V[:,0] (the loop of main.cu:1451-1466);
+ *          H receives the (m+1)-by-m Hessenberg matrix (column-major, ld m+1),
+ *          *k_used the basis size (< m after a breakdown).
+ * advance: y = sum_{i<k} coef[i] V[:,i] (the lift, main.cu:1980-2001, with
+ *          coef = |v| exp(dt H_k) e1 computed by the caller), then V[:,0] =
+ *          y/|y| (restart_from_y, main.cu:2023); *beta = |y|.
+ * result:  copies the last y. */
+int mexk_krylov_start(mexk_context_t ctx, int precision, const double* v_host, double* beta);
+int mexk_krylov_build(mexk_context_t ctx, int precision, int m, int reorthogonalize, double* H, int* k_used);
+int mexk_krylov_advance(mexk_context_t ctx, int precision, int k, const double* coef, double* beta);
+int mexk_krylov_result(mexk_context_t ctx, double* y_host);
+
+/* ---- learned step controller ----------------------------------------- */
+/* Parameters of the controller network (8 -> 64 -> 64 -> 2, GELU, FP32):
+ * W1[8][64], b1[64], W2[64][64], b2[64], W3[64][2], b3[2] (4866 trained
+ * values) followed by feature mean[8], std[8], output mean[2], std[2]. */
+#define MEXK_NET_PARAMS 4866
+#define MEXK_NET_TOTAL 4886
+
+/* Loads the network used by MEXK_CTRL_LEARNED (host array of
+ * MEXK_NET_TOTAL floats). No reference counterpart (the reference's
+ * controller is the fixed heuristic of main.cu:1476-1516). */
+int mexk_context_set_controller(mexk_context_t ctx, const float* weights, int count);
+
+/* Network on N raw feature rows X[N][8] -> raw outputs Y[N][2] (device). */
+int mexk_mlp_forward(const float* weights, const float* X, int N, float* Y, void* stream);
+/* Gradient of the mean squared error of the normalised outputs over the
+ * samples idx[0..count) of X[.][8] / T[.][2] into grad[MEXK_NET_PARAMS];
+ * loss_parts receives 64 partial sums of squared errors; scratch holds
+ * 64 * MEXK_NET_PARAMS floats. All device memory. */
+int mexk_mlp_gradient(const float* weights, const float* X, const float* T, const int* idx, int count,
+                      float* grad, float* loss_parts, float* scratch, void* stream);
+/* One Adam step (beta 0.9/0.999, eps 1e-8, step >= 1) on the same loss;
+ * adam_state holds 2 * MEXK_NET_PARAMS floats (zero before step 1). */
+int mexk_mlp_adam_step(float* weights, float* adam_state, const float* X, const float* T, const int* idx,
+                       int count, int step, float lr, float* loss_parts, float* scratch, void* stream);
+/* The controller's view of a basis: out[0..7] = features of H (device,
+ * leading dimension ldh >= k+1), out[8..9] = network outputs (0 if
+ * weights is NULL), out[10] = log2 |H_k|_1. */
+int mexk_controller_predict(const float* weights, const double* H, int ldh, int k, double rem, double tol,
+                            double vnorm, double tau_prev, double err_prev, float* out, void* stream);
+
 /* ---- allocation-free variant ------------------------------------------- */
 /* Orthonormalises w against the k orthonormal FP64 columns of V (column-major,
  * leading dimension ldv) with the solver's Gram-Schmidt sweeps (two passes if

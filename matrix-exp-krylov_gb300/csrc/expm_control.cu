@@ -19,6 +19,7 @@
 // the basis depends only on A and the start vector, never on dt, so the
 // retry here reuses it and re-evaluates only the exponential: same decisions
 // and results, m SpMVs and Gram-Schmidt sweeps fewer per reject.
+#include "controller_net.cuh"
 #include "mexk_internal.cuh"
 
 #include <math.h>
@@ -475,8 +476,9 @@ __device__ void write_log(DevState* st, mexk_step_t* log, double dt, double err,
 // reference's shrink rule.
 __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchArgs a, int m) {
     extern __shared__ double smem[];
-    __shared__ int s_k, s_bd, s_flag, s_best, s_dec;
-    __shared__ double s_tau, s_center;
+    __shared__ int s_k, s_bd, s_flag, s_best, s_dec, s_mnext;
+    __shared__ double s_tau, s_center, s_n1;
+    __shared__ float s_f[net::IN], s_a1[net::HID], s_a2[net::HID], s_o[net::OUT];
     DevState* st = a.st;
     if (st->done) return;
     if (threadIdx.x == 0) {
@@ -486,6 +488,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         s_k = k;
         s_bd = bd;
         s_center = st->dt;
+        s_mnext = m;
     }
     __syncthreads();
     const int k = s_k;
@@ -493,9 +496,39 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
     const size_t ldh = static_cast<size_t>(a.ldh);
     const double rem = st->total_t - st->t_done;
     const double tol_eff = fmax(st->tol, st->tol_floor_rel * st->v_norm);
+    // Learned centre and next dimension: every block evaluates the network on
+    // the same inputs, so all agree on the candidate grid.
+    double spacing = 0.25;
+    int offset = 24;
+    if (a.mlp != nullptr) {
+        if (threadIdx.x == 0)
+            s_n1 = net::basis_features(a.H, a.ldh, k, rem, tol_eff, st->v_norm, st->tau_prev, st->err_prev, s_f);
+        __syncthreads();
+        net::mlp_forward_block(a.mlp, s_f, s_a1, s_a2, s_o);
+        if (threadIdx.x == 0) {
+            double c = exp2(static_cast<double>(s_o[0])) / s_n1;
+            c = c > st->dt_min ? c : st->dt_min;
+            s_center = c < rem ? c : rem;
+            s_mnext = net::next_m_from(s_o[1], a.m_cap);
+        }
+        __syncthreads();
+    }
     ExpmBuf B = carve(smem, k);
     {
-        double tau = s_center * exp2(0.25 * (static_cast<int>(blockIdx.x) - 24));
+        // With a network: candidates 0..15 on a 1/8-octave grid around its
+        // prediction (2^-1 .. 2^0.875), 16..31 on the quarter-octave grid the
+        // search uses around twice the previous step (2^-4 .. 2^-0.25 of it),
+        // so a poor prediction degrades to a coarser search.
+        const int g = static_cast<int>(blockIdx.x);
+        double tau;
+        if (a.mlp != nullptr && g < SEARCH_CAND / 2) {
+            tau = s_center * exp2(0.125 * (g - 8));
+        } else if (a.mlp != nullptr) {
+            const double base = st->tau_prev > 0.0 ? 2.0 * st->tau_prev : st->dt;
+            tau = base * exp2(0.25 * (g - SEARCH_CAND / 2 - 15));
+        } else {
+            tau = s_center * exp2(spacing * (g - offset));
+        }
         tau = tau < rem ? tau : rem;
         for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = tau * a.H[(e % k) + (e / k) * ldh];
         __syncthreads();
@@ -528,8 +561,8 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         if (threadIdx.x == 0) {
             const double tau = __ldcg(&c[1]), err = __ldcg(&c[0]);
             write_log(st, a.log, tau, err, k, 0);
-            // next centre: double the step (the grid reaches 1/64 of it)
-            finish_cycle(st, true, tau, err, k, m, 2.0 * tau, false);
+            // next centre without a network: double the step (the grid reaches 1/64 of it)
+            finish_cycle(st, true, tau, err, k, s_mnext, 2.0 * tau, false);
         }
         return;
     }
@@ -566,7 +599,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         const double wi = (i < k) ? R[i] : 0.0;
         a.coef[i] = (fabs(wi) > 1e-15) ? vn * wi : 0.0;
     }
-    if (threadIdx.x == 0) finish_cycle(st, s_dec == DEC_ACCEPT, s_tau, err, k, m, 2.0 * s_tau, false);
+    if (threadIdx.x == 0) finish_cycle(st, s_dec == DEC_ACCEPT, s_tau, err, k, s_mnext, 2.0 * s_tau, false);
 }
 
 }  // namespace

@@ -85,64 +85,6 @@ __device__ __forceinline__ double transpose_reduce(double (&a)[K], int lane) {
     return v;
 }
 
-// 16-byte row-group loads: RPT consecutive rows of one basis column.
-template <int RPT, typename TV>
-struct RowIO;
-template <>
-struct RowIO<1, double> {
-    static __device__ __forceinline__ void ld(const double* p, double (&o)[1]) { o[0] = *p; }
-    static __device__ __forceinline__ void ldg(const double* p, double (&o)[1]) { o[0] = __ldg(p); }
-    static __device__ __forceinline__ void ldcs(const double* p, double (&o)[1]) { o[0] = __ldcs(p); }
-    static __device__ __forceinline__ void st(double* p, const double (&o)[1]) { *p = o[0]; }
-};
-template <>
-struct RowIO<2, double> {
-    static __device__ __forceinline__ void put(const double2 t, double (&o)[2]) {
-        o[0] = t.x;
-        o[1] = t.y;
-    }
-    static __device__ __forceinline__ void ld(const double* p, double (&o)[2]) {
-        put(*reinterpret_cast<const double2*>(p), o);
-    }
-    static __device__ __forceinline__ void ldg(const double* p, double (&o)[2]) {
-        put(__ldg(reinterpret_cast<const double2*>(p)), o);
-    }
-    static __device__ __forceinline__ void ldcs(const double* p, double (&o)[2]) {
-        put(__ldcs(reinterpret_cast<const double2*>(p)), o);
-    }
-    static __device__ __forceinline__ void st(double* p, const double (&o)[2]) {
-        *reinterpret_cast<double2*>(p) = make_double2(o[0], o[1]);
-    }
-};
-template <>
-struct RowIO<1, float> {
-    static __device__ __forceinline__ void ld(const float* p, float (&o)[1]) { o[0] = *p; }
-    static __device__ __forceinline__ void ldg(const float* p, float (&o)[1]) { o[0] = __ldg(p); }
-    static __device__ __forceinline__ void ldcs(const float* p, float (&o)[1]) { o[0] = __ldcs(p); }
-    static __device__ __forceinline__ void st(float* p, const float (&o)[1]) { *p = o[0]; }
-};
-template <>
-struct RowIO<4, float> {
-    static __device__ __forceinline__ void put(const float4 t, float (&o)[4]) {
-        o[0] = t.x;
-        o[1] = t.y;
-        o[2] = t.z;
-        o[3] = t.w;
-    }
-    static __device__ __forceinline__ void ld(const float* p, float (&o)[4]) {
-        put(*reinterpret_cast<const float4*>(p), o);
-    }
-    static __device__ __forceinline__ void ldg(const float* p, float (&o)[4]) {
-        put(__ldg(reinterpret_cast<const float4*>(p)), o);
-    }
-    static __device__ __forceinline__ void ldcs(const float* p, float (&o)[4]) {
-        put(__ldcs(reinterpret_cast<const float4*>(p)), o);
-    }
-    static __device__ __forceinline__ void st(float* p, const float (&o)[4]) {
-        *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
-    }
-};
-
 // Dot of RPT row values into an accumulator: FP64 chains DFMAs; FP32 sums the
 // RPT products in FP32 and adds the group sum with compensation.
 template <int RPT>

@@ -20,34 +20,62 @@ namespace {
 
 constexpr int LIFT_THREADS = 256;
 
-// One row of y = sum_c coef_c V_c. FP64 basis: a DFMA chain in column order
-// (the axpy order). FP32 basis: FP32 products summed with compensation and
-// widened once per row, so the FP64 pipe does O(1) work per row, not O(k).
-template <typename TV>
-__device__ __forceinline__ double lift_row(const TV* __restrict__ V, size_t ldv, int r, int k, const double* c64,
-                                           const float* c32);
-template <>
-__device__ __forceinline__ double lift_row<double>(const double* __restrict__ V, size_t ldv, int r, int k,
-                                                   const double* c64, const float*) {
-    double s = 0.0;
-    for (int c = 0; c < k; ++c) s = fma(c64[c], __ldcs(&V[c * ldv + r]), s);
-    return s;
-}
-template <>
-__device__ __forceinline__ double lift_row<float>(const float* __restrict__ V, size_t ldv, int r, int k,
-                                                  const double*, const float* c32) {
-    float s = 0.f, comp = 0.f;
-    for (int c = 0; c < k; ++c) {
-        const float y = __fmaf_rn(c32[c], __ldcs(&V[c * ldv + r]), -comp);
-        const float t = __fadd_rn(s, y);
-        comp = __fsub_rn(__fsub_rn(t, s), y);
-        s = t;
+// RPT rows of y = sum_c coef_c V_c, columns loaded 8 at a time (16-byte
+// row groups). FP64 basis: one DFMA chain per row in column order (the axpy
+// order). FP32 basis: FP32 products summed with compensation and widened
+// once per row, so the FP64 pipe does O(1) work per row, not O(k).
+template <typename TV, int RPT>
+__device__ __forceinline__ void lift_rows(const TV* __restrict__ V, size_t ldv, size_t r0, int k, const double* c64,
+                                          const float* c32, double (&y)[RPT]) {
+    constexpr int CH = 8;
+    using IO = RowIO<RPT, TV>;
+    if constexpr (sizeof(TV) == 8) {
+        double s[RPT];
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) s[i] = 0.0;
+        for (int cb = 0; cb < k; cb += CH) {
+            TV vv[CH][RPT];
+#pragma unroll
+            for (int cc = 0; cc < CH; ++cc)
+                if (cb + cc < k) IO::ldcs(V + (cb + cc) * ldv + r0, vv[cc]);
+#pragma unroll
+            for (int cc = 0; cc < CH; ++cc)
+                if (cb + cc < k) {
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i) s[i] = fma(c64[cb + cc], static_cast<double>(vv[cc][i]), s[i]);
+                }
+        }
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) y[i] = s[i];
+    } else {
+        float s[RPT], comp[RPT];
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) s[i] = comp[i] = 0.f;
+        for (int cb = 0; cb < k; cb += CH) {
+            TV vv[CH][RPT];
+#pragma unroll
+            for (int cc = 0; cc < CH; ++cc)
+                if (cb + cc < k) IO::ldcs(V + (cb + cc) * ldv + r0, vv[cc]);
+#pragma unroll
+            for (int cc = 0; cc < CH; ++cc)
+                if (cb + cc < k) {
+#pragma unroll
+                    for (int i = 0; i < RPT; ++i) {
+                        const float yv = __fmaf_rn(c32[cb + cc], static_cast<float>(vv[cc][i]), -comp[i]);
+                        const float t = __fadd_rn(s[i], yv);
+                        comp[i] = __fsub_rn(__fsub_rn(t, s[i]), yv);
+                        s[i] = t;
+                    }
+                }
+        }
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) y[i] = static_cast<double>(s[i]) - static_cast<double>(comp[i]);
     }
-    return static_cast<double>(s) - static_cast<double>(comp);
 }
 
 template <typename TV>
 __global__ void __launch_bounds__(LIFT_THREADS) lift_kernel(LiftArgs a) {
+    constexpr int RPT = 16 / sizeof(TV);
     __shared__ double s_coef[MEXK_M_MAX + 1];
     __shared__ float s_coef32[MEXK_M_MAX + 1];
     __shared__ double s_red[32];
@@ -64,11 +92,30 @@ __global__ void __launch_bounds__(LIFT_THREADS) lift_kernel(LiftArgs a) {
     __syncthreads();
     const TV* __restrict__ V = static_cast<const TV*>(a.V);
     const size_t ldv = static_cast<size_t>(a.ldv);
+    const bool vec = (reinterpret_cast<uintptr_t>(V) % 16 == 0) && (a.ldv % RPT == 0) &&
+                     (reinterpret_cast<uintptr_t>(a.y) % 16 == 0);
+    const int stride = gridDim.x * LIFT_THREADS;
     double nacc = 0.0;
-    for (int r = blockIdx.x * LIFT_THREADS + threadIdx.x; r < a.n; r += gridDim.x * LIFT_THREADS) {
-        const double s = lift_row<TV>(V, ldv, r, k, s_coef, s_coef32);
-        a.y[r] = s;
-        nacc = fma(s, s, nacc);
+    int r_tail = 0;
+    if (vec) {
+        const int ng = a.n / RPT;
+        for (int g = blockIdx.x * LIFT_THREADS + threadIdx.x; g < ng; g += stride) {
+            double y[RPT];
+            lift_rows<TV, RPT>(V, ldv, static_cast<size_t>(g) * RPT, k, s_coef, s_coef32, y);
+#pragma unroll
+            for (int i = 0; i < RPT; i += 2) {
+                *reinterpret_cast<double2*>(a.y + static_cast<size_t>(g) * RPT + i) = make_double2(y[i], y[i + 1]);
+                nacc = fma(y[i], y[i], nacc);
+                nacc = fma(y[i + 1], y[i + 1], nacc);
+            }
+        }
+        r_tail = ng * RPT;
+    }
+    for (int r = r_tail + blockIdx.x * LIFT_THREADS + threadIdx.x; r < a.n; r += stride) {
+        double y[1];
+        lift_rows<TV, 1>(V, ldv, static_cast<size_t>(r), k, s_coef, s_coef32, y);
+        a.y[r] = y[0];
+        nacc = fma(y[0], y[0], nacc);
     }
     nacc = warp_sum(nacc);
     if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = nacc;

@@ -206,6 +206,7 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, cudaStream_t
         c.cand = ctx->d_cand;
         c.counter = ctx->d_counter + 1;
         c.mlp = ctrl == MEXK_CTRL_LEARNED ? ctx->d_mlp : nullptr;
+        c.m_cap = ctx->m_alloc < ctx->n - 1 ? ctx->m_alloc : ctx->n - 1;
         if ((rc = launch_controller_search(c, m, s))) return rc;
     }
     LiftArgs l;
@@ -639,6 +640,153 @@ int mexk_arnoldi_step(mexk_context_t ctx, int j, int reorthogonalize, int precis
     for (int i = 0; i <= j; ++i) h[i] = col[i];
     *beta = col[j + 1];
     *ok = hs->breakdown ? 0 : 1;
+    return MEXK_OK;
+}
+
+// ---- stepping: the cycle's pieces driven from the host --------------------
+int mexk_krylov_start(mexk_context_t ctx, int precision, const double* v_host, double* beta) {
+    if (!ctx || !ctx->uploaded || !v_host || !beta) return MEXK_ERR_INVALID;
+    if (precision != MEXK_PREC_FP64 && precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    int rc;
+    if (precision == MEXK_PREC_MIXED && (rc = ensure_mixed(ctx))) return rc;
+    cudaStream_t s = ctx->stream;
+    memset(ctx->h_state, 0, sizeof(DevState));
+    ctx->h_state->restart = 1;
+    MEXK_CK(cudaMemcpyAsync(ctx->d_state, ctx->h_state, sizeof(DevState), cudaMemcpyHostToDevice, s));
+    MEXK_CK(cudaMemcpyAsync(ctx->d_y, v_host, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, s));
+    const int grid = gs_grid_size(ctx->n, 1, false);
+    rc = precision == MEXK_PREC_MIXED
+             ? launch_init_start<float>(ctx->n, ctx->ldv, ctx->d_y, ctx->d_V32, ctx->d_partials, ctx->d_counter,
+                                        ctx->d_state, grid, s)
+             : launch_init_start<double>(ctx->n, ctx->ldv, ctx->d_y, ctx->d_V, ctx->d_partials, ctx->d_counter,
+                                         ctx->d_state, grid, s);
+    if (rc) return rc;
+    MEXK_CK(cudaMemcpyAsync(ctx->h_state, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    MEXK_CK(cudaStreamSynchronize(s));
+    *beta = ctx->h_state->v_norm;
+    return MEXK_OK;
+}
+
+int mexk_krylov_build(mexk_context_t ctx, int precision, int m, int reorthogonalize, double* H, int* k_used) {
+    if (!ctx || !ctx->uploaded || !H || !k_used || m < 1 || m > ctx->m_alloc || m >= ctx->n)
+        return MEXK_ERR_INVALID;
+    if (precision != MEXK_PREC_FP64 && precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    int rc;
+    if (precision == MEXK_PREC_MIXED && (rc = ensure_mixed(ctx))) return rc;
+    cudaStream_t s = ctx->stream;
+    DevState* hs = ctx->h_state;
+    hs->done = 0;
+    hs->breakdown = 0;
+    hs->m = m;
+    hs->k_used = m;
+    MEXK_CK(cudaMemcpyAsync(ctx->d_state, hs, sizeof(DevState), cudaMemcpyHostToDevice, s));
+    const size_t ldv = static_cast<size_t>(ctx->ldv);
+    const bool fp32 = precision == MEXK_PREC_MIXED;
+    for (int j = 0; j < m; ++j) {
+        GsArgs g;
+        g.n = ctx->n;
+        g.k = j + 1;
+        g.j = j;
+        g.ldv = ctx->ldv;
+        g.ldh = ctx->ldh;
+        g.reortho = reorthogonalize ? 1 : 0;
+        g.V = fp32 ? static_cast<const void*>(ctx->d_V32) : static_cast<const void*>(ctx->d_V);
+        g.w = fp32 ? static_cast<void*>(ctx->d_w32) : static_cast<void*>(ctx->d_w);
+        g.H = ctx->d_H;
+        g.h1 = ctx->d_h1;
+        g.h2 = ctx->d_h2;
+        g.partials = ctx->d_partials;
+        g.counter = ctx->d_counter;
+        g.st = ctx->d_state;
+        g.beta_out = nullptr;
+        const int grid = gs_grid_size(ctx->n, j + 1, fp32);
+        if (fp32) {
+            if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
+                                                ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32,
+                                                &ctx->d_state->breakdown, s)))
+                return rc;
+            if ((rc = launch_gs<float>(GS_DOT, g, grid, s))) return rc;
+            if (g.reortho && (rc = launch_gs<float>(GS_UPD_DOT, g, grid, s))) return rc;
+            if ((rc = launch_gs<float>(GS_UPD_NORM, g, grid, s))) return rc;
+            if ((rc = launch_normalize<float>(ctx->n, j, ctx->ldv, ctx->d_w32, ctx->d_V32, ctx->d_state, nullptr, s)))
+                return rc;
+        } else {
+            if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
+                                                  ctx->d_val, ctx->d_V + j * ldv, ctx->d_w,
+                                                  &ctx->d_state->breakdown, s)))
+                return rc;
+            if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
+            if (g.reortho && (rc = launch_gs<double>(GS_UPD_DOT, g, grid, s))) return rc;
+            if ((rc = launch_gs<double>(GS_UPD_NORM, g, grid, s))) return rc;
+            if ((rc = launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s)))
+                return rc;
+        }
+    }
+    MEXK_CK(cudaMemcpy2DAsync(H, sizeof(double) * (m + 1), ctx->d_H, sizeof(double) * ctx->ldh,
+                              sizeof(double) * (m + 1), m, cudaMemcpyDeviceToHost, s));
+    MEXK_CK(cudaMemcpyAsync(hs, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    MEXK_CK(cudaStreamSynchronize(s));
+    *k_used = hs->breakdown ? hs->k_used : m;
+    // Entries below the subdiagonal and columns past a breakdown are zero.
+    for (int j = 0; j < m; ++j)
+        for (int i = 0; i <= m; ++i)
+            if (i > j + 1 || j >= *k_used || (i == j + 1 && j == *k_used - 1 && hs->breakdown))
+                H[i + static_cast<size_t>(j) * (m + 1)] = 0.0;
+    return MEXK_OK;
+}
+
+int mexk_krylov_advance(mexk_context_t ctx, int precision, int k, const double* coef, double* beta) {
+    if (!ctx || !ctx->uploaded || !coef || !beta || k < 1 || k > ctx->m_alloc + 1) return MEXK_ERR_INVALID;
+    if (precision != MEXK_PREC_FP64 && precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    DevState* hs = ctx->h_state;
+    hs->done = 0;
+    hs->lift = 1;
+    hs->restart = 1;
+    hs->k_lift = k;
+    MEXK_CK(cudaMemcpyAsync(ctx->d_state, hs, sizeof(DevState), cudaMemcpyHostToDevice, s));
+    MEXK_CK(cudaMemcpyAsync(ctx->d_coef, coef, sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    const bool fp32 = precision == MEXK_PREC_MIXED;
+    LiftArgs l;
+    l.n = ctx->n;
+    l.ldv = ctx->ldv;
+    l.V = fp32 ? static_cast<const void*>(ctx->d_V32) : static_cast<const void*>(ctx->d_V);
+    l.coef = ctx->d_coef;
+    l.y = ctx->d_y;
+    l.partials = ctx->d_partials;
+    l.counter = ctx->d_counter;
+    l.st = ctx->d_state;
+    int rc = fp32 ? launch_lift<float>(l, gs_grid_size(ctx->n, 1, false), s)
+                  : launch_lift<double>(l, gs_grid_size(ctx->n, 1, false), s);
+    if (rc) return rc;
+    rc = fp32 ? launch_restart<float>(ctx->n, ctx->ldv, ctx->d_y, ctx->d_V32, ctx->d_state, s)
+              : launch_restart<double>(ctx->n, ctx->ldv, ctx->d_y, ctx->d_V, ctx->d_state, s);
+    if (rc) return rc;
+    MEXK_CK(cudaMemcpyAsync(hs, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    MEXK_CK(cudaStreamSynchronize(s));
+    *beta = hs->v_norm;
+    return MEXK_OK;
+}
+
+int mexk_krylov_result(mexk_context_t ctx, double* y_host) {
+    if (!ctx || !ctx->uploaded || !y_host) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    MEXK_CK(cudaMemcpy(y_host, ctx->d_y, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost));
+    return MEXK_OK;
+}
+
+int mexk_context_set_controller(mexk_context_t ctx, const float* weights, int count) {
+    if (!ctx || !weights || count != 4886) {
+        set_error_text("controller network must have 4886 parameters");
+        return MEXK_ERR_INVALID;
+    }
+    MEXK_CK(cudaSetDevice(ctx->device));
+    int rc;
+    if (!ctx->d_mlp && (rc = dalloc(&ctx->d_mlp, static_cast<size_t>(count)))) return rc;
+    MEXK_CK(cudaMemcpy(ctx->d_mlp, weights, sizeof(float) * count, cudaMemcpyHostToDevice));
     return MEXK_OK;
 }
 

@@ -11,9 +11,36 @@
 #include <iostream>
 #include <vector>
 
+#include <dlfcn.h>
+
+#include <fstream>
+#include <string>
+
 #include "matrix_exp_krylov.hpp"
 
 namespace {
+
+// The trained controller network: $MEXK_CONTROLLER_NET, else the file the
+// package ships next to the build directory (../mexk/controller_net.f32).
+std::vector<float> load_controller_net() {
+    std::string path;
+    if (const char* env = std::getenv("MEXK_CONTROLLER_NET"); env && env[0]) {
+        path = env;
+    } else {
+        Dl_info info;
+        if (dladdr(reinterpret_cast<void*>(&load_controller_net), &info) && info.dli_fname) {
+            std::string lib(info.dli_fname);
+            path = lib.substr(0, lib.find_last_of('/')) + "/../mexk/controller_net.f32";
+        }
+    }
+    std::ifstream f(path, std::ios::binary);
+    std::vector<float> w(MEXK_NET_TOTAL);
+    if (!f || !f.read(reinterpret_cast<char*>(w.data()), sizeof(float) * w.size())) {
+        std::cerr << "Error: could not read the controller network from " << path << std::endl;
+        std::exit(EXIT_FAILURE);
+    }
+    return w;
+}
 
 [[noreturn]] void die(const char* what, int rc) {
     std::cerr << "mexk Error: " << what << ": " << mexk_error_string(rc);
@@ -135,6 +162,12 @@ void ArnoldiRunner::compute_expmv(const std::vector<double>& v_host, std::vector
     p.reorthogonalize = params.reorthogonalize ? 1 : 0;
     p.precision = precision;
     p.controller = controller;
+    if (controller == MEXK_CTRL_LEARNED && !net_loaded) {
+        const std::vector<float> w = load_controller_net();
+        const int lrc = mexk_context_set_controller(dc.handle, w.data(), static_cast<int>(w.size()));
+        if (lrc != MEXK_OK) die("mexk_context_set_controller", lrc);
+        net_loaded = true;
+    }
     int rc = mexk_expmv(dc.handle, &p, v_host.data(), y_host.data(), &last_result);
     if (rc != MEXK_OK) die("mexk_expmv", rc);
     converged = last_result.converged != 0;

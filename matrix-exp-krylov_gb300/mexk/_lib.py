@@ -74,6 +74,16 @@ _PROTOS = {
     "mexk_profile_kernel": ([_VP, C.c_int, C.c_int, C.c_int, C.c_int, _DP], C.c_int),
     "mexk_gram_schmidt_f64_noalloc": ([C.c_int, C.c_int, _VP, C.c_int, _VP, C.c_int, _VP, _VP, _VP, _VP],
                                       C.c_int),
+    "mexk_context_set_controller": ([_VP, C.POINTER(C.c_float), C.c_int], C.c_int),
+    "mexk_krylov_start": ([_VP, C.c_int, _DP, _DP], C.c_int),
+    "mexk_krylov_build": ([_VP, C.c_int, C.c_int, C.c_int, _DP, _IP], C.c_int),
+    "mexk_krylov_advance": ([_VP, C.c_int, C.c_int, _DP, _DP], C.c_int),
+    "mexk_krylov_result": ([_VP, _DP], C.c_int),
+    "mexk_mlp_forward": ([_VP, _VP, C.c_int, _VP, _VP], C.c_int),
+    "mexk_mlp_gradient": ([_VP, _VP, _VP, _VP, C.c_int, _VP, _VP, _VP, _VP], C.c_int),
+    "mexk_mlp_adam_step": ([_VP, _VP, _VP, _VP, _VP, C.c_int, C.c_int, C.c_float, _VP, _VP, _VP], C.c_int),
+    "mexk_controller_predict": ([_VP, _VP, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, _VP, _VP], C.c_int),
 }
 
 KERNELS = {"spmv": 0, "gs_dot": 1, "gs_upd_dot": 2, "gs_upd_norm": 3, "normalize": 4, "lift": 5, "controller": 6}

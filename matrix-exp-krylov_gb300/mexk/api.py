@@ -36,6 +36,7 @@ class Context:
 
     def __init__(self, A, m_alloc: int = 30, device: int = 0):
         self._h = C.c_void_p()
+        self._net_loaded = False
         check(lib().mexk_context_create(device, C.byref(self._h)), "mexk_context_create")
         self.n = int(A.n)
         self.nnz = int(A.nnz)
@@ -75,9 +76,24 @@ class Context:
         except Exception:
             pass
 
+    def load_controller(self, path=None):
+        """Loads the learned controller's network (default: the trained file
+        shipped with the package)."""
+        from . import controller as K
+
+        w = np.ascontiguousarray(K.load(path or K.WEIGHTS), dtype=np.float32)
+        check(lib().mexk_context_set_controller(self._h, w.ctypes.data_as(C.POINTER(C.c_float)), w.size),
+              "mexk_context_set_controller")
+        self._net_loaded = True
+
+    def _ensure_net(self, controller):
+        if controller in ("learned", 2) and not self._net_loaded:
+            self.load_controller()
+
     def expmv(self, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64",
               controller="reference"):
         """y = exp(t A) v with host vectors. Returns (y, result dict)."""
+        self._ensure_net(controller)
         v = np.ascontiguousarray(v, dtype=np.float64)
         if v.shape != (self.n,):
             raise ValueError("v must have length n")
@@ -90,6 +106,7 @@ class Context:
 
     def expmv_device(self, v_ptr: int, y_ptr: int, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True,
                      precision="fp64", stream: int = 0, controller="reference"):
+        self._ensure_net(controller)
         p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller)
         r = Result()
         check(lib().mexk_expmv_device(self._h, C.byref(p), C.c_void_p(v_ptr), C.c_void_p(y_ptr),

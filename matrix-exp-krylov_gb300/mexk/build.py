@@ -95,7 +95,7 @@ def build_host() -> None:
     base = [cxx, "-O2", "-std=c++17", "-fPIC", "-Wall", "-I", INCLUDE]
     rpath = ["-Wl,-rpath,$ORIGIN", "-L", OUT]
     if _newer(hlib, host_srcs + hdrs + [os.path.join(OUT, "libmexk.so")]):
-        _run(base + zl[0] + ["-shared", "-o", hlib] + host_srcs + rpath + ["-lmexk"] + zl[1])
+        _run(base + zl[0] + ["-shared", "-o", hlib] + host_srcs + rpath + ["-lmexk", "-ldl"] + zl[1])
     for name, src in (("matrix_exp", "matrix_exp_main.cpp"), ("csr_tool", "csr_tool.cpp")):
         exe = os.path.join(OUT, name)
         s = os.path.join(HOST, src)

@@ -1,0 +1,212 @@
+"""The learned controller's network kernels against a float64 numpy
+reference (forward, gradient), the device feature extraction against the
+host formulas, and the stepping API against a full solve."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def np_forward(w, X):
+    """float64 reference of the 8-64-64-2 GELU network and its pieces."""
+    from scipy.special import erf
+
+    from mexk.controller import NET_HID, NET_IN, NET_OUT, NET_PARAMS
+
+    w = w.astype(np.float64)
+    o = 0
+    W1 = w[o:o + NET_IN * NET_HID].reshape(NET_IN, NET_HID); o += NET_IN * NET_HID
+    b1 = w[o:o + NET_HID]; o += NET_HID
+    W2 = w[o:o + NET_HID * NET_HID].reshape(NET_HID, NET_HID); o += NET_HID * NET_HID
+    b2 = w[o:o + NET_HID]; o += NET_HID
+    W3 = w[o:o + NET_HID * NET_OUT].reshape(NET_HID, NET_OUT); o += NET_HID * NET_OUT
+    b3 = w[o:o + NET_OUT]; o += NET_OUT
+    fm, fs = w[NET_PARAMS:NET_PARAMS + 8], w[NET_PARAMS + 8:NET_PARAMS + 16]
+    om, osd = w[NET_PARAMS + 16:NET_PARAMS + 18], w[NET_PARAMS + 18:NET_PARAMS + 20]
+    g = lambda z: 0.5 * z * (1 + erf(z / np.sqrt(2)))
+    xn = (X.astype(np.float64) - fm) / fs
+    z1 = xn @ W1 + b1; a1 = g(z1)
+    z2 = a1 @ W2 + b2; a2 = g(z2)
+    z3 = a2 @ W3 + b3
+    return dict(xn=xn, z1=z1, a1=a1, z2=z2, a2=a2, z3=z3, y=z3 * osd + om, W1=W1, W2=W2, W3=W3, om=om, osd=osd)
+
+
+def np_gradient(w, X, T):
+    from scipy.special import erf
+
+    from mexk.controller import NET_PARAMS
+
+    f = np_forward(w, X)
+    B = X.shape[0]
+    tn = (T - f["om"]) / f["osd"]
+    r = f["z3"] - tn
+    loss = (r ** 2).sum()
+    d3 = 2 * r / (B * 2)
+    gp = lambda z: 0.5 * (1 + erf(z / np.sqrt(2))) + z * np.exp(-0.5 * z * z) / np.sqrt(2 * np.pi)
+    gW3 = f["a2"].T @ d3; gb3 = d3.sum(0)
+    d2 = (d3 @ f["W3"].T) * gp(f["z2"])
+    gW2 = f["a1"].T @ d2; gb2 = d2.sum(0)
+    d1 = (d2 @ f["W2"].T) * gp(f["z1"])
+    gW1 = f["xn"].T @ d1; gb1 = d1.sum(0)
+    g = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3])
+    assert g.size == NET_PARAMS
+    return g, loss
+
+
+@pytest.fixture(scope="module")
+def net_data():
+    from mexk import controller as K
+
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((300, 8)).astype(np.float32) * 3 + 1
+    T = np.stack([rng.standard_normal(300) * 4, rng.uniform(0, 1, 300)], 1).astype(np.float32)
+    w = K.init_weights(X, T, seed=3)
+    return w, X, T
+
+
+def test_mlp_forward_matches_numpy(net_data):
+    from mexk import controller as K
+
+    w, X, _ = net_data
+    Y = K.forward(w, X)
+    ref = np_forward(w, X)["y"]
+    assert np.abs(Y - ref).max() <= 2e-4 * max(1.0, np.abs(ref).max())
+
+
+def test_mlp_gradient_matches_numpy(net_data):
+    import torch
+
+    from mexk._lib import check, lib
+    from mexk.controller import NET_PARAMS
+
+    w, X, T = net_data
+    idx = np.arange(X.shape[0], dtype=np.int32)
+    wd, Xd, Td = (torch.from_numpy(a).cuda() for a in (w, X, T))
+    idd = torch.from_numpy(idx).cuda()
+    g = torch.zeros(NET_PARAMS, device="cuda")
+    parts = torch.zeros(64, device="cuda")
+    scratch = torch.zeros(64 * NET_PARAMS, device="cuda")
+    check(lib().mexk_mlp_gradient(wd.data_ptr(), Xd.data_ptr(), Td.data_ptr(), idd.data_ptr(), len(idx),
+                                  g.data_ptr(), parts.data_ptr(), scratch.data_ptr(), None))
+    torch.cuda.synchronize()
+    g_ref, loss_ref = np_gradient(w, X, T)
+    gd = g.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(gd - g_ref) <= 1e-4 * np.linalg.norm(g_ref)
+    assert abs(parts.sum().item() - loss_ref) <= 1e-4 * loss_ref
+
+
+def test_mlp_training_reduces_loss(net_data):
+    from mexk import controller as K
+
+    w0, X, _ = net_data
+    # a learnable target: smooth function of the inputs
+    T = np.stack([np.sin(X[:, 0]) + 0.5 * X[:, 1], 0.5 + 0.1 * np.tanh(X[:, 2])], 1).astype(np.float32)
+    w, losses = K.train(X, T, epochs=60, batch=64, lr=3e-3)
+    assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
+
+
+def test_device_features_match_host():
+    import torch
+
+    from mexk import controller as K
+    from mexk import synthetic as S
+    from mexk._lib import check, lib
+    from mexk.api import Context
+
+    A = S.convection_diffusion_3d(12, 100.0)
+    v = np.random.default_rng(2).uniform(0, 1, A.n)
+    m = 20
+    with Context(A, m_alloc=m) as ctx:
+        beta = C.c_double(0)
+        check(lib().mexk_krylov_start(ctx.handle, 1, v.ctypes.data_as(C.POINTER(C.c_double)), C.byref(beta)))
+        H = np.zeros((m + 1, m), order="F")
+        k = C.c_int(0)
+        check(lib().mexk_krylov_build(ctx.handle, 1, m, 1, H.ctypes.data_as(C.POINTER(C.c_double)), C.byref(k)))
+    k = k.value
+    f_host, n1 = K.features(H, k, 0.3, 1e-6, beta.value, 1e-4, 3e-7)
+    Hd = torch.from_numpy(np.asfortranarray(H).ravel(order="F")).cuda()
+    out = torch.zeros(11, device="cuda")
+    check(lib().mexk_controller_predict(None, Hd.data_ptr(), m + 1, k, 0.3, 1e-6, beta.value, 1e-4, 3e-7,
+                                        out.data_ptr(), None))
+    torch.cuda.synchronize()
+    o = out.cpu().numpy()
+    assert np.allclose(o[:8], f_host, rtol=1e-5, atol=1e-5), (o[:8], f_host)
+    assert abs(o[10] - np.log2(n1)) < 1e-4
+
+
+def test_stepping_api_reproduces_solve():
+    """start/build/advance driven by the host with the oracle's exponential
+    gives the device solve's result for a fixed step sequence."""
+    from scipy.linalg import expm
+
+    from mexk import synthetic as S
+    from mexk._lib import check, lib
+    from mexk.api import Context
+
+    A = S.random_diag_dominant(3000, 8, seed=4)
+    v = np.random.default_rng(5).standard_normal(A.n)
+    m, t = 20, 1.0
+    with Context(A, m_alloc=m) as ctx:
+        y_ref, res = ctx.expmv(v, t, m, max_restarts=4)
+        steps = ctx.steps()
+        # accepted attempts: the last one, and each one followed by a higher accept count
+        dts = [s[1] for i, s in enumerate(steps) if i == len(steps) - 1 or steps[i + 1][4] > s[4]]
+        assert len(dts) == res["restarts_done"] >= 2
+        beta = C.c_double(0)
+        check(lib().mexk_krylov_start(ctx.handle, 0, v.ctypes.data_as(C.POINTER(C.c_double)), C.byref(beta)))
+        b = beta.value
+        for dt in dts:
+            H = np.zeros((m + 1, m), order="F")
+            k = C.c_int(0)
+            check(lib().mexk_krylov_build(ctx.handle, 0, m, 1, H.ctypes.data_as(C.POINTER(C.c_double)), C.byref(k)))
+            w = expm(dt * H[:m, :m])[:, 0]
+            coef = np.ascontiguousarray(b * w)
+            nb = C.c_double(0)
+            check(lib().mexk_krylov_advance(ctx.handle, 0, m, coef.ctypes.data_as(C.POINTER(C.c_double)),
+                                            C.byref(nb)))
+            b = nb.value
+        y = np.zeros(A.n)
+        check(lib().mexk_krylov_result(ctx.handle, y.ctypes.data_as(C.POINTER(C.c_double))))
+    # scipy's expm vs the device Pade: same method family, rounding-level differences
+    assert np.linalg.norm(y - y_ref) <= 1e-11 * np.linalg.norm(y_ref)
+
+
+@pytest.mark.parametrize("case", ["convdiff36_pe300", "heat160", "skew30k"])
+def test_learned_controller_gains_over_reference(case):
+    """Held-out problems (not in the training sweeps): the trained network
+    (with the candidate search it centres) needs fewer sparse products than
+    the reference heuristic, at an error within the per-step tolerances."""
+    import time
+
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    from mexk.controller import skew_problem
+
+    if case == "convdiff36_pe300":
+        A = S.convection_diffusion_3d(36, 300.0, h=1.0 / 129)
+        v = np.random.default_rng(7).uniform(0, 1, A.n)
+        t = 4e-4
+    elif case == "heat160":
+        A = S.laplacian_2d(160, h=1.0 / 2049)
+        v = np.random.default_rng(8).uniform(0, 1, A.n)
+        t = 1e-5
+    else:
+        A = skew_problem(30000, 6, seed=77)
+        v = np.random.default_rng(9).standard_normal(A.n)
+        t = 12.0
+    with Context(A, m_alloc=60) as ctx:
+        y64, r64 = ctx.expmv(v, t, 30)
+        out = {}
+        for ctrl in ("reference", "search", "learned"):
+            ctx.expmv(v, t, 30, precision="mixed", controller=ctrl)  # graphs captured
+            t0 = time.perf_counter()
+            y, r = ctx.expmv(v, t, 30, precision="mixed", controller=ctrl)
+            out[ctrl] = (time.perf_counter() - t0, r, np.linalg.norm(y - y64) / np.linalg.norm(y64))
+    print({k: (round(v[0] * 1e3, 2), v[1]["spmv_count"], v[1]["cycles"], f"{v[2]:.2e}") for k, v in out.items()})
+    assert out["learned"][1]["spmv_count"] < out["reference"][1]["spmv_count"]
+    for ctrl, (_, r, err) in out.items():
+        assert r["converged"] == 1
+        assert err <= 1e-6, (ctrl, err)
