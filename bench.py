@@ -107,24 +107,39 @@ def kernel_bytes(kind, n, nnz, k, fp32):
     s = 4 if fp32 else 8
     if kind == "spmv":
         return nnz * (s + 4) + 4 * (n + 1) + 2 * n * s  # values+cols, row_ptr, x once, y
-    if kind == "gs_dot":
+    if kind in ("gs_dot", "gram_dot"):
         return k * n * s + n * s  # V_k, w
-    if kind in ("gs_upd_dot", "gs_upd_norm"):
-        return k * n * s + 2 * n * s  # V_k, w read + write
+    if kind in ("gs_upd_dot", "gs_upd_norm", "gram_update"):
+        return k * n * s + 2 * n * s  # V_k, w read; w (or the next column) written
     if kind == "normalize":
         return 2 * n * s
+    if kind == "gram_norm":
+        return n * s
     if kind == "lift":
         return k * n * s + 8 * n
     return 0
 
 
+def cgs2_step_bytes(n, k, fp32):
+    """Bytes of one CGS2 Gram-Schmidt step as the hot-path scope counts them:
+    two passes, each reading V_k twice and w twice and writing w once."""
+    s = 4 if fp32 else 8
+    return 2 * (2 * k * n * s + 3 * n * s)
+
+
+STEP_KINDS = {"fp64": ["spmv", "gs_dot", "gs_upd_dot", "gs_upd_norm", "normalize"],
+              "mixed": ["spmv", "gram_dot", "gram_update"]}
+CYCLE_KINDS = {"fp64": ["controller", "lift"], "mixed": ["controller", "lift", "gram_norm"]}
+
+
 def profile_cycle(ctx, m, n, nnz, precision, iters=2):
     """CUDA-event timing of every kernel kind of one Krylov cycle."""
     fp32 = precision == "mixed"
-    kinds = ["spmv", "gs_dot", "gs_upd_dot", "gs_upd_norm", "normalize"]
-    per = {k: {"ms": 0.0, "bytes": 0.0, "launches": 0} for k in kinds + ["controller", "lift"]}
+    kinds = STEP_KINDS[precision]
+    once = CYCLE_KINDS[precision]
+    per = {k: {"ms": 0.0, "bytes": 0.0, "launches": 0} for k in kinds + once}
     # The controller first: it runs on the Hessenberg matrix the last solve left.
-    for kind in ("controller", "lift"):
+    for kind in once:
         ms = ctx.profile_kernel(kind, m - 1, iters, precision)
         per[kind]["ms"] += ms
         per[kind]["bytes"] += kernel_bytes(kind, n, nnz, m, fp32)
@@ -136,6 +151,28 @@ def profile_cycle(ctx, m, n, nnz, precision, iters=2):
             per[kind]["bytes"] += kernel_bytes(kind, n, nnz, j + 1, fp32)
             per[kind]["launches"] += 1
     return per
+
+
+def launches_per_solve(ctx, precision, res, m):
+    """Kernels one solve launches: the start vector (2), then per cycle m steps
+    of (SpMV + sweeps) and the cycle's controller, lift and restart (+ the
+    mixed form's last-column norm). Cycle sizes come from the attempt log."""
+    per_step, per_cycle = (3, 4) if precision == "mixed" else (5, 3)
+    sizes = [int(s[3]) for s in ctx.steps()]
+    if len(sizes) != res["cycles"]:  # rejects reuse their cycle's basis
+        sizes = [m] * res["cycles"]
+    return 2 + sum(per_step * k + per_cycle for k in sizes)
+
+
+def gs_cgs2_equivalent(per, n, m, precision):
+    """Gram-Schmidt of one cycle against the CGS2 byte count: all GS kernel
+    time of the cycle over sum_j cgs2_step_bytes."""
+    fp32 = precision == "mixed"
+    gs = [k for k in per if k.startswith("gs_") or k.startswith("gram_") or k == "normalize"]
+    ms = sum(per[k]["ms"] for k in gs)
+    b = sum(cgs2_step_bytes(n, j + 1, fp32) for j in range(m))
+    return {"ms_per_cycle": round(ms, 4), "cgs2_bytes": b, "gbs": round(b / (ms / 1e3) / 1e9, 1),
+            "moved_bytes": sum(per[k]["bytes"] for k in gs)}
 
 
 # ------------------------------------------------------------------ CPU baseline
@@ -252,7 +289,7 @@ def run_ours(args, rank, world, local_rank):
             for _ in range(K):
                 res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), P.t, m, precision=precision,
                                        controller=controller)
-                launches += 2 + res["cycles"] * (5 * m + 3)
+                launches += launches_per_solve(ctx, precision, res, m)
             e1.record(stream)
             torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -344,6 +381,8 @@ def run_ours(args, rank, world, local_rank):
             "kernels": {f: {k: {"ms_per_cycle": round(p["ms"], 4),
                                 "gbs": round(p["bytes"] / (p["ms"] / 1e3) / 1e9, 1) if p["bytes"] else None}
                             for k, p in pp.items()} for f, pp in (("chosen", per), ("fp64", per64))},
+            "gram_schmidt_vs_cgs2_bytes": {"chosen": gs_cgs2_equivalent(per, n, m, form),
+                                           "fp64": gs_cgs2_equivalent(per64, n, m, "fp64")},
             "trace": {"fp64": [(round(s[1], 12), float(f"{s[2]:.3g}")) for s in steps64],
                       **{f"{c['precision']}+{c['controller']}": [(round(s[1], 12), float(f"{s[2]:.3g}"))
                                                                  for s in c["steps"]] for c in checked}},
@@ -354,8 +393,8 @@ def run_ours(args, rank, world, local_rank):
 
 
 def run_solve_once(local_rank):
-    """One FP64 and one mixed solve of the workload, untimed: the command
-    that ncu captures (profiles/ summaries name it)."""
+    """One mixed-precision (candidate-step controller) and one plain FP64
+    solve of the workload, untimed: the command ncu captures."""
     import torch
 
     from mexk.api import Context
@@ -363,9 +402,9 @@ def run_solve_once(local_rank):
     torch.cuda.set_device(local_rank)
     P = make_problem()
     with Context(P.A, m_alloc=P.m, device=local_rank) as ctx:
-        for prec in ("fp64", "mixed"):
-            _, res = ctx.expmv(P.v, P.t, P.m, precision=prec)
-            print(prec, res, flush=True)
+        for prec, ctrl in (("mixed", "search"), ("fp64", "reference")):
+            _, res = ctx.expmv(P.v, P.t, P.m, precision=prec, controller=ctrl)
+            print(prec, ctrl, res, flush=True)
 
 
 def main():

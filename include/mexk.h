@@ -226,20 +226,25 @@ int mexk_gram_schmidt_f64_noalloc(int n, int k, const double* V, int ldv, double
 
 /* ---- measurement ------------------------------------------------------ */
 #define MEXK_KERNEL_SPMV 0
-#define MEXK_KERNEL_GS_DOT 1      /* pass-1 dots */
-#define MEXK_KERNEL_GS_UPD_DOT 2  /* pass-1 update fused with pass-2 dots */
-#define MEXK_KERNEL_GS_UPD_NORM 3 /* pass-2 update + norm */
-#define MEXK_KERNEL_NORMALIZE 4
+#define MEXK_KERNEL_GS_DOT 1      /* FP64: pass-1 dots */
+#define MEXK_KERNEL_GS_UPD_DOT 2  /* FP64: pass-1 update fused with pass-2 dots */
+#define MEXK_KERNEL_GS_UPD_NORM 3 /* FP64: pass-2 update + norm */
+#define MEXK_KERNEL_NORMALIZE 4   /* FP64 */
 #define MEXK_KERNEL_LIFT 5
 #define MEXK_KERNEL_CONTROLLER 6
-#define MEXK_KERNEL_KINDS 7
+#define MEXK_KERNEL_GRAM_DOT 7    /* mixed: dots with w and the newest column, Gram correction */
+#define MEXK_KERNEL_GRAM_UPDATE 8 /* mixed: streaming update into the next column */
+#define MEXK_KERNEL_GRAM_NORM 9   /* mixed: norm of the last column (once per basis) */
+#define MEXK_KERNEL_KINDS 10
 
 /* Times `iters` launches of one solver kernel for Arnoldi step j (k = j+1
  * basis columns) on the context stream with a CUDA event pair around each
  * launch, on the context's current basis and matrix (run a solve first).
  * Each launch starts from a fresh running state. *ms_per_launch = mean
  * launch duration in milliseconds. No reference counterpart (the reference
- * times only the whole solve, METRIC total_compute_expmv_ms at main.cu:1570). */
+ * times only the whole solve, METRIC total_compute_expmv_ms at main.cu:1570).
+ * A kind marked FP64 or mixed returns MEXK_ERR_UNSUPPORTED for the other
+ * precision. */
 int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int iters, double* ms_per_launch);
 
 #ifdef __cplusplus

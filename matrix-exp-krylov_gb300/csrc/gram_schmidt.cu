@@ -15,9 +15,8 @@
 // reduces per-thread partials with warp butterflies, then across warps in
 // shared memory, then across blocks with a last-block-done handshake
 // (no spin waits), always in the same order, so results are deterministic.
-// FP64 storage accumulates with DFMA; FP32 storage (mixed precision)
-// multiplies in FP32 and accumulates each thread's terms with Kahan
-// compensation before the FP64 block and grid stages.
+// These are the FP64 form's sweeps (DFMA throughout); the mixed-precision
+// form orthogonalises its FP32 basis in gram_mixed.cu.
 #include "mexk_internal.cuh"
 
 #include <math.h>
@@ -38,31 +37,11 @@ struct Acc<double> {
     __device__ __forceinline__ void fma_add(double a, double b) { s = fma(a, b, s); }
     __device__ __forceinline__ double value() const { return s; }
 };
-template <>
-struct Acc<float> {
-    float s, c;
-    __device__ __forceinline__ void zero() {
-        s = 0.f;
-        c = 0.f;
-    }
-    __device__ __forceinline__ void fma_add(float a, float b) {
-        const float y = __fmaf_rn(a, b, -c);
-        const float t = __fadd_rn(s, y);
-        c = __fsub_rn(__fsub_rn(t, s), y);
-        s = t;
-    }
-    __device__ __forceinline__ double value() const { return static_cast<double>(s) - static_cast<double>(c); }
-};
-
 template <typename TV>
 struct Compute;
 template <>
 struct Compute<double> {
     using type = double;
-};
-template <>
-struct Compute<float> {
-    using type = float;
 };
 
 // Butterfly transpose-reduction of a[0..K) over the warp (K power of two,
@@ -85,19 +64,49 @@ __device__ __forceinline__ double transpose_reduce(double (&a)[K], int lane) {
     return v;
 }
 
-// Dot of RPT row values into an accumulator: FP64 chains DFMAs; FP32 sums the
-// RPT products in FP32 and adds the group sum with compensation.
+// Dot of RPT row values into an accumulator (DFMA chain).
 template <int RPT>
 __device__ __forceinline__ void acc_dot(Acc<double>& a, const double (&v)[RPT], const double (&w)[RPT]) {
 #pragma unroll
     for (int i = 0; i < RPT; ++i) a.fma_add(v[i], w[i]);
 }
-template <int RPT>
-__device__ __forceinline__ void acc_dot(Acc<float>& a, const float (&v)[RPT], const float (&w)[RPT]) {
-    float p = v[0] * w[0];
-#pragma unroll
-    for (int i = 1; i < RPT; ++i) p = __fmaf_rn(v[i], w[i], p);
-    a.fma_add(p, 1.0f);
+
+// Grid stage shared by both sweep kernels: after every block wrote its
+// partials, the last block to arrive sums them in block order and writes the
+// Hessenberg entries, the next pass's coefficients, or the norm and the
+// breakdown test (main.cu:1911).
+template <int MODE>
+__device__ __forceinline__ void gs_finish(const GsArgs& a, int ncols, double* s_out, double* s_scratch, int* s_flag) {
+    if (!grid_last_block(a.counter, s_flag)) return;
+    reduce_partials(a.partials, gridDim.x, ncols, s_out, s_scratch);
+    DevState* st = a.st;
+    const int k = a.k;
+    const int j = a.j;
+    const size_t ldh = static_cast<size_t>(a.ldh);
+    if (MODE == GS_DOT) {
+        if (threadIdx.x < k) {
+            a.h1[threadIdx.x] = s_out[threadIdx.x];
+            if (!a.reortho && a.H) a.H[threadIdx.x + j * ldh] = s_out[threadIdx.x];
+        }
+    } else if (MODE == GS_UPD_DOT) {
+        if (threadIdx.x < k) {
+            a.h2[threadIdx.x] = s_out[threadIdx.x];
+            if (a.H) a.H[threadIdx.x + j * ldh] = a.h1[threadIdx.x] + s_out[threadIdx.x];
+        }
+    } else if (threadIdx.x == 0) {
+        const double beta = sqrt(s_out[0]);
+        const bool bad = beta < 1e-14 || isnan(beta) || isinf(beta);
+        if (a.beta_out) *a.beta_out = bad ? 0.0 : beta;
+        if (a.H && j + 1 < a.ldh) a.H[(j + 1) + j * ldh] = bad ? 0.0 : beta;
+        if (st != nullptr) {
+            if (bad) {
+                st->breakdown = 1;
+                st->k_used = j + 1;
+            } else {
+                st->inv_beta = 1.0 / beta;
+            }
+        }
+    }
 }
 
 // One row group (RPT rows starting at r0) of a sweep. Columns are read in
@@ -281,40 +290,10 @@ __global__ void __launch_bounds__(GS_THREADS, (gs_min_blocks<KMAX, MODE>())) gs_
         a.partials[static_cast<size_t>(blockIdx.x) * RED_STRIDE + threadIdx.x] = s;
     }
 
-    // ---- grid reduction by the last block
-    if (!grid_last_block(a.counter, &s_flag)) return;
-    reduce_partials(a.partials, gridDim.x, ncols, s_out, s_scratch);
-    const int j = a.j;
-    const size_t ldh = static_cast<size_t>(a.ldh);
-    if (MODE == GS_DOT) {
-        if (threadIdx.x < k) {
-            a.h1[threadIdx.x] = s_out[threadIdx.x];
-            if (!a.reortho && a.H) a.H[threadIdx.x + j * ldh] = s_out[threadIdx.x];
-        }
-    } else if (MODE == GS_UPD_DOT) {
-        if (threadIdx.x < k) {
-            a.h2[threadIdx.x] = s_out[threadIdx.x];
-            if (a.H) a.H[threadIdx.x + j * ldh] = a.h1[threadIdx.x] + s_out[threadIdx.x];
-        }
-    } else if (threadIdx.x == 0) {
-        const double beta = sqrt(s_out[0]);
-        const bool bad = beta < 1e-14 || isnan(beta) || isinf(beta);
-        if (a.beta_out) *a.beta_out = bad ? 0.0 : beta;
-        if (a.H && j + 1 < a.ldh) a.H[(j + 1) + j * ldh] = bad ? 0.0 : beta;
-        if (st != nullptr) {
-            if (bad) {
-                st->breakdown = 1;
-                st->k_used = j + 1;
-            } else {
-                st->inv_beta = 1.0 / beta;
-            }
-        }
-    }
+    gs_finish<MODE>(a, ncols, s_out, s_scratch, &s_flag);
 }
 
-// V[:,j+1] = w * (1/beta) in the storage precision (FP64: the reference's
-// w * reciprocal; FP32: one conversion of 1/beta, then FP32 multiplies --
-// float<->double conversions run on the scarce FP64 pipe).
+// V[:,j+1] = w * (1/beta), the reference's multiply by the reciprocal.
 template <typename TV>
 __global__ void __launch_bounds__(256) normalize_kernel(int n, int j, int ldv, const TV* __restrict__ w,
                                                         TV* __restrict__ V, const DevState* st,
@@ -407,26 +386,15 @@ int occupancy_for(int k) {
     return occupancy_k<64, TV>();
 }
 
-int num_sms() {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
-    return sms;
-}
-
 }  // namespace
 
 // One wave of resident blocks (at most 4 per SM), fewer for short vectors.
-int gs_grid_size(int n, int k, bool fp32) {
-    int per_sm = fp32 ? occupancy_for<float>(k) : occupancy_for<double>(k);
+int gs_grid_size(int n, int k) {
+    int per_sm = occupancy_for<double>(k);
     if (per_sm > 4) per_sm = 4;
-    const int rpt = fp32 ? 4 : 2;
+    constexpr int rpt = 2;
     const long long need = (static_cast<long long>(n) + rpt * GS_THREADS - 1) / (rpt * GS_THREADS);
-    long long g = static_cast<long long>(num_sms()) * per_sm;
+    long long g = static_cast<long long>(device_sm_count()) * per_sm;
     if (need < g) g = need;
     if (g < 1) g = 1;
     return static_cast<int>(g);
@@ -434,10 +402,7 @@ int gs_grid_size(int n, int k, bool fp32) {
 
 // Resolves every occupancy query once, outside any stream capture.
 void gs_prepare() {
-    for (int k : {8, 16, 32, 64}) {
-        (void)gs_grid_size(1 << 20, k, false);
-        (void)gs_grid_size(1 << 20, k, true);
-    }
+    for (int k : {8, 16, 32, 64}) (void)gs_grid_size(1 << 20, k);
 }
 
 template <typename TV>
@@ -463,10 +428,7 @@ int launch_normalize(int n, int j, int ldv, const TV* w, TV* V, const DevState* 
 }
 
 template int launch_gs<double>(GsMode, const GsArgs&, int, cudaStream_t);
-template int launch_gs<float>(GsMode, const GsArgs&, int, cudaStream_t);
 template int launch_normalize<double>(int, int, int, const double*, double*, const DevState*,
                                       const double*, cudaStream_t);
-template int launch_normalize<float>(int, int, int, const float*, float*, const DevState*,
-                                     const double*, cudaStream_t);
 
 }  // namespace mexk

@@ -82,7 +82,7 @@ extern "C" int mexk_gram_schmidt_f64_noalloc(int n, int k, const double* V, int 
     int rc = scratch_address(&base);
     if (rc != MEXK_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    int grid = gs_grid_size(n, k, false);
+    int grid = gs_grid_size(n, k);
     if (grid > NOALLOC_MAX_BLOCKS) grid = NOALLOC_MAX_BLOCKS;
     DevState* st = reinterpret_cast<DevState*>(base + OFF_STATE);
     // A fresh running state (no breakdown, not done) and a zero block counter.

@@ -86,8 +86,9 @@ __global__ void __launch_bounds__(LIFT_THREADS) lift_kernel(LiftArgs a) {
     if (!st->lift) return;
     const int k = st->k_lift;
     for (int i = threadIdx.x; i < k; i += blockDim.x) {
-        s_coef[i] = a.coef[i];
-        s_coef32[i] = static_cast<float>(a.coef[i]);
+        const double c = a.scale ? a.coef[i] * a.scale[i] : a.coef[i];
+        s_coef[i] = c;
+        s_coef32[i] = static_cast<float>(c);
     }
     __syncthreads();
     const TV* __restrict__ V = static_cast<const TV*>(a.V);

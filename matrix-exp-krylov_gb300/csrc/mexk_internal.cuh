@@ -75,6 +75,7 @@ enum : int {
     ST_LU_SINGULAR = 1,
     ST_SMEM = 2,
     ST_BAD_K = 4,
+    ST_TIMEOUT = 8,  // a bounded wait gave up (the kernel skipped its work)
 };
 
 // ------------------------------------------------------------ constants
@@ -219,6 +220,8 @@ __device__ __forceinline__ void reduce_partials(const double* partials, int nblo
 // holds <= SPMV_TILE nonzeros and <= SPMV_TILE_ROWS rows, or one longer row.
 std::vector<int> build_row_blocks(int n, const int* row_ptr);
 
+int launch_narrow_values(const double* src, float* dst, size_t count, cudaStream_t s);
+
 template <typename TA, typename TX>
 int launch_spmv(int n, int nblocks, const int* blocks, const int* row_ptr, const int* col_idx,
                 const TA* values, const TX* x, TX* y, const int* skip_flag, cudaStream_t s);
@@ -246,12 +249,42 @@ struct GsArgs {
 
 template <typename TV>
 int launch_gs(GsMode mode, const GsArgs& a, int grid, cudaStream_t s);
-int gs_grid_size(int n, int k, bool fp32);
+int gs_grid_size(int n, int k);
 void gs_prepare();
 
 template <typename TV>
 int launch_normalize(int n, int j, int ldv, const TV* w, TV* V, const DevState* st,
                      const double* inv_beta, cudaStream_t s);
+
+// ------------------------------------------------------------ Gram-corrected sweeps (FP32 basis)
+// Column c of the FP32 basis stores u_c; the basis vector is v_c = s[c] * u_c.
+constexpr int GRAM_LD = MEXK_M_MAX + 1;         // leading dimension of G
+constexpr int GRAM_STRIDE = 2 * MEXK_M_MAX + 8; // doubles per row-block partial
+constexpr int GRAM_BOFF = MEXK_M_MAX;           // partial slots: a [0,64), b [64,128), |w|^2 128
+constexpr int GRAM_NWOFF = 2 * MEXK_M_MAX;
+constexpr int GRAM_MAX_ROW_BLOCKS = 1024;
+struct GramState {
+    double G[GRAM_LD * GRAM_LD];  // Gram matrix V^T V (unit diagonal), column-major
+    double s[MEXK_M_MAX + 2];     // column scales 1/|u_c|
+    double p[MEXK_M_MAX + 2];     // pre-scale applied when column c was written
+    float coef[MEXK_M_MAX + 8];   // update coefficients s_c h_c of the current step
+    float wsc, psc;               // update: u_{j+1} = psc * (wsc * w - sum coef_c u_c)
+};
+struct GramArgs {
+    int n, j, ldv, ldh, reortho;
+    float* V;          // FP32 basis, column-major, ldv >= 4*ceil(n/4), rows n..ldv-1 zero
+    const float* w;    // A u_j (unscaled), rows n..ldv-1 zero
+    double* H;
+    GramState* gs;
+    double* part;      // GRAM_MAX_ROW_BLOCKS x GRAM_STRIDE
+    unsigned int* counter;
+    DevState* st;
+};
+int device_sm_count();
+int launch_gram_dot(const GramArgs& a, cudaStream_t s);
+int launch_gram_update(const GramArgs& a, cudaStream_t s);
+// |u_{j+1}| -> H(j+1, j) and s[j+1] (the last step of a basis, or a single step).
+int launch_gram_norm(const GramArgs& a, cudaStream_t s);
 
 // ------------------------------------------------------------ expm / control
 // Raises the dynamic shared-memory limits of the expm kernels; call once
@@ -294,6 +327,7 @@ struct LiftArgs {
     double* partials;
     unsigned int* counter;
     DevState* st;
+    const double* scale = nullptr;  // per-column scale of the stored basis (FP32 basis)
 };
 template <typename TV>
 int launch_lift(const LiftArgs& a, int grid, cudaStream_t s);

@@ -8,13 +8,17 @@
 // exponential + controller, the lift and the restart -- is one CUDA graph
 // whose kernels read and write a device-resident state block, so the host
 // launches one graph per accepted step and syncs once to read `done`.
+// The FP64 form runs three CGS2 sweeps and a normalisation per step
+// (gram_schmidt.cu); the mixed form one reducing and one streaming sweep
+// over an FP32 basis with a device-resident Gram matrix (gram_mixed.cu).
 //
 // HBM layout per context (n rows, m_alloc maximum Krylov dimension):
 //   CSR        row_ptr int32[n+1], col_idx int32[nnz], values f64[nnz]
 //              (+ f32 copy of values for the mixed-precision form)
 //   row blocks int32[nblocks+1] SpMV schedule
 //   basis V    column-major, leading dimension ldv = n rounded up to 64,
-//              m_alloc+1 columns, f64 (+ f32 basis for the mixed form)
+//              m_alloc+1 columns, f64 (+ f32 basis for the mixed form, whose
+//              columns carry f64 scales, with the Gram matrix, in GramState)
 //   w, y       work vector (basis precision) and result (f64)
 //   H          f64 (m_alloc+1) x m_alloc column-major; h1, h2, coef f64
 //   partials   f64[4096 x RED_STRIDE] grid-reduction scratch + counter
@@ -80,6 +84,8 @@ struct mexk_context_s {
     double* d_cand = nullptr;
     float* d_mlp = nullptr;
     double* d_partials = nullptr;
+    GramState* d_gram = nullptr;
+    double* d_gram_part = nullptr;
     unsigned int* d_counter = nullptr;
     DevState* d_state = nullptr;
     DevState* h_state = nullptr;
@@ -129,6 +135,22 @@ int check_params(const mexk_context_t ctx, const mexk_params_t* p) {
     return MEXK_OK;
 }
 
+// Gram state of a basis whose first columns are orthonormal: G = I, s = p = 1.
+int reset_gram(mexk_context_t ctx, cudaStream_t s) {
+    static GramState h0;
+    static bool init = false;
+    if (!init) {
+        memset(&h0, 0, sizeof(h0));
+        for (int i = 0; i < GRAM_LD; ++i) h0.G[i + i * GRAM_LD] = 1.0;
+        for (int i = 0; i < MEXK_M_MAX + 2; ++i) h0.s[i] = h0.p[i] = 1.0;
+        h0.wsc = h0.psc = 1.0f;
+        init = true;
+    }
+    MEXK_CK(cudaMemcpyAsync(ctx->d_gram, &h0, sizeof(GramState), cudaMemcpyHostToDevice, s));
+    MEXK_CK(cudaStreamSynchronize(s));
+    return MEXK_OK;
+}
+
 int ensure_mixed(mexk_context_t ctx) {
     if (ctx->d_V32) return MEXK_OK;
     int rc;
@@ -137,20 +159,97 @@ int ensure_mixed(mexk_context_t ctx) {
     // Rows n..ldv-1 stay zero: the vectorised sweeps read and write them.
     MEXK_CK(cudaMemset(ctx->d_V32, 0, sizeof(float) * static_cast<size_t>(ctx->ldv) * (ctx->m_alloc + 1)));
     MEXK_CK(cudaMemset(ctx->d_w32, 0, sizeof(float) * static_cast<size_t>(ctx->ldv)));
+    if ((rc = dalloc(&ctx->d_gram, 1))) return rc;
+    if ((rc = dalloc(&ctx->d_gram_part, static_cast<size_t>(GRAM_MAX_ROW_BLOCKS) * GRAM_STRIDE))) return rc;
+    if ((rc = reset_gram(ctx, ctx->stream))) return rc;
     if ((rc = dalloc(&ctx->d_val32, static_cast<size_t>(ctx->nnz) + 4))) return rc;
-    // FP32 copy of the matrix values (device conversion).
-    std::vector<double> tmp;
-    // Convert on the host in slices to bound memory.
-    const size_t slice = 1u << 24;
-    std::vector<double> hv(std::min<size_t>(slice, static_cast<size_t>(ctx->nnz) + 1));
-    std::vector<float> hf(hv.size());
-    for (size_t off = 0; off < static_cast<size_t>(ctx->nnz); off += slice) {
-        const size_t cnt = std::min<size_t>(slice, static_cast<size_t>(ctx->nnz) - off);
-        MEXK_CK(cudaMemcpy(hv.data(), ctx->d_val + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost));
-        for (size_t i = 0; i < cnt; ++i) hf[i] = static_cast<float>(hv[i]);
-        MEXK_CK(cudaMemcpy(ctx->d_val32 + off, hf.data(), sizeof(float) * cnt, cudaMemcpyHostToDevice));
-    }
+    if ((rc = launch_narrow_values(ctx->d_val, ctx->d_val32, static_cast<size_t>(ctx->nnz), ctx->stream))) return rc;
+    MEXK_CK(cudaStreamSynchronize(ctx->stream));
     return MEXK_OK;
+}
+
+GsArgs gs_args(mexk_context_t ctx, int j, int reortho, bool fp32) {
+    GsArgs g;
+    g.n = ctx->n;
+    g.k = j + 1;
+    g.j = j;
+    g.ldv = ctx->ldv;
+    g.ldh = ctx->ldh;
+    g.reortho = reortho ? 1 : 0;
+    g.V = fp32 ? static_cast<const void*>(ctx->d_V32) : static_cast<const void*>(ctx->d_V);
+    g.w = fp32 ? static_cast<void*>(ctx->d_w32) : static_cast<void*>(ctx->d_w);
+    g.H = ctx->d_H;
+    g.h1 = ctx->d_h1;
+    g.h2 = ctx->d_h2;
+    g.partials = ctx->d_partials;
+    g.counter = ctx->d_counter;
+    g.st = ctx->d_state;
+    g.beta_out = nullptr;
+    return g;
+}
+
+GramArgs gram_args(mexk_context_t ctx, int j, int reortho) {
+    GramArgs g;
+    g.n = ctx->n;
+    g.j = j;
+    g.ldv = ctx->ldv;
+    g.ldh = ctx->ldh;
+    g.reortho = reortho ? 1 : 0;
+    g.V = ctx->d_V32;
+    g.w = ctx->d_w32;
+    g.H = ctx->d_H;
+    g.gs = ctx->d_gram;
+    g.part = ctx->d_gram_part;
+    g.counter = ctx->d_counter;
+    g.st = ctx->d_state;
+    return g;
+}
+
+LiftArgs lift_args(mexk_context_t ctx, bool fp32) {
+    LiftArgs l;
+    l.n = ctx->n;
+    l.ldv = ctx->ldv;
+    l.V = fp32 ? static_cast<const void*>(ctx->d_V32) : static_cast<const void*>(ctx->d_V);
+    l.coef = ctx->d_coef;
+    l.y = ctx->d_y;
+    l.partials = ctx->d_partials;
+    l.counter = ctx->d_counter;
+    l.st = ctx->d_state;
+    l.scale = fp32 ? reinterpret_cast<const double*>(reinterpret_cast<const char*>(ctx->d_gram) +
+                                                     offsetof(GramState, s))
+                   : nullptr;
+    return l;
+}
+
+// Arnoldi step j: w = A v_j, then orthogonalise into column j+1 and H(:, j).
+// The FP64 form finishes the step (H(j+1, j), normalised column); the mixed
+// form leaves H(j+1, j) to the next step's dot sweep or to finish_basis.
+int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t s) {
+    const size_t ldv = static_cast<size_t>(ctx->ldv);
+    int rc;
+    if (fp32) {
+        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
+                                            ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32,
+                                            &ctx->d_state->breakdown, s)))
+            return rc;
+        const GramArgs g = gram_args(ctx, j, reortho);
+        if ((rc = launch_gram_dot(g, s))) return rc;
+        return launch_gram_update(g, s);
+    }
+    if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
+                                          ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, &ctx->d_state->breakdown, s)))
+        return rc;
+    const GsArgs g = gs_args(ctx, j, reortho, false);
+    const int grid = gs_grid_size(ctx->n, j + 1);
+    if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
+    if (reortho && (rc = launch_gs<double>(GS_UPD_DOT, g, grid, s))) return rc;
+    if ((rc = launch_gs<double>(GS_UPD_NORM, g, grid, s))) return rc;
+    return launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s);
+}
+
+// After the last step j of a basis: H(j+1, j) of the mixed form.
+int finish_basis(mexk_context_t ctx, int j, bool fp32, cudaStream_t s) {
+    return fp32 ? launch_gram_norm(gram_args(ctx, j, 1), s) : MEXK_OK;
 }
 
 // One Krylov cycle: the unit that is captured into a graph.
@@ -158,36 +257,10 @@ template <typename TV>
 int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, cudaStream_t s) {
     const bool fp32 = sizeof(TV) == 4;
     TV* V = fp32 ? reinterpret_cast<TV*>(ctx->d_V32) : reinterpret_cast<TV*>(ctx->d_V);
-    TV* w = fp32 ? reinterpret_cast<TV*>(ctx->d_w32) : reinterpret_cast<TV*>(ctx->d_w);
-    const TV* A = fp32 ? reinterpret_cast<const TV*>(ctx->d_val32) : reinterpret_cast<const TV*>(ctx->d_val);
-    const size_t ldv = static_cast<size_t>(ctx->ldv);
     int rc;
-    for (int j = 0; j < m; ++j) {
-        rc = launch_spmv<TV, TV>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col, A,
-                                 V + j * ldv, w, &ctx->d_state->breakdown, s);
-        if (rc) return rc;
-        GsArgs g;
-        g.n = ctx->n;
-        g.k = j + 1;
-        g.j = j;
-        g.ldv = ctx->ldv;
-        g.ldh = ctx->ldh;
-        g.reortho = reortho;
-        g.V = V;
-        g.w = w;
-        g.H = ctx->d_H;
-        g.h1 = ctx->d_h1;
-        g.h2 = ctx->d_h2;
-        g.partials = ctx->d_partials;
-        g.counter = ctx->d_counter;
-        g.st = ctx->d_state;
-        g.beta_out = nullptr;
-        const int grid = gs_grid_size(ctx->n, j + 1, fp32);
-        if ((rc = launch_gs<TV>(GS_DOT, g, grid, s))) return rc;
-        if (reortho && (rc = launch_gs<TV>(GS_UPD_DOT, g, grid, s))) return rc;
-        if ((rc = launch_gs<TV>(GS_UPD_NORM, g, grid, s))) return rc;
-        if ((rc = launch_normalize<TV>(ctx->n, j, ctx->ldv, w, V, ctx->d_state, nullptr, s))) return rc;
-    }
+    for (int j = 0; j < m; ++j)
+        if ((rc = enqueue_step(ctx, j, reortho, fp32, s))) return rc;
+    if ((rc = finish_basis(ctx, m - 1, fp32, s))) return rc;
     if (ctrl == MEXK_CTRL_REFERENCE) {
         ControlArgs c;
         c.st = ctx->d_state;
@@ -209,16 +282,8 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, cudaStream_t
         c.m_cap = ctx->m_alloc < ctx->n - 1 ? ctx->m_alloc : ctx->n - 1;
         if ((rc = launch_controller_search(c, m, s))) return rc;
     }
-    LiftArgs l;
-    l.n = ctx->n;
-    l.ldv = ctx->ldv;
-    l.V = V;
-    l.coef = ctx->d_coef;
-    l.y = ctx->d_y;
-    l.partials = ctx->d_partials;
-    l.counter = ctx->d_counter;
-    l.st = ctx->d_state;
-    if ((rc = launch_lift<TV>(l, gs_grid_size(ctx->n, 1, false), s))) return rc;
+    const LiftArgs l = lift_args(ctx, fp32);
+    if ((rc = launch_lift<TV>(l, gs_grid_size(ctx->n, 1), s))) return rc;
     return launch_restart<TV>(ctx->n, ctx->ldv, ctx->d_y, V, ctx->d_state, s);
 }
 
@@ -297,7 +362,7 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
         // The reference never lifts when no step runs: y stays zero (main_cpu.cpp:467).
         MEXK_CK(cudaMemsetAsync(ctx->d_y, 0, sizeof(double) * ctx->n, s));
     } else {
-        const int grid = gs_grid_size(ctx->n, 1, false);
+        const int grid = gs_grid_size(ctx->n, 1);
         if (p->precision == MEXK_PREC_MIXED)
             rc = launch_init_start<float>(ctx->n, ctx->ldv, v_dev, ctx->d_V32, ctx->d_partials, ctx->d_counter,
                                           ctx->d_state, grid, s);
@@ -336,6 +401,10 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
     MEXK_CK(cudaMemcpyAsync(ctx->h_state, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
     MEXK_CK(cudaStreamSynchronize(s));
     const DevState* st = ctx->h_state;
+    if (st->status & ST_TIMEOUT) {
+        set_error_text("a device wait gave up (bulk copy did not complete)");
+        return MEXK_ERR_DEVICE;
+    }
     if (result) {
         result->converged = st->converged;
         result->restarts_done = st->accepted;
@@ -430,6 +499,8 @@ int mexk_context_upload_csr(mexk_context_t ctx, int rows, long long nnz, const i
     ctx->n = rows;
     ctx->nnz = nnz;
     ctx->m_alloc = m_alloc_max;
+    // Column stride: a multiple of 64 elements, so every column starts on a
+    // 256-byte boundary and the vectorised sweeps cover whole 16-byte groups.
     ctx->ldv = (rows + 63) / 64 * 64;
     ctx->ldh = m_alloc_max + 1;
     int rc;
@@ -497,6 +568,8 @@ int mexk_context_destroy(mexk_context_t ctx) {
     dfree(ctx->d_cand);
     dfree(ctx->d_mlp);
     dfree(ctx->d_partials);
+    dfree(ctx->d_gram);
+    dfree(ctx->d_gram_part);
     dfree(ctx->d_counter);
     dfree(ctx->d_state);
     dfree(ctx->d_log);
@@ -558,7 +631,8 @@ int mexk_context_set_basis(mexk_context_t ctx, int precision, const double* V_ho
     for (size_t i = 0; i < f.size(); ++i) f[i] = static_cast<float>(V_host[i]);
     MEXK_CK(cudaMemcpy2D(ctx->d_V32, sizeof(float) * ctx->ldv, f.data(), sizeof(float) * n, sizeof(float) * n,
                          ncols, cudaMemcpyHostToDevice));
-    return MEXK_OK;
+    // The given columns are taken as orthonormal: unit scales, G = I.
+    return reset_gram(ctx, ctx->stream);
 }
 
 int mexk_context_get_basis(mexk_context_t ctx, int precision, double* V_host, int ncols) {
@@ -574,7 +648,12 @@ int mexk_context_get_basis(mexk_context_t ctx, int precision, double* V_host, in
     std::vector<float> f(n * ncols);
     MEXK_CK(cudaMemcpy2D(f.data(), sizeof(float) * n, ctx->d_V32, sizeof(float) * ctx->ldv, sizeof(float) * n,
                          ncols, cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < f.size(); ++i) V_host[i] = static_cast<double>(f[i]);
+    // Stored columns are the basis vectors up to their scales.
+    std::vector<double> sc(MEXK_M_MAX + 2);
+    MEXK_CK(cudaMemcpy(sc.data(), reinterpret_cast<const char*>(ctx->d_gram) + offsetof(GramState, s),
+                       sizeof(double) * sc.size(), cudaMemcpyDeviceToHost));
+    for (int c = 0; c < ncols; ++c)
+        for (size_t i = 0; i < n; ++i) V_host[c * n + i] = static_cast<double>(f[c * n + i]) * sc[c];
     return MEXK_OK;
 }
 
@@ -593,45 +672,8 @@ int mexk_arnoldi_step(mexk_context_t ctx, int j, int reorthogonalize, int precis
     hs->k_used = ctx->m_alloc;
     MEXK_CK(cudaMemcpyAsync(ctx->d_state, hs, sizeof(DevState), cudaMemcpyHostToDevice, s));
     const bool fp32 = precision == MEXK_PREC_MIXED;
-    GsArgs g;
-    g.n = ctx->n;
-    g.k = j + 1;
-    g.j = j;
-    g.ldv = ctx->ldv;
-    g.ldh = ctx->ldh;
-    g.reortho = reorthogonalize ? 1 : 0;
-    g.H = ctx->d_H;
-    g.h1 = ctx->d_h1;
-    g.h2 = ctx->d_h2;
-    g.partials = ctx->d_partials;
-    g.counter = ctx->d_counter;
-    g.st = ctx->d_state;
-    g.beta_out = nullptr;
-    const int grid = gs_grid_size(ctx->n, j + 1, fp32);
-    const size_t ldv = static_cast<size_t>(ctx->ldv);
-    if (fp32) {
-        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
-                                            ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr, s)))
-            return rc;
-        g.V = ctx->d_V32;
-        g.w = ctx->d_w32;
-        if ((rc = launch_gs<float>(GS_DOT, g, grid, s))) return rc;
-        if (g.reortho && (rc = launch_gs<float>(GS_UPD_DOT, g, grid, s))) return rc;
-        if ((rc = launch_gs<float>(GS_UPD_NORM, g, grid, s))) return rc;
-        if ((rc = launch_normalize<float>(ctx->n, j, ctx->ldv, ctx->d_w32, ctx->d_V32, ctx->d_state, nullptr, s)))
-            return rc;
-    } else {
-        if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
-                                              ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, nullptr, s)))
-            return rc;
-        g.V = ctx->d_V;
-        g.w = ctx->d_w;
-        if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
-        if (g.reortho && (rc = launch_gs<double>(GS_UPD_DOT, g, grid, s))) return rc;
-        if ((rc = launch_gs<double>(GS_UPD_NORM, g, grid, s))) return rc;
-        if ((rc = launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s)))
-            return rc;
-    }
+    if ((rc = enqueue_step(ctx, j, reorthogonalize, fp32, s))) return rc;
+    if ((rc = finish_basis(ctx, j, fp32, s))) return rc;
     std::vector<double> col(static_cast<size_t>(ctx->ldh));
     MEXK_CK(cudaMemcpyAsync(col.data(), ctx->d_H + static_cast<size_t>(j) * ctx->ldh, sizeof(double) * ctx->ldh,
                             cudaMemcpyDeviceToHost, s));
@@ -655,7 +697,7 @@ int mexk_krylov_start(mexk_context_t ctx, int precision, const double* v_host, d
     ctx->h_state->restart = 1;
     MEXK_CK(cudaMemcpyAsync(ctx->d_state, ctx->h_state, sizeof(DevState), cudaMemcpyHostToDevice, s));
     MEXK_CK(cudaMemcpyAsync(ctx->d_y, v_host, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, s));
-    const int grid = gs_grid_size(ctx->n, 1, false);
+    const int grid = gs_grid_size(ctx->n, 1);
     rc = precision == MEXK_PREC_MIXED
              ? launch_init_start<float>(ctx->n, ctx->ldv, ctx->d_y, ctx->d_V32, ctx->d_partials, ctx->d_counter,
                                         ctx->d_state, grid, s)
@@ -682,48 +724,10 @@ int mexk_krylov_build(mexk_context_t ctx, int precision, int m, int reorthogonal
     hs->m = m;
     hs->k_used = m;
     MEXK_CK(cudaMemcpyAsync(ctx->d_state, hs, sizeof(DevState), cudaMemcpyHostToDevice, s));
-    const size_t ldv = static_cast<size_t>(ctx->ldv);
     const bool fp32 = precision == MEXK_PREC_MIXED;
-    for (int j = 0; j < m; ++j) {
-        GsArgs g;
-        g.n = ctx->n;
-        g.k = j + 1;
-        g.j = j;
-        g.ldv = ctx->ldv;
-        g.ldh = ctx->ldh;
-        g.reortho = reorthogonalize ? 1 : 0;
-        g.V = fp32 ? static_cast<const void*>(ctx->d_V32) : static_cast<const void*>(ctx->d_V);
-        g.w = fp32 ? static_cast<void*>(ctx->d_w32) : static_cast<void*>(ctx->d_w);
-        g.H = ctx->d_H;
-        g.h1 = ctx->d_h1;
-        g.h2 = ctx->d_h2;
-        g.partials = ctx->d_partials;
-        g.counter = ctx->d_counter;
-        g.st = ctx->d_state;
-        g.beta_out = nullptr;
-        const int grid = gs_grid_size(ctx->n, j + 1, fp32);
-        if (fp32) {
-            if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
-                                                ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32,
-                                                &ctx->d_state->breakdown, s)))
-                return rc;
-            if ((rc = launch_gs<float>(GS_DOT, g, grid, s))) return rc;
-            if (g.reortho && (rc = launch_gs<float>(GS_UPD_DOT, g, grid, s))) return rc;
-            if ((rc = launch_gs<float>(GS_UPD_NORM, g, grid, s))) return rc;
-            if ((rc = launch_normalize<float>(ctx->n, j, ctx->ldv, ctx->d_w32, ctx->d_V32, ctx->d_state, nullptr, s)))
-                return rc;
-        } else {
-            if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
-                                                  ctx->d_val, ctx->d_V + j * ldv, ctx->d_w,
-                                                  &ctx->d_state->breakdown, s)))
-                return rc;
-            if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
-            if (g.reortho && (rc = launch_gs<double>(GS_UPD_DOT, g, grid, s))) return rc;
-            if ((rc = launch_gs<double>(GS_UPD_NORM, g, grid, s))) return rc;
-            if ((rc = launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s)))
-                return rc;
-        }
-    }
+    for (int j = 0; j < m; ++j)
+        if ((rc = enqueue_step(ctx, j, reorthogonalize, fp32, s))) return rc;
+    if ((rc = finish_basis(ctx, m - 1, fp32, s))) return rc;
     MEXK_CK(cudaMemcpy2DAsync(H, sizeof(double) * (m + 1), ctx->d_H, sizeof(double) * ctx->ldh,
                               sizeof(double) * (m + 1), m, cudaMemcpyDeviceToHost, s));
     MEXK_CK(cudaMemcpyAsync(hs, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
@@ -750,17 +754,10 @@ int mexk_krylov_advance(mexk_context_t ctx, int precision, int k, const double* 
     MEXK_CK(cudaMemcpyAsync(ctx->d_state, hs, sizeof(DevState), cudaMemcpyHostToDevice, s));
     MEXK_CK(cudaMemcpyAsync(ctx->d_coef, coef, sizeof(double) * k, cudaMemcpyHostToDevice, s));
     const bool fp32 = precision == MEXK_PREC_MIXED;
-    LiftArgs l;
-    l.n = ctx->n;
-    l.ldv = ctx->ldv;
-    l.V = fp32 ? static_cast<const void*>(ctx->d_V32) : static_cast<const void*>(ctx->d_V);
-    l.coef = ctx->d_coef;
-    l.y = ctx->d_y;
-    l.partials = ctx->d_partials;
-    l.counter = ctx->d_counter;
-    l.st = ctx->d_state;
-    int rc = fp32 ? launch_lift<float>(l, gs_grid_size(ctx->n, 1, false), s)
-                  : launch_lift<double>(l, gs_grid_size(ctx->n, 1, false), s);
+    if (fp32 && !ctx->d_V32) return MEXK_ERR_NOT_READY;
+    const LiftArgs l = lift_args(ctx, fp32);
+    int rc = fp32 ? launch_lift<float>(l, gs_grid_size(ctx->n, 1), s)
+                  : launch_lift<double>(l, gs_grid_size(ctx->n, 1), s);
     if (rc) return rc;
     rc = fp32 ? launch_restart<float>(ctx->n, ctx->ldv, ctx->d_y, ctx->d_V32, ctx->d_state, s)
               : launch_restart<double>(ctx->n, ctx->ldv, ctx->d_y, ctx->d_V, ctx->d_state, s);
@@ -825,23 +822,9 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
     MEXK_CK(cudaEventCreate(&e0));
     MEXK_CK(cudaEventCreate(&e1));
     const size_t ldv = static_cast<size_t>(ctx->ldv);
-    GsArgs g;
-    g.n = ctx->n;
-    g.k = j + 1;
-    g.j = j;
-    g.ldv = ctx->ldv;
-    g.ldh = ctx->ldh;
-    g.reortho = 1;
-    g.V = fp32 ? static_cast<const void*>(ctx->d_V32) : static_cast<const void*>(ctx->d_V);
-    g.w = fp32 ? static_cast<void*>(ctx->d_w32) : static_cast<void*>(ctx->d_w);
-    g.H = ctx->d_H;
-    g.h1 = ctx->d_h1;
-    g.h2 = ctx->d_h2;
-    g.partials = ctx->d_partials;
-    g.counter = ctx->d_counter;
-    g.st = ctx->d_state;
-    g.beta_out = nullptr;
-    const int grid = gs_grid_size(ctx->n, j + 1, fp32);
+    const GsArgs g = gs_args(ctx, j, 1, false);
+    const GramArgs ga = fp32 ? gram_args(ctx, j, 1) : GramArgs{};
+    const int grid = gs_grid_size(ctx->n, j + 1);
     double total = 0.0;
     rc = MEXK_OK;
     for (int it = 0; it < iters && rc == MEXK_OK; ++it) {
@@ -866,25 +849,26 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
                 const GsMode mode = kind == MEXK_KERNEL_GS_DOT ? GS_DOT
                                     : kind == MEXK_KERNEL_GS_UPD_DOT ? GS_UPD_DOT
                                                                        : GS_UPD_NORM;
-                rc = fp32 ? launch_gs<float>(mode, g, grid, s) : launch_gs<double>(mode, g, grid, s);
+                rc = fp32 ? MEXK_ERR_UNSUPPORTED : launch_gs<double>(mode, g, grid, s);
                 break;
             }
             case MEXK_KERNEL_NORMALIZE:
-                rc = fp32 ? launch_normalize<float>(ctx->n, j, ctx->ldv, ctx->d_w32, ctx->d_V32, ctx->d_state, nullptr, s)
+                rc = fp32 ? MEXK_ERR_UNSUPPORTED
                           : launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s);
                 break;
+            case MEXK_KERNEL_GRAM_DOT:
+                rc = fp32 ? launch_gram_dot(ga, s) : MEXK_ERR_UNSUPPORTED;
+                break;
+            case MEXK_KERNEL_GRAM_UPDATE:
+                rc = fp32 ? launch_gram_update(ga, s) : MEXK_ERR_UNSUPPORTED;
+                break;
+            case MEXK_KERNEL_GRAM_NORM:
+                rc = fp32 ? launch_gram_norm(ga, s) : MEXK_ERR_UNSUPPORTED;
+                break;
             case MEXK_KERNEL_LIFT: {
-                LiftArgs l;
-                l.n = ctx->n;
-                l.ldv = ctx->ldv;
-                l.V = g.V;
-                l.coef = ctx->d_coef;
-                l.y = ctx->d_y;
-                l.partials = ctx->d_partials;
-                l.counter = ctx->d_counter;
-                l.st = ctx->d_state;
-                rc = fp32 ? launch_lift<float>(l, gs_grid_size(ctx->n, 1, false), s)
-                          : launch_lift<double>(l, gs_grid_size(ctx->n, 1, false), s);
+                const LiftArgs l = lift_args(ctx, fp32);
+                rc = fp32 ? launch_lift<float>(l, gs_grid_size(ctx->n, 1), s)
+                          : launch_lift<double>(l, gs_grid_size(ctx->n, 1), s);
                 break;
             }
             case MEXK_KERNEL_CONTROLLER: {

@@ -113,6 +113,23 @@ template int launch_spmv<double, double>(int, int, const int*, const int*, const
 template int launch_spmv<float, float>(int, int, const int*, const int*, const int*, const float*,
                                        const float*, float*, const int*, cudaStream_t);
 
+// FP32 copy of the FP64 matrix values for the mixed-precision form
+// (round to nearest).
+__global__ void narrow_kernel(const double* __restrict__ src, float* __restrict__ dst, size_t count) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+        dst[i] = __double2float_rn(src[i]);
+}
+
+int launch_narrow_values(const double* src, float* dst, size_t count, cudaStream_t s) {
+    if (count == 0) return MEXK_OK;
+    const size_t want = (count + 255) / 256;
+    const int grid = static_cast<int>(want < 4096 ? want : 4096);
+    narrow_kernel<<<grid, 256, 0, s>>>(src, dst, count);
+    MEXK_CK_LAUNCH("narrow_kernel");
+    return MEXK_OK;
+}
+
 // Free-standing C entry points: build the schedule on the host from a device
 // row_ptr copy. Meant for tests and one-off products; the solver keeps the
 // schedule resident.
