@@ -40,6 +40,8 @@
 
 #include <math.h>
 
+#include <algorithm>
+
 namespace mexk {
 
 namespace {
@@ -351,7 +353,11 @@ int device_sm_count() {
 int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
     if (a.j < 0 || a.j >= MEXK_M_MAX) return MEXK_ERR_INVALID;
     const int ngroups = (a.j + 1 + GG - 1) / GG;
-    gram_dot_kernel<<<row_blocks(a.n, 2) * ngroups, GT, 0, s>>>(a);
+    // One wave of 4 resident blocks per SM over all column groups (a partial
+    // second wave would run at half occupancy); 2 row blocks per SM at most.
+    int nrb = row_blocks(a.n, 2);
+    if (ngroups > 2) nrb = std::min(nrb, std::max(1, 4 * device_sm_count() / ngroups));
+    gram_dot_kernel<<<nrb * ngroups, GT, 0, s>>>(a);
     MEXK_CK_LAUNCH("gram_dot_kernel");
     return MEXK_OK;
 }

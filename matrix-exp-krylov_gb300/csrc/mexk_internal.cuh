@@ -222,9 +222,11 @@ std::vector<int> build_row_blocks(int n, const int* row_ptr);
 
 int launch_narrow_values(const double* src, float* dst, size_t count, cudaStream_t s);
 
+// padded: col_idx and values are 16-byte aligned with at least 3 readable
+// entries past nnz (the context's arrays), enabling 16-byte group loads.
 template <typename TA, typename TX>
 int launch_spmv(int n, int nblocks, const int* blocks, const int* row_ptr, const int* col_idx,
-                const TA* values, const TX* x, TX* y, const int* skip_flag, cudaStream_t s);
+                const TA* values, const TX* x, TX* y, const int* skip_flag, cudaStream_t s, bool padded);
 
 // ------------------------------------------------------------ Gram-Schmidt
 enum GsMode : int { GS_DOT = 0, GS_UPD_DOT = 1, GS_UPD_NORM = 2 };

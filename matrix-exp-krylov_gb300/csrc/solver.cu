@@ -230,14 +230,15 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
     if (fp32) {
         if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
                                             ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32,
-                                            &ctx->d_state->breakdown, s)))
+                                            &ctx->d_state->breakdown, s, true)))
             return rc;
         const GramArgs g = gram_args(ctx, j, reortho);
         if ((rc = launch_gram_dot(g, s))) return rc;
         return launch_gram_update(g, s);
     }
     if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
-                                          ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, &ctx->d_state->breakdown, s)))
+                                          ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, &ctx->d_state->breakdown, s,
+                                          true)))
         return rc;
     const GsArgs g = gs_args(ctx, j, reortho, false);
     const int grid = gs_grid_size(ctx->n, j + 1);
@@ -838,10 +839,11 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
         switch (kind) {
             case MEXK_KERNEL_SPMV:
                 rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
-                                                      ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr, s)
+                                                      ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr, s,
+                                                      true)
                           : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr,
                                                         ctx->d_col, ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, nullptr,
-                                                        s);
+                                                        s, true);
                 break;
             case MEXK_KERNEL_GS_DOT:
             case MEXK_KERNEL_GS_UPD_DOT:

@@ -50,7 +50,39 @@ struct AccType<float> {
     using type = float;
 };
 
-template <typename TA, typename TX>
+// Four consecutive values starting at a 16-byte boundary.
+template <typename TA>
+struct Quad;
+template <>
+struct Quad<float> {
+    static __device__ __forceinline__ void ld(const float* p, float (&o)[4]) {
+        const float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+        o[0] = t.x;
+        o[1] = t.y;
+        o[2] = t.z;
+        o[3] = t.w;
+    }
+};
+template <>
+struct Quad<double> {
+    static __device__ __forceinline__ void ld(const double* p, double (&o)[4]) {
+        const double2 t0 = __ldcs(reinterpret_cast<const double2*>(p));
+        const double2 t1 = __ldcs(reinterpret_cast<const double2*>(p) + 1);
+        o[0] = t0.x;
+        o[1] = t0.y;
+        o[2] = t1.x;
+        o[3] = t1.y;
+    }
+};
+
+// Groups of 4 nonzeros one thread covers in a tile (the tile's span, widened
+// down to a multiple of 4, has at most SPMV_TILE + 3 entries).
+constexpr int SPMV_QUADS = ((SPMV_TILE + 3 + 3) / 4 + SPMV_THREADS - 1) / SPMV_THREADS;
+
+// VEC: values and column indices are 16-byte aligned arrays padded by at
+// least 3 entries past nnz, so whole aligned groups of 4 may be loaded; every
+// thread issues all its column/value loads, then all its x gathers.
+template <typename TA, typename TX, bool VEC>
 __global__ void __launch_bounds__(SPMV_THREADS)
     spmv_rowblock_kernel(int nblocks, const int* __restrict__ blocks, const int* __restrict__ row_ptr,
                          const int* __restrict__ col_idx, const TA* __restrict__ values,
@@ -77,21 +109,65 @@ __global__ void __launch_bounds__(SPMV_THREADS)
             if (tid == 0) y[r0] = static_cast<TX>(s);
             continue;
         }
+        // Row extents for phase 2, fetched alongside phase 1.
+        constexpr int RPT = SPMV_TILE_ROWS / SPMV_THREADS;
+        int ra[RPT], rz[RPT];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            const int r = r0 + tid + q * SPMV_THREADS;
+            ra[q] = r < r1 ? row_ptr[r] : 0;
+            rz[q] = r < r1 ? row_ptr[r + 1] : 0;
+        }
         // Phase 1: coalesced stream of (value, column) pairs.
+        if constexpr (VEC) {
+            const int base = e0 & ~3;
+            const int nq = (e1 - base + 3) >> 2;
+            int4 cq[SPMV_QUADS];
+            TA aq[SPMV_QUADS][4];
+#pragma unroll
+            for (int q = 0; q < SPMV_QUADS; ++q) {
+                const int g = tid + q * SPMV_THREADS;
+                if (g < nq) {
+                    cq[q] = __ldcs(reinterpret_cast<const int4*>(col_idx + base) + g);
+                    Quad<TA>::ld(values + base + 4 * g, aq[q]);
+                }
+            }
+            TP xq[SPMV_QUADS][4];
+#pragma unroll
+            for (int q = 0; q < SPMV_QUADS; ++q) {
+                const int g = tid + q * SPMV_THREADS;
+                const int e = base + 4 * g;
+                const int c4[4] = {cq[q].x, cq[q].y, cq[q].z, cq[q].w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    xq[q][i] = (g < nq && e + i >= e0 && e + i < e1) ? static_cast<TP>(__ldg(&x[c4[i]])) : TP(0);
+            }
+#pragma unroll
+            for (int q = 0; q < SPMV_QUADS; ++q) {
+                const int g = tid + q * SPMV_THREADS;
+                const int e = base + 4 * g;
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (g < nq && e + i >= e0 && e + i < e1) prod[e + i - e0] = static_cast<TP>(aq[q][i]) * xq[q][i];
+            }
+        } else {
 #pragma unroll 4
-        for (int e = tid; e < cnt; e += SPMV_THREADS) {
-            const int c = __ldcs(&col_idx[e0 + e]);
-            const TA a = __ldcs(&values[e0 + e]);
-            prod[e] = static_cast<TP>(a) * static_cast<TP>(__ldg(&x[c]));
+            for (int e = tid; e < cnt; e += SPMV_THREADS) {
+                const int c = __ldcs(&col_idx[e0 + e]);
+                const TA a = __ldcs(&values[e0 + e]);
+                prod[e] = static_cast<TP>(a) * static_cast<TP>(__ldg(&x[c]));
+            }
         }
         __syncthreads();
         // Phase 2: per-row left-to-right sums.
-        for (int r = r0 + tid; r < r1; r += SPMV_THREADS) {
-            const int a = row_ptr[r] - e0;
-            const int z = row_ptr[r + 1] - e0;
-            TP s = 0;
-            for (int p = a; p < z; ++p) s += prod[p];
-            y[r] = static_cast<TX>(s);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            const int r = r0 + tid + q * SPMV_THREADS;
+            if (r < r1) {
+                TP s = 0;
+                for (int p = ra[q] - e0; p < rz[q] - e0; ++p) s += prod[p];
+                y[r] = static_cast<TX>(s);
+            }
         }
         __syncthreads();
     }
@@ -99,19 +175,25 @@ __global__ void __launch_bounds__(SPMV_THREADS)
 
 template <typename TA, typename TX>
 int launch_spmv(int n, int nblocks, const int* blocks, const int* row_ptr, const int* col_idx,
-                const TA* values, const TX* x, TX* y, const int* skip_flag, cudaStream_t s) {
+                const TA* values, const TX* x, TX* y, const int* skip_flag, cudaStream_t s, bool padded) {
     if (n <= 0 || nblocks <= 0) return MEXK_OK;
     const int grid = nblocks < 1048576 ? nblocks : 1048576;
-    spmv_rowblock_kernel<TA, TX><<<grid, SPMV_THREADS, 0, s>>>(nblocks, blocks, row_ptr, col_idx,
-                                                               values, x, y, skip_flag);
+    const bool vec = padded && reinterpret_cast<uintptr_t>(col_idx) % 16 == 0 &&
+                     reinterpret_cast<uintptr_t>(values) % 16 == 0;
+    if (vec)
+        spmv_rowblock_kernel<TA, TX, true><<<grid, SPMV_THREADS, 0, s>>>(nblocks, blocks, row_ptr, col_idx,
+                                                                         values, x, y, skip_flag);
+    else
+        spmv_rowblock_kernel<TA, TX, false><<<grid, SPMV_THREADS, 0, s>>>(nblocks, blocks, row_ptr, col_idx,
+                                                                          values, x, y, skip_flag);
     MEXK_CK_LAUNCH("spmv_rowblock_kernel");
     return MEXK_OK;
 }
 
 template int launch_spmv<double, double>(int, int, const int*, const int*, const int*, const double*,
-                                         const double*, double*, const int*, cudaStream_t);
+                                         const double*, double*, const int*, cudaStream_t, bool);
 template int launch_spmv<float, float>(int, int, const int*, const int*, const int*, const float*,
-                                       const float*, float*, const int*, cudaStream_t);
+                                       const float*, float*, const int*, cudaStream_t, bool);
 
 // FP32 copy of the FP64 matrix values for the mixed-precision form
 // (round to nearest).
@@ -147,7 +229,7 @@ static int spmv_standalone(int rows, const int* row_ptr, const int* col_idx, con
     MEXK_CK(cudaMallocAsync(reinterpret_cast<void**>(&d_blocks), sizeof(int) * blocks.size(), s));
     MEXK_CK(cudaMemcpyAsync(d_blocks, blocks.data(), sizeof(int) * blocks.size(), cudaMemcpyHostToDevice, s));
     int rc = launch_spmv<TA, TX>(rows, static_cast<int>(blocks.size()) - 1, d_blocks, row_ptr, col_idx,
-                                 values, x, y, nullptr, s);
+                                 values, x, y, nullptr, s, false);
     cudaError_t e = cudaFreeAsync(d_blocks, s);
     if (rc == MEXK_OK && e != cudaSuccess) {
         set_cuda_error(e, "cudaFreeAsync", __FILE__, __LINE__);
