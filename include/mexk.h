@@ -224,6 +224,59 @@ int mexk_gram_schmidt_f64_noalloc(int n, int k, const double* V, int ldv, double
                                   int reorthogonalize, double* h, double* beta, double* q,
                                   void* stream);
 
+/* ---- batched solves ---------------------------------------------------- */
+/* Many independent problems -- a CSR matrix, a time t and a block of up to
+ * MEXK_BATCH_RHS right-hand sides each -- solved together in mixed
+ * precision (FP32 matrix values and Krylov bases, FP64 Hessenberg, Gram
+ * matrix, exponentials and results), every (problem, rhs) pair by the
+ * reference method and step controller (ArnoldiRunner::compute_expmv,
+ * main.cu:1411-1571) with its own step size. The reference solves one vector
+ * per process; the batch has no reference counterpart beyond that method.
+ * Problems are laid out in one row space and advanced in waves whose bases
+ * fit the basis budget; one cycle of a wave is one CUDA graph launch. The
+ * tolerance of a right-hand side is raised to the FP32 resolution of its
+ * start vector when smaller: max(tol, 2^-24 |v|). */
+#define MEXK_BATCH_RHS 16
+#define MEXK_BATCH_M_MAX 32
+typedef struct mexk_batch_s* mexk_batch_t;
+typedef struct {
+    int m;                 /* Krylov dimension, 1..MEXK_BATCH_M_MAX, < every problem's rows */
+    double tol;            /* absolute a-posteriori error per accepted step, as ArnoldiParams::tol */
+    int max_restarts;      /* as mexk_params_t.max_restarts */
+    int reorthogonalize;
+    long long basis_bytes; /* device memory for one wave's bases; 0 = 60% of the free memory at upload */
+    int autotune;          /* 1 = choose the tile and sweep schedule by timing candidates on the first wave */
+} mexk_batch_params_t;
+typedef struct {
+    int problems;
+    int waves;
+    int tile_rows;         /* rows per reduction tile */
+    int dot_columns;       /* basis columns per block of the dot sweep */
+    int spmm_unroll;       /* nonzeros fetched ahead per row by the SpMM */
+    int cycles;            /* graph launches over all waves in the last run */
+    long long rows;        /* padded rows of the whole batch */
+    long long nnz;
+    double tune_ms;        /* time spent timing candidate schedules */
+} mexk_batch_info_t;
+
+/* Creates an empty batch for `device`; touches no device until upload. */
+int mexk_batch_create(int device, const mexk_batch_params_t* p, mexk_batch_t* out);
+/* Adds problem *index: CSR (int32, 0-based, rows x rows), time t and nrhs
+ * (1..16) start vectors V, row-major rows x nrhs (V[i*nrhs + r]). The
+ * arrays are read again by mexk_batch_upload and must stay valid until it
+ * returns. Invalid input returns MEXK_ERR_INVALID (CSRHost checks,
+ * main.cu:394-522). */
+int mexk_batch_add(mexk_batch_t b, int rows, const int* row_ptr, const int* col_idx, const double* values,
+                   double t, int nrhs, const double* V, int* index);
+/* Copies every problem to the device, lays out the row space and plans the waves. */
+int mexk_batch_upload(mexk_batch_t b);
+/* Solves every (problem, rhs); may be called again (restarts from the start vectors). */
+int mexk_batch_run(mexk_batch_t b);
+/* Y: rows x nrhs row-major; results: nrhs entries (may be null). */
+int mexk_batch_result(mexk_batch_t b, int problem, double* Y, mexk_result_t* results);
+int mexk_batch_info(mexk_batch_t b, mexk_batch_info_t* info);
+int mexk_batch_destroy(mexk_batch_t b);
+
 /* ---- measurement ------------------------------------------------------ */
 #define MEXK_KERNEL_SPMV 0
 #define MEXK_KERNEL_GS_DOT 1      /* FP64: pass-1 dots */

@@ -296,7 +296,10 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
     extern __shared__ double smem[];
     __shared__ int s_k, s_bd, s_dec;
     __shared__ double s_dt;
-    DevState* st = a.st;
+    // One block per state: block b drives state b (a batch), or the only one.
+    DevState* st = a.st + blockIdx.x;
+    const double* Hb = a.H + blockIdx.x * a.h_stride;
+    double* coef = a.coef + blockIdx.x * a.coef_stride;
     if (st->done) return;
     if (threadIdx.x == 0) {
         const int bd = st->breakdown;
@@ -319,11 +322,11 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
     double* R = nullptr;
     while (true) {
         const double dt = s_dt;
-        for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = dt * a.H[(e % k) + (e / k) * ldh];
+        for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = dt * Hb[(e % k) + (e / k) * ldh];
         __syncthreads();
         R = expm_block(B, k, &st->status);
         if (threadIdx.x == 0) {
-            err = bd ? 0.0 : fabs(a.H[k + (k - 1) * ldh] * R[k - 1]) * st->v_norm;
+            err = bd ? 0.0 : fabs(Hb[k + (k - 1) * ldh] * R[k - 1]) * st->v_norm;
             if (st->nlog < st->log_cap && a.log != nullptr) {
                 mexk_step_t& L = a.log[st->nlog];
                 L.t_done = st->t_done;
@@ -357,7 +360,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
     const double vn = st->v_norm;
     for (int i = threadIdx.x; i <= k; i += blockDim.x) {
         const double wi = (i < k) ? R[i] : 0.0;
-        a.coef[i] = (fabs(wi) > 1e-15) ? vn * wi : 0.0;
+        coef[i] = (fabs(wi) > 1e-15) ? vn * wi : 0.0;
     }
     if (threadIdx.x == 0) {
         double dt = s_dt;
@@ -625,9 +628,9 @@ int launch_expm_standalone(int k, const double* A, int lda, double* E, int lde, 
     return MEXK_OK;
 }
 
-int launch_controller(const ControlArgs& a, int m, cudaStream_t s) {
+int launch_controller(const ControlArgs& a, int m, cudaStream_t s, int nstates) {
     const size_t smem = expm_smem_bytes(m);
-    controller_kernel<<<1, EXPM_THREADS, smem, s>>>(a, m);
+    controller_kernel<<<nstates, EXPM_THREADS, smem, s>>>(a, m);
     MEXK_CK_LAUNCH("controller_kernel");
     return MEXK_OK;
 }

@@ -301,8 +301,11 @@ struct ControlArgs {
     int ldh;
     double* coef;       // lift coefficients (k+1)
     mexk_step_t* log;   // attempt log (log_cap entries)
+    size_t h_stride = 0;     // batch: state b uses st + b, H + b*h_stride,
+    size_t coef_stride = 0;  //        coef + b*coef_stride (no log)
 };
-int launch_controller(const ControlArgs& a, int m, cudaStream_t s);
+// One thread block per state (nstates > 1: a batch of independent solves).
+int launch_controller(const ControlArgs& a, int m, cudaStream_t s, int nstates = 1);
 
 // Candidate-step controller: one thread block per candidate step.
 constexpr int SEARCH_CAND = 32;

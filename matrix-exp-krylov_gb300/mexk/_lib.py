@@ -49,6 +49,23 @@ class Step(C.Structure):
                 ("accepts", C.c_int), ("rejects", C.c_int)]
 
 
+class BatchParams(C.Structure):
+    _fields_ = [("m", C.c_int), ("tol", C.c_double), ("max_restarts", C.c_int), ("reorthogonalize", C.c_int),
+                ("basis_bytes", C.c_longlong), ("autotune", C.c_int)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("problems", C.c_int), ("waves", C.c_int), ("tile_rows", C.c_int), ("dot_columns", C.c_int),
+                ("spmm_unroll", C.c_int), ("cycles", C.c_int), ("rows", C.c_longlong), ("nnz", C.c_longlong),
+                ("tune_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+BATCH_RHS = 16
+BATCH_M_MAX = 32
+
 _VP = C.c_void_p
 _IP = C.POINTER(C.c_int)
 _DP = C.POINTER(C.c_double)
@@ -57,6 +74,14 @@ _PROTOS = {
     "mexk_error_string": ([C.c_int], C.c_char_p),
     "mexk_last_error_detail": ([], C.c_char_p),
     "mexk_version": ([], C.c_char_p),
+    "mexk_batch_create": ([C.c_int, C.POINTER(BatchParams), C.POINTER(C.c_void_p)], C.c_int),
+    "mexk_batch_add": ([C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                        C.c_double, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)], C.c_int),
+    "mexk_batch_upload": ([C.c_void_p], C.c_int),
+    "mexk_batch_run": ([C.c_void_p], C.c_int),
+    "mexk_batch_result": ([C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(Result)], C.c_int),
+    "mexk_batch_info": ([C.c_void_p, C.POINTER(BatchInfo)], C.c_int),
+    "mexk_batch_destroy": ([C.c_void_p], C.c_int),
     "mexk_device_count": ([_IP], C.c_int),
     "mexk_context_create": ([C.c_int, C.POINTER(_VP)], C.c_int),
     "mexk_context_upload_csr": ([_VP, C.c_int, C.c_longlong, _IP, _IP, _DP, C.c_int], C.c_int),
