@@ -275,6 +275,12 @@ int mexk_batch_run(mexk_batch_t b);
 /* Y: rows x nrhs row-major; results: nrhs entries (may be null). */
 int mexk_batch_result(mexk_batch_t b, int problem, double* Y, mexk_result_t* results);
 int mexk_batch_info(mexk_batch_t b, mexk_batch_info_t* info);
+/* Times `iters` launches of one per-step kernel of the first wave at step j
+ * with the schedule in use (after a run): kind 0 SpMM, 1 dot sweep (timing
+ * only, states untouched), 2 update sweep. *ms_per_launch and the wave's
+ * rows / nonzeros (for byte counts) are returned. */
+int mexk_batch_profile(mexk_batch_t b, int kind, int j, int iters, double* ms_per_launch, long long* wave_rows,
+                       long long* wave_nnz);
 int mexk_batch_destroy(mexk_batch_t b);
 
 /* ---- measurement ------------------------------------------------------ */

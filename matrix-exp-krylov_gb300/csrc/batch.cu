@@ -599,6 +599,34 @@ int mexk_batch_info(mexk_batch_t b, mexk_batch_info_t* info) {
     return MEXK_OK;
 }
 
+int mexk_batch_profile(mexk_batch_t b, int kind, int j, int iters, double* ms_per_launch, long long* wave_rows,
+                       long long* wave_nnz) {
+    if (!b || !b->uploaded || !ms_per_launch || iters < 1 || j < 0 || j >= b->prm.m || kind < 0 || kind > 2)
+        return MEXK_ERR_INVALID;
+    if (!b->have_final) return MEXK_ERR_NOT_READY;
+    MEXK_CK(cudaSetDevice(b->device));
+    const Wave& w = b->waves[0];
+    const Layout L = layout(b, w);
+    // Finished problems skip every kernel: time the wave as if all were running.
+    std::vector<int> saved(w.p1 - w.p0);
+    MEXK_CK(cudaMemcpy(saved.data(), b->d_pdone + w.p0, sizeof(int) * saved.size(), cudaMemcpyDeviceToHost));
+    MEXK_CK(cudaMemset(b->d_pdone + w.p0, 0, sizeof(int) * saved.size()));
+    int rc;
+    if (kind == 0) rc = time_ms(b, [&] { return launch_spmm(L, j, b->unroll, b->stream); }, iters, ms_per_launch);
+    else if (kind == 1)
+        rc = time_ms(b, [&] { return launch_dot(L, j, 1, b->gg, 1, b->stream); }, iters, ms_per_launch);
+    else rc = time_ms(b, [&] { return launch_update(L, j, b->stream); }, iters, ms_per_launch);
+    MEXK_CK(cudaMemcpy(b->d_pdone + w.p0, saved.data(), sizeof(int) * saved.size(), cudaMemcpyHostToDevice));
+    if (rc) return rc;
+    if (wave_rows) *wave_rows = w.R1 - w.R0;
+    if (wave_nnz) {
+        long long nz = 0;
+        for (int p = w.p0; p < w.p1; ++p) nz += b->probs[p].nnz;
+        *wave_nnz = nz;
+    }
+    return MEXK_OK;
+}
+
 int mexk_batch_destroy(mexk_batch_t b) {
     if (!b) return MEXK_OK;
     if (b->uploaded || b->stream) {

@@ -82,6 +82,8 @@ _PROTOS = {
     "mexk_batch_result": ([C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(Result)], C.c_int),
     "mexk_batch_info": ([C.c_void_p, C.POINTER(BatchInfo)], C.c_int),
     "mexk_batch_destroy": ([C.c_void_p], C.c_int),
+    "mexk_batch_profile": ([C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                            C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], C.c_int),
     "mexk_device_count": ([_IP], C.c_int),
     "mexk_context_create": ([C.c_int, C.POINTER(_VP)], C.c_int),
     "mexk_context_upload_csr": ([_VP, C.c_int, C.c_longlong, _IP, _IP, _DP, C.c_int], C.c_int),

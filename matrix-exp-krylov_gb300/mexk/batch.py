@@ -68,6 +68,16 @@ class Batch:
         check(lib().mexk_batch_info(self._h, C.byref(i)), "mexk_batch_info")
         return i.as_dict()
 
+    KINDS = {"spmm": 0, "dot": 1, "update": 2}
+
+    def profile(self, kind: str, j: int, iters: int = 3):
+        """(ms per launch, wave rows, wave nonzeros) of one per-step kernel
+        of the first wave at step j (after a run)."""
+        ms, rows, nnz = C.c_double(), C.c_longlong(), C.c_longlong()
+        check(lib().mexk_batch_profile(self._h, self.KINDS[kind], j, iters, C.byref(ms), C.byref(rows),
+                                       C.byref(nnz)), "mexk_batch_profile")
+        return ms.value, rows.value, nnz.value
+
     def close(self):
         if self._h:
             lib().mexk_batch_destroy(self._h)

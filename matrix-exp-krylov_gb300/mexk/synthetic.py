@@ -226,6 +226,59 @@ def config3_problem(index: int, n_range=(1e4, 2e6), nrhs: int = 16) -> Problem:
     return Problem(A, V, t, 30, meta={"config": 3, "seed": seed, "degree": deg})
 
 
+def config3_sizes(index: int):
+    """(n, degree, t) of problem ``index`` of the batched workload, drawn
+    from numpy's generator seeded 100 + index: n log-uniform in [1e4, 2e6],
+    degree uniform in {5..20}, t uniform in [0.1, 2]."""
+    rng = np.random.default_rng(100 + index)
+    n = int(round(10 ** rng.uniform(4.0, math.log10(2e6))))
+    deg = int(rng.integers(5, 21))
+    t = float(rng.uniform(0.1, 2.0))
+    return n, deg, t
+
+
+def config3_generated(index: int, nrhs: int = 16, device: str = "cuda") -> Problem:
+    """Problem ``index`` of the batched workload generated on the GPU (torch's
+    seeded Philox generator, seed 100 + index): config 0's structure -- each
+    row has ``degree`` distinct off-diagonal columns uniform over the other
+    columns, values U[-0.5, 0.5], diagonal -(row |off| sum) - 1 -- with the
+    sizes of config3_sizes and nrhs N(0,1) start vectors. Much faster than
+    the numpy generator at the workload's 1.5e9 nonzeros; not bit-identical
+    to it."""
+    import torch
+
+    n, deg, t = config3_sizes(index)
+    g = torch.Generator(device=device)
+    g.manual_seed(100 + index)
+    rows = torch.arange(n, device=device, dtype=torch.int64).unsqueeze(1)
+
+    def draw(r):
+        c = torch.randint(0, n - 1, (r.shape[0], deg), generator=g, device=device, dtype=torch.int64)
+        return c + (c >= r).to(torch.int64)  # skip the diagonal
+
+    cols, _ = torch.sort(draw(rows), dim=1)
+    for _ in range(64):
+        dup = (cols[:, 1:] == cols[:, :-1]).any(dim=1)
+        idx = dup.nonzero().squeeze(1)
+        if idx.numel() == 0:
+            break
+        fresh, _ = torch.sort(draw(rows[idx]), dim=1)
+        cols[idx] = fresh
+    else:
+        raise RuntimeError("duplicate columns left after 64 redraws")
+    vals = torch.rand((n, deg), generator=g, device=device, dtype=torch.float64) - 0.5
+    diag = -vals.abs().sum(dim=1, keepdim=True) - 1.0
+    allc = torch.cat([cols, rows], dim=1)
+    allv = torch.cat([vals, diag], dim=1)
+    order = torch.argsort(allc, dim=1)
+    allc = torch.gather(allc, 1, order).to(torch.int32).reshape(-1).cpu().numpy()
+    allv = torch.gather(allv, 1, order).reshape(-1).cpu().numpy()
+    V = torch.randn((nrhs, n), generator=g, device=device, dtype=torch.float64).cpu().numpy()
+    row_ptr = np.arange(0, (n + 1) * (deg + 1), deg + 1, dtype=np.int32)
+    A = CSR(n, row_ptr, allc, allv, f"config3_{index}")
+    return Problem(A, V, t, 30, meta={"config": 3, "seed": 100 + index, "degree": deg, "generator": "torch"})
+
+
 def config4(N: int = 128, pe: float = 10.0, seed: int = 4) -> Problem:
     """3D convection-diffusion, upwinded velocity (1,0.5,0.25)*pe, h = 1/(N+1); v ~ U[0,1]; t = 1."""
     A = convection_diffusion_3d(N, pe)
