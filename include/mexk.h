@@ -252,7 +252,7 @@ typedef struct {
     int waves;
     int tile_rows;         /* rows per reduction tile */
     int dot_columns;       /* basis columns per block of the dot sweep */
-    int spmm_unroll;       /* nonzeros fetched ahead per row by the SpMM */
+    int spmm_unroll;       /* x gathers the SpMM issues together per row */
     int cycles;            /* graph launches over all waves in the last run */
     long long rows;        /* padded rows of the whole batch */
     long long nnz;

@@ -288,10 +288,10 @@ int autotune(mexk_batch_t b) {
     if ((rc = build_tiles(b, best_tr))) return rc;
     b->gg = best_gg;
     const Layout L = layout(b, b->waves[0]);
-    double ms1 = 0.0, ms4 = 0.0;
-    if ((rc = time_ms(b, [&] { return launch_spmm(L, 0, 1, b->stream); }, 3, &ms1))) return rc;
+    double ms4 = 0.0, ms8 = 0.0;
     if ((rc = time_ms(b, [&] { return launch_spmm(L, 0, 4, b->stream); }, 3, &ms4))) return rc;
-    b->unroll = ms4 <= ms1 ? 4 : 1;
+    if ((rc = time_ms(b, [&] { return launch_spmm(L, 0, 8, b->stream); }, 3, &ms8))) return rc;
+    b->unroll = ms8 < ms4 ? 8 : 4;
     MEXK_CK(cudaStreamSynchronize(b->stream));
     b->tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     b->tuned = true;

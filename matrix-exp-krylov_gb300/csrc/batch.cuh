@@ -68,7 +68,7 @@ struct Layout {
 };
 
 // Per-step kernels; gg = columns per block of the dot sweep (2 or 4),
-// unroll = nonzeros fetched ahead per row by the SpMM (1 or 4).
+// unroll = x gathers issued together per row by the SpMM (4 or 8).
 int launch_spmm(const Layout& L, int j, int unroll, cudaStream_t s);
 int launch_dot(const Layout& L, int j, int reortho, int gg, int tune, cudaStream_t s);
 int launch_update(const Layout& L, int j, cudaStream_t s);

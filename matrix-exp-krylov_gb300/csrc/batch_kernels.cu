@@ -80,8 +80,16 @@ __device__ __forceinline__ double tiles_sum(const Layout& L, int p, int slot) {
 }
 
 // ---------------------------------------------------------------- SpMM
+// One 64-row chunk per block iteration: the chunk's nonzeros (contiguous in
+// CSR) are staged in shared memory with coalesced loads, then each row
+// quarter issues its row's x gathers U at a time from the staged columns.
+// Chunks with more than SP_STAGE nonzeros read their columns directly.
+constexpr int SP_STAGE = 2048;
+
 template <int U>
 __global__ void __launch_bounds__(BT) spmm_kernel(Layout L, int j) {
+    __shared__ int s_col[SP_STAGE];
+    __shared__ float s_val[SP_STAGE];
     const int q = threadIdx.x & 3;
     const int rl = threadIdx.x >> 2;
     const float4* __restrict__ X4 = col4(L, j);
@@ -89,31 +97,58 @@ __global__ void __launch_bounds__(BT) spmm_kernel(Layout L, int j) {
     for (int ch = L.C0 + blockIdx.x; ch < L.C1; ch += gridDim.x) {
         const int p = L.chunk_prob[ch];
         if (L.pdone[p]) continue;
-        const long long row = static_cast<long long>(ch) * BROWS + rl;
-        const long long xoff = L.prow0[p] - L.R0;
+        const long long r0 = static_cast<long long>(ch) * BROWS;
+        const long long row = r0 + rl;
+        const long long c0 = L.row_ptr[r0];
+        const long long c1 = L.row_ptr[r0 + BROWS];
+        const long long e0 = L.row_ptr[row];
         const long long e1 = L.row_ptr[row + 1];
-        long long e = L.row_ptr[row];
+        const long long xoff = L.prow0[p] - L.R0;
         float4 acc = zero4();
-        if (U > 1) {
-            for (; e + U <= e1; e += U) {
-                int c[U];
-                float a[U];
+        if (c1 - c0 <= SP_STAGE) {
+            const int cnt = static_cast<int>(c1 - c0);
+            __syncthreads();
+            for (int e = threadIdx.x; e < cnt; e += BT) {
+                s_col[e] = __ldcs(&L.col[c0 + e]);
+                s_val[e] = __ldcs(&L.val[c0 + e]);
+            }
+            __syncthreads();
+            int e = static_cast<int>(e0 - c0);
+            const int z = static_cast<int>(e1 - c0);
+            for (; e + U <= z; e += U) {
+                float4 xv[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) xv[u] = __ldg(X4 + (xoff + s_col[e + u]) * 4 + q);
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
+                    const float a = s_val[e + u];
+                    fma4(acc, make_float4(a, a, a, a), xv[u]);
+                }
+            }
+            for (; e < z; ++e) {
+                const float a = s_val[e];
+                fma4(acc, make_float4(a, a, a, a), __ldg(X4 + (xoff + s_col[e]) * 4 + q));
+            }
+        } else {
+            long long e = e0;
+            for (; e + 4 <= e1; e += 4) {
+                int c[4];
+                float a[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
                     c[u] = __ldg(&L.col[e + u]);
                     a[u] = __ldg(&L.val[e + u]);
                 }
-                float4 xv[U];
+                float4 xv[4];
 #pragma unroll
-                for (int u = 0; u < U; ++u) xv[u] = __ldg(X4 + (xoff + c[u]) * 4 + q);
+                for (int u = 0; u < 4; ++u) xv[u] = __ldg(X4 + (xoff + c[u]) * 4 + q);
 #pragma unroll
-                for (int u = 0; u < U; ++u) fma4(acc, make_float4(a[u], a[u], a[u], a[u]), xv[u]);
+                for (int u = 0; u < 4; ++u) fma4(acc, make_float4(a[u], a[u], a[u], a[u]), xv[u]);
             }
-        }
-        for (; e < e1; ++e) {
-            const float a = __ldg(&L.val[e]);
-            const float4 xv = __ldg(X4 + (xoff + __ldg(&L.col[e])) * 4 + q);
-            fma4(acc, make_float4(a, a, a, a), xv);
+            for (; e < e1; ++e) {
+                const float a = __ldg(&L.val[e]);
+                fma4(acc, make_float4(a, a, a, a), __ldg(X4 + (xoff + __ldg(&L.col[e])) * 4 + q));
+            }
         }
         Y4[(row - L.R0) * 4 + q] = acc;
     }
@@ -541,8 +576,8 @@ int launch_spmm(const Layout& L, int j, int unroll, cudaStream_t s) {
     const int chunks = L.C1 - L.C0;
     if (chunks <= 0) return MEXK_OK;
     const int grid = chunks < sm_blocks(8) ? chunks : sm_blocks(8);
-    if (unroll >= 4) spmm_kernel<4><<<grid, BT, 0, s>>>(L, j);
-    else spmm_kernel<1><<<grid, BT, 0, s>>>(L, j);
+    if (unroll >= 8) spmm_kernel<8><<<grid, BT, 0, s>>>(L, j);
+    else spmm_kernel<4><<<grid, BT, 0, s>>>(L, j);
     MEXK_CK_LAUNCH("batch spmm_kernel");
     return MEXK_OK;
 }
