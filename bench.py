@@ -514,15 +514,35 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
-def run_solve_once(local_rank):
-    """One mixed-precision (candidate-step controller) and one plain FP64
-    solve of the workload, untimed: the command ncu captures."""
+def run_batch_once(args):
+    """One untimed batch run over problems [first, first + problems) of the
+    batched workload (autotuning off): the command ncu captures."""
     import torch
 
+    from mexk import synthetic as S
+    from mexk.batch import Batch
+
+    torch.cuda.set_device(0)
+    probs = [S.config3_generated(i) for i in range(args.first, args.first + args.problems)]
+    with Batch(m=30, tol=1e-6, autotune=False) as b:
+        for P in probs:
+            b.add(P.A, P.v, P.t)
+        b.upload()
+        b.run()
+        print(json.dumps(b.info()), flush=True)
+
+
+def run_solve_once(local_rank, grid=2048):
+    """One mixed-precision (candidate-step controller) and one plain FP64
+    solve of the workload (heat equation on a grid x grid mesh), untimed: the
+    command ncu captures."""
+    import torch
+
+    from mexk import synthetic as S
     from mexk.api import Context
 
     torch.cuda.set_device(local_rank)
-    P = make_problem()
+    P = make_problem() if grid == 2048 else S.config1(N=grid)
     with Context(P.A, m_alloc=P.m, device=local_rank) as ctx:
         for prec, ctrl in (("mixed", "search"), ("fp64", "reference")):
             _, res = ctx.expmv(P.v, P.t, P.m, precision=prec, controller=ctrl)
@@ -542,12 +562,17 @@ def main():
     ap.add_argument("--workload", default="heat2048", choices=["heat2048", "batch"])
     ap.add_argument("--problems", type=int, default=256, help="batch workload: number of problems")
     ap.add_argument("--sample", type=int, default=8, help="batch workload: problems in the serial FP64 sample")
+    ap.add_argument("--grid", type=int, default=2048, help="--solve-once: heat-equation grid size")
+    ap.add_argument("--first", type=int, default=0, help="batch --solve-once: index of the first problem")
     args = ap.parse_args()
-    if args.workload == "batch" and args.impl == "ours":
-        run_batch(args)
+    if args.solve_once and args.workload == "batch":
+        run_batch_once(args)
         return
     if args.solve_once:
-        run_solve_once(int(os.environ.get("LOCAL_RANK", "0")))
+        run_solve_once(int(os.environ.get("LOCAL_RANK", "0")), args.grid)
+        return
+    if args.workload == "batch" and args.impl == "ours":
+        run_batch(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
