@@ -65,14 +65,31 @@ def features(H, k, rem, tol, vnorm, tau_prev, err_prev):
 
 
 # ------------------------------------------------------------------ cost model
-def cycle_cost(m, n, nnz, precision="mixed", fixed_s=2.5e-4, gbs=5.0e12):
-    """Seconds per Krylov cycle from algorithmic bytes at `gbs` plus a fixed
-    per-cycle cost (controller, launches, host sync)."""
+# Cycles are priced at the workloads' scale: the sweep problems are small,
+# but the trained policy runs on matrices of millions of rows, where bytes
+# dominate the fixed per-launch costs. The network sees no problem size, so
+# the labels must come from one consistent price.
+TARGET_ROWS = 4_194_304
+
+
+def cycle_cost(m, n, nnz, precision="mixed", target_rows=TARGET_ROWS, step_fixed_s=2.0e-5,
+               cycle_fixed_s=2.5e-4, gbs=5.5e12):
+    """Seconds per Krylov cycle of dimension m for a matrix with this
+    nonzeros-per-row ratio at `target_rows` rows (None: its own n):
+    algorithmic bytes at `gbs`, plus a fixed cost per Arnoldi step (launches,
+    the dot sweep's grid reduction) and per cycle (controller, lift, sync).
+    Mixed: SpMV, a (k+1)-vector dot sweep and a (k+2)-vector update per step,
+    one norm per cycle; FP64: SpMV, three CGS2 sweeps and a normalisation."""
     s = 4 if precision == "mixed" else 8
-    spmv = m * (nnz * (s + 4) + 4 * (n + 1) + 2 * n * s)
-    gs = s * n * sum(3 * j + 5 for j in range(1, m + 1)) + 2 * s * n * m
-    lift = (m * s + 8) * n
-    return (spmv + gs + lift) / gbs + fixed_s
+    rows = target_rows if target_rows else n
+    nz = nnz / max(n, 1) * rows
+    spmv = m * (nz * (s + 4) + 4 * (rows + 1) + 2 * rows * s)
+    if precision == "mixed":
+        gs = s * rows * (sum(2 * k + 3 for k in range(1, m + 1)) + 1)
+    else:
+        gs = s * rows * sum(3 * k + 7 for k in range(1, m + 1))
+    lift = (m * s + 8) * rows
+    return (spmv + gs + lift) / gbs + m * step_fixed_s + cycle_fixed_s
 
 
 # ------------------------------------------------------------------ step search
@@ -209,17 +226,22 @@ def training_problems(scale="small"):
     from . import synthetic as S
 
     probs = []
-    grids = (20, 28, 40) if scale == "small" else (48, 64)
+    wide = scale == "wide"
+    grids = (20, 28, 40, 52) if wide else ((20, 28, 40) if scale == "small" else (48, 64))
     for N in grids:
         for pe, t in CONVDIFF_T.items():
             A = S.convection_diffusion_3d(N, pe, h=1.0 / 129)
             v = np.random.default_rng(int(pe) + N).uniform(0, 1, A.n)
             probs.append((f"convdiff{N}_pe{pe:g}", A, v, t))
-    for N in (64, 128, 192, 256):
+            if wide:  # the same operator over a twice longer horizon
+                probs.append((f"convdiff{N}_pe{pe:g}_2t", A, v, 2 * t))
+    for N in ((64, 128, 192, 256, 320, 384) if wide else (64, 128, 192, 256)):
         A = S.laplacian_2d(N, h=1.0 / 2049)
         v = np.random.default_rng(N).uniform(0, 1, A.n)
         probs.append((f"heat{N}", A, v, 1e-5))
-    for seed in range(3):
+        if wide:
+            probs.append((f"heat{N}_3t", A, v, 3e-5))
+    for seed in range(6 if wide else 3):
         A = skew_problem(20000, 6, seed=50 + seed)
         v = np.random.default_rng(60 + seed).standard_normal(A.n)
         probs.append((f"skew20k_{seed}", A, v, 15.0))
@@ -308,8 +330,9 @@ def evaluate_loss(w, Xd, Td):
 
 
 def save(weights, meta, path=WEIGHTS):
+    """Weights as raw little-endian float32 at `path`, description beside it (.json)."""
     np.asarray(weights, dtype="<f4").tofile(path)
-    with open(META, "w") as f:
+    with open(os.path.splitext(path)[0] + ".json", "w") as f:
         json.dump(meta, f, indent=1)
 
 
@@ -330,10 +353,12 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=400)
     ap.add_argument("--states", type=int, default=40)
     ap.add_argument("--data-out", default=None, help="also save the raw sweep data (.npz)")
+    ap.add_argument("--scale", default="small", choices=["small", "wide", "large"], help="training problem set")
+    ap.add_argument("--out", default=None, help="directory for controller_net.f32 / .json (default: the package)")
     args = ap.parse_args(argv)
     t0 = time.time()
     Xs, Ts, ntuples, names = [], [], 0, []
-    for name, A, v, t in training_problems():
+    for name, A, v, t in training_problems(args.scale):
         with Context(A, m_alloc=max(M_SET)) as ctx:
             X, T, tup = sweep_problem(ctx, A, v, t, max_states=args.states)
         Xs.append(X)
@@ -349,8 +374,10 @@ def main(argv=None):
     meta = {"inputs": NET_IN, "hidden": NET_HID, "outputs": NET_OUT, "samples": int(len(X)),
             "tuples": int(ntuples), "problems": names, "epochs": args.epochs, "final_loss": losses[-1],
             "initial_loss": losses[0], "m_set": list(M_SET), "precision": "mixed",
-            "seconds": round(time.time() - t0, 1)}
-    save(w, meta)
+            "cost_model": {"target_rows": TARGET_ROWS, "step_fixed_s": 2.0e-5, "cycle_fixed_s": 2.5e-4,
+                           "gbs": 5.5e12},
+            "scale": args.scale, "seconds": round(time.time() - t0, 1)}
+    save(w, meta, os.path.join(args.out, "controller_net.f32") if args.out else WEIGHTS)
     print(json.dumps(meta))
 
 
