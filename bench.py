@@ -514,6 +514,73 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ learned-controller workload
+CONV_METRIC = ("exp(tA)v solves/s and SpMVs of the learned controller vs the plain restart heuristic "
+               "(128^3 convection-diffusion, Pe 1-1000)")
+
+
+def run_convdiff(args):
+    """Config-4 workload: for each Peclet number, the same solve under the plain
+    heuristic (FP64 and mixed), the candidate-step search and the learned
+    controller (mixed); SpMVs, cycles, CUDA-event time and error vs FP64."""
+    import torch
+
+    from mexk import synthetic as S
+    from mexk.api import Context
+    from mexk.controller import CONVDIFF_T
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    forms = (("fp64", "reference"), ("mixed", "reference"), ("mixed", "search"), ("mixed", "learned"))
+    per_pe, tot = [], {f"{p}+{c}": {"ms": 0.0, "spmv": 0, "cycles": 0} for p, c in forms}
+    for pe, t in CONVDIFF_T.items():
+        P = S.config4(128, pe)
+        entry = {"pe": pe, "t": t, "n": P.A.n, "nnz": P.A.nnz}
+        with Context(P.A, m_alloc=60) as ctx:
+            v_d = torch.from_numpy(P.v).cuda()
+            y64 = torch.zeros_like(v_d)
+            y = torch.zeros_like(v_d)
+            for prec, ctrl in forms:
+                out = y64 if (prec, ctrl) == forms[0] else y
+                res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), t, 30, precision=prec, controller=ctrl)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(args.steps):
+                    res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), t, 30, precision=prec, controller=ctrl)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / args.steps
+                err = float(torch.linalg.norm(out - y64) / torch.linalg.norm(y64)) if out is y else 0.0
+                key = f"{prec}+{ctrl}"
+                entry[key] = {"ms": round(ms, 2), "spmv": res["spmv_count"], "cycles": res["cycles"],
+                              "attempts": res["attempts"], "converged": res["converged"], "rel_err_vs_fp64": err}
+                tot[key]["ms"] += ms
+                tot[key]["spmv"] += res["spmv_count"]
+                tot[key]["cycles"] += res["cycles"]
+        per_pe.append(entry)
+    nprob = len(per_pe)
+    learned, plain = tot["mixed+learned"], tot["mixed+reference"]
+    line = {
+        "metric": CONV_METRIC, "value": nprob / (learned["ms"] / 1e3), "unit": "solves/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": 1, "ms_per_step": learned["ms"] / nprob, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": ("convdiff128: 3D 7-point convection-diffusion, 128^3 grid, h = 1/129, upwinded "
+                                "velocity (1,0.5,0.25)*Pe, Pe in {1,10,100,1000}; v ~ U[0,1] seed 4; "
+                                "t per Pe = " + json.dumps(CONVDIFF_T) + "; m = 30 (learned: chosen per cycle), "
+                                "tol 1e-6")},
+        "learned_vs_plain_heuristic": {"solves_per_s": nprob / (learned["ms"] / 1e3),
+                                       "plain_solves_per_s": nprob / (plain["ms"] / 1e3),
+                                       "speedup": plain["ms"] / learned["ms"],
+                                       "spmv": learned["spmv"], "plain_spmv": plain["spmv"],
+                                       "spmv_ratio": plain["spmv"] / max(learned["spmv"], 1)},
+        "totals": {k: {"ms": round(v["ms"], 2), "spmv": v["spmv"], "cycles": v["cycles"]} for k, v in tot.items()},
+        "per_pe": per_pe,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_batch_once(args):
     """One untimed batch run over problems [first, first + problems) of the
     batched workload (autotuning off): the command ncu captures."""
@@ -559,7 +626,7 @@ def main():
     ap.add_argument("--controller", default="search", choices=["reference", "search", "learned"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--solve-once", action="store_true", help="one untimed FP64 + mixed solve (for ncu)")
-    ap.add_argument("--workload", default="heat2048", choices=["heat2048", "batch"])
+    ap.add_argument("--workload", default="heat2048", choices=["heat2048", "batch", "convdiff"])
     ap.add_argument("--problems", type=int, default=256, help="batch workload: number of problems")
     ap.add_argument("--sample", type=int, default=8, help="batch workload: problems in the serial FP64 sample")
     ap.add_argument("--grid", type=int, default=2048, help="--solve-once: heat-equation grid size")
@@ -573,6 +640,9 @@ def main():
         return
     if args.workload == "batch" and args.impl == "ours":
         run_batch(args)
+        return
+    if args.workload == "convdiff" and args.impl == "ours":
+        run_convdiff(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
