@@ -581,6 +581,73 @@ def run_convdiff(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ power-law workload
+PL_METRIC = "exp(tA)v solves/s at <=1e-6 rel err, mixed precision vs plain FP64 (irregular power-law rows)"
+
+
+def run_powerlaw(args):
+    """Config-2 workload: power-law rows (Zipf 1.8, 2..2048 off-diagonals),
+    n = 8,388,608, t = 0.5, m = 40; each form timed after one untimed solve,
+    error vs FP64, SpMV rates from CUDA events."""
+    import torch
+
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    P = S.config2()
+    t_gen = time.perf_counter() - t0
+    n, nnz = P.A.n, P.A.nnz
+    forms = (("fp64", "reference"), ("mixed", "reference"), ("mixed", "search"), ("mixed", "learned"))
+    out = {}
+    with Context(P.A, m_alloc=P.m) as ctx:
+        v_d = torch.from_numpy(P.v).cuda()
+        y64 = torch.zeros_like(v_d)
+        y = torch.zeros_like(v_d)
+        for prec, ctrl in forms:
+            dst = y64 if (prec, ctrl) == forms[0] else y
+            res = ctx.expmv_device(v_d.data_ptr(), dst.data_ptr(), P.t, P.m, precision=prec, controller=ctrl)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                res = ctx.expmv_device(v_d.data_ptr(), dst.data_ptr(), P.t, P.m, precision=prec, controller=ctrl)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            err = float(torch.linalg.norm(dst - y64) / torch.linalg.norm(y64)) if dst is y else 0.0
+            out[f"{prec}+{ctrl}"] = {"ms": round(ms, 2), "solves_per_s": 1e3 / ms, "rel_err_vs_fp64": err,
+                                     "cycles": res["cycles"], "attempts": res["attempts"],
+                                     "spmv": res["spmv_count"], "converged": res["converged"]}
+        spmv = {}
+        for prec in ("mixed", "fp64"):
+            ms = min(ctx.profile_kernel("spmv", j, 5, prec) for j in (0, 10, 20))
+            b = kernel_bytes("spmv", n, nnz, 1, prec == "mixed")
+            spmv[prec] = {"us": round(ms * 1e3, 1), "gbs": round(b / (ms / 1e3) / 1e9, 1)}
+    ok = {k: v for k, v in out.items() if k != "fp64+reference" and v["rel_err_vs_fp64"] <= 1e-6}
+    best = min(ok, key=lambda k: out[k]["ms"]) if ok else "fp64+reference"
+    peak, _ = measured_peaks()
+    row_len = np.diff(P.A.row_ptr)
+    line = {
+        "metric": PL_METRIC, "value": out[best]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": 1, "ms_per_step": out[best]["ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": ("powerlaw: n = 8,388,608, seed 2, row off-diagonal counts ~ Zipf(1.8) clipped to "
+                                "[2, 2048], uniform distinct columns, values U[-1,1], diagonal -(row |off| sum)-0.5; "
+                                "v ~ N(0,1); t = 0.5, m = 40, tol 1e-6"),
+                   "nnz": nnz, "row_len_mean": float(row_len.mean()), "row_len_max": int(row_len.max()),
+                   "chosen": best, "generate_s": round(t_gen, 1)},
+        "fp64_solves_per_s": out["fp64+reference"]["solves_per_s"],
+        "speedup_vs_fp64": out[best]["solves_per_s"] / out["fp64+reference"]["solves_per_s"],
+        "forms": out,
+        "spmv": {k: dict(v, frac=round(v["gbs"] / peak, 3)) for k, v in spmv.items()},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_batch_once(args):
     """One untimed batch run over problems [first, first + problems) of the
     batched workload (autotuning off): the command ncu captures."""
@@ -626,7 +693,7 @@ def main():
     ap.add_argument("--controller", default="search", choices=["reference", "search", "learned"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--solve-once", action="store_true", help="one untimed FP64 + mixed solve (for ncu)")
-    ap.add_argument("--workload", default="heat2048", choices=["heat2048", "batch", "convdiff"])
+    ap.add_argument("--workload", default="heat2048", choices=["heat2048", "batch", "convdiff", "powerlaw"])
     ap.add_argument("--problems", type=int, default=256, help="batch workload: number of problems")
     ap.add_argument("--sample", type=int, default=8, help="batch workload: problems in the serial FP64 sample")
     ap.add_argument("--grid", type=int, default=2048, help="--solve-once: heat-equation grid size")
@@ -643,6 +710,9 @@ def main():
         return
     if args.workload == "convdiff" and args.impl == "ours":
         run_convdiff(args)
+        return
+    if args.workload == "powerlaw" and args.impl == "ours":
+        run_powerlaw(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

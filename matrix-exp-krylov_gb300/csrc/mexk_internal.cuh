@@ -82,6 +82,7 @@ enum : int {
 constexpr int SPMV_THREADS = 256;
 constexpr int SPMV_TILE = 2048;     // nonzeros staged per row block
 constexpr int SPMV_TILE_ROWS = 512; // rows per row block
+constexpr int SEQ_ROW_MAX = 64;     // longest row summed by one thread (reference order)
 constexpr int GS_THREADS = 256;
 constexpr int RED_STRIDE = 72;      // doubles per block partial (>= MEXK_M_MAX + 2)
 

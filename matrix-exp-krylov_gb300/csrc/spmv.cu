@@ -7,9 +7,12 @@
 // contiguous range of values and column indices with coalesced loads,
 // whatever the row-length distribution (Laplacian stencils, Zipf rows).
 // Phase 1 multiplies value * x[col] into shared memory; phase 2 sums each
-// row's products in column order. For rows that fit a tile the FP64 result
-// equals the reference's serial loop (main_cpu.cpp:388-397) bit for bit: one
-// rounded product per nonzero, added left to right. The gathers of x are
+// row's products. Rows of at most SEQ_ROW_MAX nonzeros are summed in column
+// order by one thread, so their FP64 result equals the reference's serial
+// loop (main_cpu.cpp:388-397) bit for bit: one rounded product per nonzero,
+// added left to right. Longer rows (the power-law tails) are summed by one
+// warp each, and rows longer than a tile by the whole block, in fixed
+// orders (deterministic, within rounding of the serial sum). The gathers of x are
 // served from L2 (x is one basis column, read right after it was written).
 #include "mexk_internal.cuh"
 
@@ -90,9 +93,13 @@ __global__ void __launch_bounds__(SPMV_THREADS)
     using TP = typename AccType<TX>::type;
     __shared__ TP prod[SPMV_TILE];
     __shared__ TP red[32];
+    __shared__ int s_long[SPMV_TILE / (SEQ_ROW_MAX + 1) + 1];
+    __shared__ int s_nlong;
     if (skip != nullptr && *skip) return;
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
+        if (tid == 0) s_nlong = 0;
         const int r0 = blocks[b];
         const int r1 = blocks[b + 1];
         const int e0 = row_ptr[r0];
@@ -159,15 +166,33 @@ __global__ void __launch_bounds__(SPMV_THREADS)
             }
         }
         __syncthreads();
-        // Phase 2: per-row left-to-right sums.
+        // Phase 2: rows of at most SEQ_ROW_MAX nonzeros are summed left to
+        // right by one thread (the reference's order); longer rows go to a
+        // list and are summed by one warp each.
 #pragma unroll
         for (int q = 0; q < RPT; ++q) {
             const int r = r0 + tid + q * SPMV_THREADS;
             if (r < r1) {
-                TP s = 0;
-                for (int p = ra[q] - e0; p < rz[q] - e0; ++p) s += prod[p];
-                y[r] = static_cast<TX>(s);
+                if (rz[q] - ra[q] > SEQ_ROW_MAX) {
+                    s_long[atomicAdd(&s_nlong, 1)] = r;
+                } else {
+                    TP s = 0;
+                    for (int p = ra[q] - e0; p < rz[q] - e0; ++p) s += prod[p];
+                    y[r] = static_cast<TX>(s);
+                }
             }
+        }
+        __syncthreads();
+        // Each lane sums its strided share in order, then a fixed butterfly:
+        // the result does not depend on which warp takes the row.
+        for (int i = tid >> 5; i < s_nlong; i += SPMV_THREADS / 32) {
+            const int r = s_long[i];
+            const int a = row_ptr[r] - e0;
+            const int z = row_ptr[r + 1] - e0;
+            TP s = 0;
+            for (int p = a + lane; p < z; p += 32) s += prod[p];
+            s = warp_sum(s);
+            if (lane == 0) y[r] = static_cast<TX>(s);
         }
         __syncthreads();
     }

@@ -51,10 +51,13 @@ def test_spmv_f64_bitwise(torch_cuda, oracle_mod, case):
     y = yd.cpu().numpy()
     y_ref = oracle_mod.spmv(A, x)
     lens = np.diff(A.row_ptr)
-    short = lens <= 2048
-    # Rows that fit one tile: one rounded product per nonzero, summed in order.
+    short = lens <= 64
+    # Rows of at most 64 nonzeros: one rounded product per nonzero, summed in
+    # order (longer rows are summed by a warp or the block: within rounding).
     assert np.array_equal(y[short], y_ref[short])
-    assert np.allclose(y[~short], y_ref[~short], rtol=1e-13, atol=0)
+    rows = np.repeat(np.arange(A.n), lens)
+    absum = np.bincount(rows, weights=np.abs(A.values * x[A.col_idx]), minlength=A.n)
+    assert np.all(np.abs(y[~short] - y_ref[~short]) <= 1e-13 * absum[~short])
 
 
 def test_spmv_long_rows_and_empty_rows(torch_cuda, oracle_mod):
@@ -139,10 +142,12 @@ def test_arnoldi_steps_vs_oracle(oracle_mod, precision):
     v = np.random.default_rng(5).standard_normal(A.n)
     V = np.zeros((m + 1, A.n))
     V[0] = v / np.linalg.norm(v)
+    ratios = []
     with Context(A, m_alloc=m) as ctx:
         ctx.set_basis(V[:1], precision=precision)
         for j in range(m):
             ok_o, h_o, beta_o, _ = oracle_mod.arnoldi_step(A, V, j)
+            ratios.append(np.sqrt(np.sum(np.asarray(h_o) ** 2) + beta_o ** 2) / beta_o)
             ok, h, beta = ctx.arnoldi_step(j, precision=precision)
             assert ok and ok_o
             scale = np.abs(h_o).max()
@@ -154,9 +159,13 @@ def test_arnoldi_steps_vs_oracle(oracle_mod, precision):
         Vg = ctx.get_basis(m + 1, precision=precision)
     tolv = 1e-12 if precision == "fp64" else 1e-4
     assert np.abs(Vg - V).max() < tolv
-    # orthonormality of the device basis
+    # Orthonormality of the device basis. FP64: CGS2 to rounding. Mixed: the
+    # Gram-corrected step measures and removes every earlier loss (no growth
+    # from step to step), but the FP32 rounding of its single update stays in
+    # the new column: a few u = 2^-24 times |w| / h_{j+1,j} of that step.
     G = Vg @ Vg.T
-    assert np.abs(G - np.eye(m + 1)).max() < (1e-13 if precision == "fp64" else 1e-6)
+    bound = 1e-13 if precision == "fp64" else 4 * 2.0 ** -24 * max(ratios)
+    assert np.abs(G - np.eye(m + 1)).max() < bound
 
 
 def test_arnoldi_breakdown_detected():
