@@ -84,6 +84,7 @@ __device__ __forceinline__ const float4* col4(const float* V, size_t ldv, int c)
 // of row block b / ngroups; the groups of one row block are adjacent in launch
 // order, so w and u_j are fetched from DRAM once and re-read from L2.
 __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
+    pdl_wait();
     DevState* st = g.st;
     if (st->breakdown || st->done) return;
     const int j = g.j;
@@ -118,6 +119,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
         }
         if (grp == 0) acc_w += dot4(x, x);
     }
+    pdl_trigger();
 
     // block stage: warp butterflies, then the warps in order, in FP64
     __shared__ double s_red[GW][2 * GG + 1];
@@ -151,11 +153,18 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
     __shared__ int s_flag;
     if (!grid_last_block(g.counter, &s_flag)) return;
     __shared__ double s_a[MEXK_M_MAX + 1], s_b[MEXK_M_MAX + 1], s_c[MEXK_M_MAX + 1], s_h[MEXK_M_MAX + 1];
+    __shared__ double s_sc[MEXK_M_MAX + 1];
+    __shared__ double s_G[MEXK_M_MAX][MEXK_M_MAX + 1];  // G(0:k, 0:k), row-major, padded
     __shared__ double s_scr[GT];
     __shared__ double s_w2, s_sj;
     __shared__ int s_bad;
     const int t = threadIdx.x;
+    GramState* gs = g.gs;
+    double* G = gs->G;
     {
+        // Every load of this stage is independent: the row-block partials
+        // (four running sums per thread, combined in a fixed order), the
+        // previous columns' Gram block and scales.
         const int nv = 2 * k + 1;
         const int groups = GT / nv;
         const int vi = t % nv;
@@ -163,8 +172,23 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
         double sum = 0.0;
         if (gi < groups) {
             const int off = vi < k ? vi : (vi < 2 * k ? GRAM_BOFF + (vi - k) : GRAM_NWOFF);
-            for (int b = gi; b < nrb; b += groups) sum += __ldcg(&g.part[static_cast<size_t>(b) * GRAM_STRIDE + off]);
+            const double* P = g.part + off;
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            int b = gi;
+            for (; b + 3 * groups < nrb; b += 4 * groups) {
+                a0 += __ldcg(P + static_cast<size_t>(b) * GRAM_STRIDE);
+                a1 += __ldcg(P + static_cast<size_t>(b + groups) * GRAM_STRIDE);
+                a2 += __ldcg(P + static_cast<size_t>(b + 2 * groups) * GRAM_STRIDE);
+                a3 += __ldcg(P + static_cast<size_t>(b + 3 * groups) * GRAM_STRIDE);
+            }
+            for (; b < nrb; b += groups) a0 += __ldcg(P + static_cast<size_t>(b) * GRAM_STRIDE);
+            sum = (a0 + a1) + (a2 + a3);
         }
+        for (int e = t; e < j * j; e += GT) {
+            const int r = e % j, c = e / j;
+            s_G[r][c] = G[r + static_cast<size_t>(c) * GRAM_LD];
+        }
+        if (t < j) s_sc[t] = gs->s[t];
         s_scr[t] = sum;
         __syncthreads();
         if (t < nv) {
@@ -176,7 +200,6 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
         }
         __syncthreads();
     }
-    GramState* gs = g.gs;
     const size_t ldh = static_cast<size_t>(g.ldh);
     if (t == 0) {
         const double bj = s_b[j];
@@ -193,18 +216,20 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
         }
         const double sj = (bj > 0.0 && !isinf(bj)) ? 1.0 / sqrt(bj) : 0.0;
         gs->s[j] = sj;
+        s_sc[j] = sj;
         s_sj = sj;
         s_bad = bad;
     }
     __syncthreads();
     if (s_bad) return;
     const double sj = s_sj;
-    double* G = gs->G;
     if (t < k) {
-        const double sc = (t == j) ? sj : gs->s[t];
+        const double sc = s_sc[t];
         const double gv = (t == j) ? 1.0 : sc * sj * s_b[t];
         G[t + static_cast<size_t>(j) * GRAM_LD] = gv;
         G[j + static_cast<size_t>(t) * GRAM_LD] = gv;
+        s_G[t][j] = gv;
+        s_G[j][t] = gv;
         s_c[t] = sc * sj * s_a[t];
     }
     __syncthreads();
@@ -213,19 +238,19 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
         if (g.reortho) {
             double e = 0.0;
             for (int q = 0; q < k; ++q)
-                if (q != t) e = fma(G[t + static_cast<size_t>(q) * GRAM_LD], s_c[q], e);
+                if (q != t) e = fma(s_G[t][q], s_c[q], e);
             hv -= e;
         }
         s_h[t] = hv;
         g.H[t + static_cast<size_t>(j) * ldh] = hv;
-        gs->coef[t] = static_cast<float>(((t == j) ? sj : gs->s[t]) * hv);
+        gs->coef[t] = static_cast<float>(s_sc[t] * hv);
     }
     __syncthreads();
     // |w - V h|^2 = |w|^2 - 2 h.c + h^T G h  (pre-scale of the new column)
     double part = 0.0;
     if (t < k) {
         double gh = 0.0;
-        for (int q = 0; q < k; ++q) gh = fma(G[t + static_cast<size_t>(q) * GRAM_LD], s_h[q], gh);
+        for (int q = 0; q < k; ++q) gh = fma(s_G[t][q], s_h[q], gh);
         part = s_h[t] * gh - 2.0 * s_h[t] * s_c[t];
     }
     part = block_sum(part, s_scr);
@@ -244,6 +269,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
 // Sweep 2: u_{j+1} = psc * (wsc * w - sum_c coef_c u_c), written to column
 // j+1 with a default (L2-allocating) store: the next SpMV gathers from it.
 __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
+    pdl_wait();
     DevState* st = g.st;
     if (st->breakdown || st->done) return;
     __shared__ float s_coef[MEXK_M_MAX + UCH];
@@ -289,6 +315,7 @@ __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
         r.w = fmaf(x.w, wsc, -s.w) * psc;
         out[i] = r;
     }
+    pdl_trigger();
 }
 
 // |u_{j+1}|^2 by grid reduction; the last block sets H(j+1, j), s_{j+1} and
@@ -357,15 +384,21 @@ int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
     // second wave would run at half occupancy); 2 row blocks per SM at most.
     int nrb = row_blocks(a.n, 2);
     if (ngroups > 2) nrb = std::min(nrb, std::max(1, 4 * device_sm_count() / ngroups));
-    gram_dot_kernel<<<nrb * ngroups, GT, 0, s>>>(a);
-    MEXK_CK_LAUNCH("gram_dot_kernel");
+    const cudaError_t e = launch_dependent(gram_dot_kernel, nrb * ngroups, GT, 0, s, a);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "gram_dot_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
     return MEXK_OK;
 }
 
 int launch_gram_update(const GramArgs& a, cudaStream_t s) {
     if (a.j < 0 || a.j >= MEXK_M_MAX) return MEXK_ERR_INVALID;
-    gram_update_kernel<<<row_blocks(a.n, 4), GT, 0, s>>>(a);
-    MEXK_CK_LAUNCH("gram_update_kernel");
+    const cudaError_t e = launch_dependent(gram_update_kernel, row_blocks(a.n, 4), GT, 0, s, a);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "gram_update_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
     return MEXK_OK;
 }
 

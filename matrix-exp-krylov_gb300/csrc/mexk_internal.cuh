@@ -87,6 +87,30 @@ constexpr int GS_THREADS = 256;
 constexpr int RED_STRIDE = 72;      // doubles per block partial (>= MEXK_M_MAX + 2)
 
 // ------------------------------------------------------------ helpers
+// Programmatic dependent launch: a kernel launched with launch_dependent()
+// may start while the previous kernel of the stream finishes; it calls
+// pdl_wait() before reading anything that kernel wrote, and the previous
+// kernel calls pdl_trigger() once its blocks no longer need the launch held
+// back. Both are no-ops for ordinary launches.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_dependent(void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                             Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -204,7 +228,17 @@ __device__ __forceinline__ void reduce_partials(const double* partials, int nblo
     const int g = t / ncols;
     double s = 0.0;
     if (g < groups) {
-        for (int b = g; b < nblocks; b += groups) s += __ldcg(&partials[(size_t)b * RED_STRIDE + c]);
+        // four independent running sums (their loads overlap), fixed combination order
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int b = g;
+        for (; b + 3 * groups < nblocks; b += 4 * groups) {
+            s0 += __ldcg(&partials[(size_t)b * RED_STRIDE + c]);
+            s1 += __ldcg(&partials[(size_t)(b + groups) * RED_STRIDE + c]);
+            s2 += __ldcg(&partials[(size_t)(b + 2 * groups) * RED_STRIDE + c]);
+            s3 += __ldcg(&partials[(size_t)(b + 3 * groups) * RED_STRIDE + c]);
+        }
+        for (; b < nblocks; b += groups) s0 += __ldcg(&partials[(size_t)b * RED_STRIDE + c]);
+        s = (s0 + s1) + (s2 + s3);
     }
     scratch[t] = s;
     __syncthreads();

@@ -95,6 +95,7 @@ __global__ void __launch_bounds__(SPMV_THREADS)
     __shared__ TP red[32];
     __shared__ int s_long[SPMV_TILE / (SEQ_ROW_MAX + 1) + 1];
     __shared__ int s_nlong;
+    pdl_wait();
     if (skip != nullptr && *skip) return;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
@@ -183,6 +184,7 @@ __global__ void __launch_bounds__(SPMV_THREADS)
             }
         }
         __syncthreads();
+        if (b + static_cast<int>(gridDim.x) >= nblocks) pdl_trigger();  // this block's last row block
         // Each lane sums its strided share in order, then a fixed butterfly:
         // the result does not depend on which warp takes the row.
         for (int i = tid >> 5; i < s_nlong; i += SPMV_THREADS / 32) {
@@ -206,8 +208,15 @@ int launch_spmv(int n, int nblocks, const int* blocks, const int* row_ptr, const
     const bool vec = padded && reinterpret_cast<uintptr_t>(col_idx) % 16 == 0 &&
                      reinterpret_cast<uintptr_t>(values) % 16 == 0;
     if (vec)
-        spmv_rowblock_kernel<TA, TX, true><<<grid, SPMV_THREADS, 0, s>>>(nblocks, blocks, row_ptr, col_idx,
-                                                                         values, x, y, skip_flag);
+    {
+        const cudaError_t e = launch_dependent(spmv_rowblock_kernel<TA, TX, true>, grid, SPMV_THREADS, 0, s,
+                                               nblocks, blocks, row_ptr, col_idx, values, x, y, skip_flag);
+        if (e != cudaSuccess) {
+            set_cuda_error(e, "spmv_rowblock_kernel", __FILE__, __LINE__);
+            return MEXK_ERR_CUDA;
+        }
+        return MEXK_OK;
+    }
     else
         spmv_rowblock_kernel<TA, TX, false><<<grid, SPMV_THREADS, 0, s>>>(nblocks, blocks, row_ptr, col_idx,
                                                                           values, x, y, skip_flag);
