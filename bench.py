@@ -102,9 +102,12 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ bytes model
-def kernel_bytes(kind, n, nnz, k, fp32):
-    """Algorithmic HBM bytes of one launch (per-kernel minimum traffic)."""
+def kernel_bytes(kind, n, nnz, k, fp32, window=0):
+    """Algorithmic HBM bytes of one launch (per-kernel minimum traffic); with a
+    short-recurrence window the sweeps touch only the last `window` columns."""
     s = 4 if fp32 else 8
+    if window and kind in ("gram_dot", "gram_update"):
+        k = min(k, window)
     if kind == "spmv":
         return nnz * (s + 4) + 4 * (n + 1) + 2 * n * s  # values+cols, row_ptr, x once, y
     if kind in ("gs_dot", "gram_dot"):
@@ -132,8 +135,9 @@ STEP_KINDS = {"fp64": ["spmv", "gs_dot", "gs_upd_dot", "gs_upd_norm", "normalize
 CYCLE_KINDS = {"fp64": ["controller", "lift"], "mixed": ["controller", "lift", "gram_norm"]}
 
 
-def profile_cycle(ctx, m, n, nnz, precision, iters=2):
-    """CUDA-event timing of every kernel kind of one Krylov cycle."""
+def profile_cycle(ctx, m, n, nnz, precision, iters=2, window=0):
+    """CUDA-event timing of every kernel kind of one Krylov cycle (the sweeps
+    as the context's last solve ran them: with its window, if any)."""
     fp32 = precision == "mixed"
     kinds = STEP_KINDS[precision]
     once = CYCLE_KINDS[precision]
@@ -142,13 +146,13 @@ def profile_cycle(ctx, m, n, nnz, precision, iters=2):
     for kind in once:
         ms = ctx.profile_kernel(kind, m - 1, iters, precision)
         per[kind]["ms"] += ms
-        per[kind]["bytes"] += kernel_bytes(kind, n, nnz, m, fp32)
+        per[kind]["bytes"] += kernel_bytes(kind, n, nnz, m, fp32, window)
         per[kind]["launches"] += 1
     for j in range(m):
         for kind in kinds:
             ms = ctx.profile_kernel(kind, j, iters, precision)
             per[kind]["ms"] += ms
-            per[kind]["bytes"] += kernel_bytes(kind, n, nnz, j + 1, fp32)
+            per[kind]["bytes"] += kernel_bytes(kind, n, nnz, j + 1, fp32, window)
             per[kind]["launches"] += 1
     return per
 
@@ -251,33 +255,46 @@ def run_ours(args, rank, world, local_rank):
     # chosen form is the fastest candidate within 1e-6 of it.
     res64 = ctx.expmv_device(v_d.data_ptr(), y64.data_ptr(), P.t, m, precision="fp64")
     steps64 = ctx.steps()
-    candidates = [("mixed", "learned"), ("mixed", "search"), ("mixed", "reference"), ("fp64", "search")]
+    # (precision, controller, window): window 2 = Lanczos' short recurrence,
+    # which the library accepts only for a symmetric matrix (refusals skipped).
+    candidates = [("mixed", "search", 2), ("mixed", "learned", 0), ("mixed", "search", 0),
+                  ("mixed", "reference", 0), ("fp64", "search", 0)]
     if args.precision != "auto":
-        candidates = [(args.precision, args.controller)]
+        candidates = [(args.precision, args.controller, args.window)]
     checked = []
-    for prec, ctrl in candidates:
-        r = ctx.expmv_device(v_d.data_ptr(), y32.data_ptr(), P.t, m, precision=prec, controller=ctrl)
+    from mexk._lib import MexkError
+    for prec, ctrl, win in candidates:
+        try:
+            r = ctx.expmv_device(v_d.data_ptr(), y32.data_ptr(), P.t, m, precision=prec, controller=ctrl,
+                                 window=win)
+        except MexkError as exc:
+            print(f"skipping {prec}+{ctrl}+w{win}: {exc}", file=sys.stderr)
+            continue
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ctx.expmv_device(v_d.data_ptr(), y32.data_ptr(), P.t, m, precision=prec, controller=ctrl)
+        ctx.expmv_device(v_d.data_ptr(), y32.data_ptr(), P.t, m, precision=prec, controller=ctrl, window=win)
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
         e = float(torch.linalg.norm(y32 - y64) / torch.linalg.norm(y64))
-        checked.append({"precision": prec, "controller": ctrl, "rel_err_vs_fp64": e, "cycles": r["cycles"],
-                        "attempts": r["attempts"], "solve_ms": round(secs * 1e3, 2), "steps": ctx.steps()})
+        checked.append({"precision": prec, "controller": ctrl, "window": win, "rel_err_vs_fp64": e,
+                        "cycles": r["cycles"], "attempts": r["attempts"], "solve_ms": round(secs * 1e3, 2),
+                        "steps": ctx.steps()})
     ok = [c for c in checked if c["rel_err_vs_fp64"] <= 1e-6] or [{"precision": "fp64", "controller": "reference",
-                                                                  "rel_err_vs_fp64": 0.0, "cycles": res64["cycles"],
+                                                                  "window": 0, "rel_err_vs_fp64": 0.0,
+                                                                  "cycles": res64["cycles"],
                                                                   "attempts": res64["attempts"], "solve_ms": 0.0,
                                                                   "steps": steps64}]
     chosen = min(ok, key=lambda c: c["solve_ms"])  # fastest single solve
     form, ctrl_form, rel_err = chosen["precision"], chosen["controller"], chosen["rel_err_vs_fp64"]
+    win_form = chosen["window"]
     steps32 = chosen["steps"]
 
-    def timed(precision, K, W, controller="reference"):
+    def timed(precision, K, W, controller="reference", window=0):
         out = torch.zeros(n, dtype=torch.float64, device="cuda")
         res = None
         for _ in range(W):
-            res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), P.t, m, precision=precision, controller=controller)
+            res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), P.t, m, precision=precision, controller=controller,
+                                   window=window)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -288,7 +305,7 @@ def run_ours(args, rank, world, local_rank):
             e0.record(stream)
             for _ in range(K):
                 res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), P.t, m, precision=precision,
-                                       controller=controller)
+                                       controller=controller, window=window)
                 launches += launches_per_solve(ctx, precision, res, m)
             e1.record(stream)
             torch.cuda.synchronize()
@@ -300,9 +317,9 @@ def run_ours(args, rank, world, local_rank):
             ms = float(t.item())
         return ms, res, launches, clk.summary()
 
-    ms_c, res_c, launches, clocks = timed(form, args.steps, args.warmup, ctrl_form)
+    ms_c, res_c, launches, clocks = timed(form, args.steps, args.warmup, ctrl_form, win_form)
     value = world * args.steps / (ms_c / 1e3)
-    same = form == "fp64" and ctrl_form == "reference"
+    same = form == "fp64" and ctrl_form == "reference" and not win_form
     ms64, _, _, _ = timed("fp64", max(1, args.steps), 1) if not same else (ms_c, None, None, None)
     fp64_sps = world * max(1, args.steps) / (ms64 / 1e3)
 
@@ -314,7 +331,7 @@ def run_ours(args, rank, world, local_rank):
     from mexk._lib import Result, check, lib
     from mexk.api import params as mkparams
 
-    pr = mkparams(m, P.t, precision=form, controller=ctrl_form)
+    pr = mkparams(m, P.t, precision=form, controller=ctrl_form, window=win_form)
     r = Result()
     vp = C.cast(v_pin.data_ptr(), C.POINTER(C.c_double))
     yp = C.cast(y_pin.data_ptr(), C.POINTER(C.c_double))
@@ -335,7 +352,7 @@ def run_ours(args, rank, world, local_rank):
 
     # kernel roofline from live CUDA-event timings of each kernel kind
     peak, peak_kind = measured_peaks()
-    per = profile_cycle(ctx, m, n, nnz, form)
+    per = profile_cycle(ctx, m, n, nnz, form, window=win_form)
     tot_ms = sum(p["ms"] for p in per.values())
     dom = max(per, key=lambda k: per[k]["ms"])
     ach = per[dom]["bytes"] / (per[dom]["ms"] / 1e3) / 1e9
@@ -367,7 +384,8 @@ def run_ours(args, rank, world, local_rank):
             "warmup": args.warmup, "ms_per_step": ms_c / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if form == "mixed" else "f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "form": f"{form} + {ctrl_form} controller",
+            "config": {"workload": WORKLOAD,
+                       "form": f"{form} + {ctrl_form} controller" + (f" + window {win_form}" if win_form else ""),
                        "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (CSR 251 MB, basis >= 520 MB); no flush"},
             "fp64_solves_per_s": fp64_sps, "chosen_rel_err_vs_fp64": rel_err,
@@ -381,10 +399,11 @@ def run_ours(args, rank, world, local_rank):
             "kernels": {f: {k: {"ms_per_cycle": round(p["ms"], 4),
                                 "gbs": round(p["bytes"] / (p["ms"] / 1e3) / 1e9, 1) if p["bytes"] else None}
                             for k, p in pp.items()} for f, pp in (("chosen", per), ("fp64", per64))},
-            "gram_schmidt_vs_cgs2_bytes": {"chosen": gs_cgs2_equivalent(per, n, m, form),
+            "gram_schmidt_vs_cgs2_bytes": {"chosen": gs_cgs2_equivalent(per, n, m, form) if not win_form else None,
                                            "fp64": gs_cgs2_equivalent(per64, n, m, "fp64")},
             "trace": {"fp64": [(round(s[1], 12), float(f"{s[2]:.3g}")) for s in steps64],
-                      **{f"{c['precision']}+{c['controller']}": [(round(s[1], 12), float(f"{s[2]:.3g}"))
+                      **{f"{c['precision']}+{c['controller']}" + (f"+w{c['window']}" if c["window"] else ""):
+                         [(round(s[1], 12), float(f"{s[2]:.3g}"))
                                                                  for s in c["steps"]] for c in checked}},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
         }
@@ -691,6 +710,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--controller", default="search", choices=["reference", "search", "learned"])
+    ap.add_argument("--window", type=int, default=0, help="with --precision: short-recurrence window (0 = Arnoldi)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--solve-once", action="store_true", help="one untimed FP64 + mixed solve (for ncu)")
     ap.add_argument("--workload", default="heat2048", choices=["heat2048", "batch", "convdiff", "powerlaw"])

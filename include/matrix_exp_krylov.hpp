@@ -140,6 +140,9 @@ struct ArnoldiRunner {
     // lines, and the statistics of the last solve.
     int precision = MEXK_PREC_FP64;
     int controller = MEXK_CTRL_REFERENCE;
+    // 0: orthogonalise against the whole basis; W >= 2: against the last W
+    // vectors (mixed precision, symmetric A only; no reference counterpart).
+    int ortho_window = 0;
     bool net_loaded = false;
     bool verbose = true;
     mexk_result_t last_result{};

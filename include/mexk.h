@@ -59,6 +59,11 @@ typedef struct {
     int reorthogonalize; /* nonzero: second Gram-Schmidt pass (CLI always on) */
     int precision;       /* MEXK_PREC_* */
     int controller;      /* MEXK_CTRL_*: step-size control (0 = the reference's) */
+    int ortho_window;    /* 0: orthogonalise against the whole basis (Arnoldi, the
+                            reference's method). W >= 2 (mixed precision, symmetric A
+                            only): against the last W basis vectors, the short
+                            recurrence of Lanczos; the context verifies symmetry
+                            (MEXK_ERR_INVALID otherwise). No reference counterpart. */
 } mexk_params_t;
 
 /* Outcome of one solve. converged / restarts_done / last_residual are the
@@ -303,7 +308,8 @@ int mexk_batch_destroy(mexk_batch_t b);
  * launch duration in milliseconds. No reference counterpart (the reference
  * times only the whole solve, METRIC total_compute_expmv_ms at main.cu:1570).
  * A kind marked FP64 or mixed returns MEXK_ERR_UNSUPPORTED for the other
- * precision. */
+ * precision. The mixed sweeps use the ortho_window of the context's last
+ * solve. */
 int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int iters, double* ms_per_launch);
 
 #ifdef __cplusplus

@@ -32,6 +32,10 @@
 // comes from |w - V h|^2 = |w|^2 - 2 h.c + h^T G h and only keeps the stored
 // column near unit length: the next step measures its norm exactly.
 //
+// With a window of W columns (symmetric A only: the short recurrence of
+// Lanczos) both sweeps use columns j+1-W..j and H(0:j-W, j) = 0; the Gram
+// correction then re-orthogonalises against the window.
+//
 // Dots multiply and accumulate in FP32 per thread (a few dozen terms), then
 // sum across warps, blocks and the grid in FP64 in a fixed order, so every
 // result is deterministic. The FP64 path keeps explicit CGS2 sweeps
@@ -89,11 +93,13 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
     if (st->breakdown || st->done) return;
     const int j = g.j;
     const int k = j + 1;
-    const int ngroups = (k + GG - 1) / GG;
+    const int lo = g.lo;      // columns lo..j take part (lo = 0: all)
+    const int kw = k - lo;
+    const int ngroups = (kw + GG - 1) / GG;
     const int grp = blockIdx.x % ngroups;
     const int rb = blockIdx.x / ngroups;
     const int nrb = gridDim.x / ngroups;
-    const int c0 = grp * GG;
+    const int c0 = lo + grp * GG;
     const size_t ldv = static_cast<size_t>(g.ldv);
     const float4* __restrict__ w4 = reinterpret_cast<const float4*>(g.w);
     const float4* __restrict__ u4 = col4(g.V, ldv, j);
@@ -165,13 +171,13 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
         // Every load of this stage is independent: the row-block partials
         // (four running sums per thread, combined in a fixed order), the
         // previous columns' Gram block and scales.
-        const int nv = 2 * k + 1;
+        const int nv = 2 * kw + 1;
         const int groups = GT / nv;
         const int vi = t % nv;
         const int gi = t / nv;
         double sum = 0.0;
         if (gi < groups) {
-            const int off = vi < k ? vi : (vi < 2 * k ? GRAM_BOFF + (vi - k) : GRAM_NWOFF);
+            const int off = vi < kw ? lo + vi : (vi < 2 * kw ? GRAM_BOFF + lo + (vi - kw) : GRAM_NWOFF);
             const double* P = g.part + off;
             double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
             int b = gi;
@@ -184,18 +190,19 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
             for (; b < nrb; b += groups) a0 += __ldcg(P + static_cast<size_t>(b) * GRAM_STRIDE);
             sum = (a0 + a1) + (a2 + a3);
         }
-        for (int e = t; e < j * j; e += GT) {
-            const int r = e % j, c = e / j;
+        const int jw = j - lo;  // previous columns inside the window
+        for (int e = t; e < jw * jw; e += GT) {
+            const int r = lo + e % jw, c = lo + e / jw;
             s_G[r][c] = G[r + static_cast<size_t>(c) * GRAM_LD];
         }
-        if (t < j) s_sc[t] = gs->s[t];
+        if (t >= lo && t < j) s_sc[t] = gs->s[t];
         s_scr[t] = sum;
         __syncthreads();
         if (t < nv) {
             double tot = 0.0;
             for (int q = 0; q < groups; ++q) tot += s_scr[q * nv + t];
-            if (t < k) s_a[t] = tot;
-            else if (t < 2 * k) s_b[t - k] = tot;
+            if (t < kw) s_a[lo + t] = tot;
+            else if (t < 2 * kw) s_b[lo + t - kw] = tot;
             else s_w2 = tot;
         }
         __syncthreads();
@@ -223,7 +230,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
     __syncthreads();
     if (s_bad) return;
     const double sj = s_sj;
-    if (t < k) {
+    if (t >= lo && t < k) {
         const double sc = s_sc[t];
         const double gv = (t == j) ? 1.0 : sc * sj * s_b[t];
         G[t + static_cast<size_t>(j) * GRAM_LD] = gv;
@@ -233,11 +240,13 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
         s_c[t] = sc * sj * s_a[t];
     }
     __syncthreads();
-    if (t < k) {
+    if (t < lo) {
+        g.H[t + static_cast<size_t>(j) * ldh] = 0.0;  // outside the window
+    } else if (t < k) {
         double hv = s_c[t];
         if (g.reortho) {
             double e = 0.0;
-            for (int q = 0; q < k; ++q)
+            for (int q = lo; q < k; ++q)
                 if (q != t) e = fma(s_G[t][q], s_c[q], e);
             hv -= e;
         }
@@ -248,9 +257,9 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
     __syncthreads();
     // |w - V h|^2 = |w|^2 - 2 h.c + h^T G h  (pre-scale of the new column)
     double part = 0.0;
-    if (t < k) {
+    if (t >= lo && t < k) {
         double gh = 0.0;
-        for (int q = 0; q < k; ++q) gh = fma(s_G[t][q], s_h[q], gh);
+        for (int q = lo; q < k; ++q) gh = fma(s_G[t][q], s_h[q], gh);
         part = s_h[t] * gh - 2.0 * s_h[t] * s_c[t];
     }
     part = block_sum(part, s_scr);
@@ -275,6 +284,7 @@ __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
     __shared__ float s_coef[MEXK_M_MAX + UCH];
     __shared__ float s_sc[2];
     const int k = g.j + 1;
+    const int lo = g.lo;
     const GramState* gs = g.gs;
     if (threadIdx.x < MEXK_M_MAX + UCH) s_coef[threadIdx.x] = threadIdx.x < k ? gs->coef[threadIdx.x] : 0.f;
     if (threadIdx.x == 0) {
@@ -292,7 +302,8 @@ __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
         const float4 x = __ldg(w4 + i);
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int cb = 0; cb < MEXK_M_MAX; cb += UCH) {
+        for (int cbi = 0; cbi < MEXK_M_MAX; cbi += UCH) {
+            const int cb = lo + cbi;
             if (cb < k) {
                 float4 v[UCH];
 #pragma unroll
@@ -379,7 +390,8 @@ int device_sm_count() {
 
 int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
     if (a.j < 0 || a.j >= MEXK_M_MAX) return MEXK_ERR_INVALID;
-    const int ngroups = (a.j + 1 + GG - 1) / GG;
+    if (a.lo < 0 || a.lo > a.j) return MEXK_ERR_INVALID;
+    const int ngroups = (a.j + 1 - a.lo + GG - 1) / GG;
     // One wave of 4 resident blocks per SM over all column groups (a partial
     // second wave would run at half occupancy); 2 row blocks per SM at most.
     int nrb = row_blocks(a.n, 2);
@@ -393,7 +405,7 @@ int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
 }
 
 int launch_gram_update(const GramArgs& a, cudaStream_t s) {
-    if (a.j < 0 || a.j >= MEXK_M_MAX) return MEXK_ERR_INVALID;
+    if (a.j < 0 || a.j >= MEXK_M_MAX || a.lo < 0 || a.lo > a.j) return MEXK_ERR_INVALID;
     const cudaError_t e = launch_dependent(gram_update_kernel, row_blocks(a.n, 4), GT, 0, s, a);
     if (e != cudaSuccess) {
         set_cuda_error(e, "gram_update_kernel", __FILE__, __LINE__);

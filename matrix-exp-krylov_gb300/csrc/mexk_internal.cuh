@@ -256,6 +256,9 @@ __device__ __forceinline__ void reduce_partials(const double* partials, int nblo
 std::vector<int> build_row_blocks(int n, const int* row_ptr);
 
 int launch_narrow_values(const double* src, float* dst, size_t count, cudaStream_t s);
+// *ok = 1 when A equals its transpose exactly, else 0.
+int launch_symmetric_check(int n, const int* row_ptr, const int* col_idx, const double* values, int* ok,
+                           cudaStream_t s);
 
 // padded: col_idx and values are 16-byte aligned with at least 3 readable
 // entries past nnz (the context's arrays), enabling 16-byte group loads.
@@ -309,6 +312,7 @@ struct GramState {
 };
 struct GramArgs {
     int n, j, ldv, ldh, reortho;
+    int lo = 0;        // first basis column of the step (0: all; j+1-W for a window of W)
     float* V;          // FP32 basis, column-major, ldv >= 4*ceil(n/4), rows n..ldv-1 zero
     const float* w;    // A u_j (unscaled), rows n..ldv-1 zero
     double* H;

@@ -53,7 +53,7 @@ constexpr int LOG_CAP = 8192;
 using namespace mexk;
 
 struct GraphEntry {
-    int m, prec, reortho, ctrl;
+    int m, prec, reortho, ctrl, window;
     cudaGraphExec_t exec;
 };
 
@@ -67,6 +67,8 @@ struct mexk_context_s {
     int ldv = 0;
     int ldh = 0;
     int nblocks = 0;
+    int symmetric = -1;  // A == A^T exactly: -1 not yet checked
+    int last_window = 0; // ortho_window of the last solve (kernel profiling follows it)
     int* d_row_ptr = nullptr;
     int* d_col = nullptr;
     double* d_val = nullptr;
@@ -114,7 +116,31 @@ void dfree(T*& p) {
     p = nullptr;
 }
 
-int check_params(const mexk_context_t ctx, const mexk_params_t* p) {
+// Whether A equals its transpose exactly (checked on the device once).
+int matrix_symmetric(mexk_context_t ctx, int* sym) {
+    if (ctx->symmetric < 0) {
+        int* d_ok = nullptr;
+        int rc = dalloc(&d_ok, 1);
+        if (rc) return rc;
+        rc = launch_symmetric_check(ctx->n, ctx->d_row_ptr, ctx->d_col, ctx->d_val, d_ok, ctx->stream);
+        int ok = 0;
+        if (!rc) {
+            const cudaError_t e1 = cudaMemcpyAsync(&ok, d_ok, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+            const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+            if (e1 != cudaSuccess || e2 != cudaSuccess) {
+                set_cuda_error(e1 != cudaSuccess ? e1 : e2, "symmetry check", __FILE__, __LINE__);
+                rc = MEXK_ERR_CUDA;
+            }
+        }
+        dfree(d_ok);
+        if (rc) return rc;
+        ctx->symmetric = ok ? 1 : 0;
+    }
+    *sym = ctx->symmetric;
+    return MEXK_OK;
+}
+
+int check_params(mexk_context_t ctx, const mexk_params_t* p) {
     if (!ctx || !p) return MEXK_ERR_INVALID;
     if (!ctx->uploaded) return MEXK_ERR_NOT_READY;
     if (p->m < 1 || p->m > ctx->m_alloc || p->m > MEXK_M_MAX) {
@@ -131,6 +157,23 @@ int check_params(const mexk_context_t ctx, const mexk_params_t* p) {
     if (p->controller == MEXK_CTRL_LEARNED && ctx->d_mlp == nullptr) {
         set_error_text("learned controller requested but no controller network is loaded");
         return MEXK_ERR_NOT_READY;
+    }
+    if (p->ortho_window != 0) {
+        if (p->ortho_window < 2 || p->ortho_window > p->m) {
+            set_error_text("ortho_window must be 0 or in 2..m");
+            return MEXK_ERR_INVALID;
+        }
+        if (p->precision != MEXK_PREC_MIXED) {
+            set_error_text("a short-recurrence window is implemented for the mixed form only");
+            return MEXK_ERR_UNSUPPORTED;
+        }
+        int sym = 0;
+        const int rc = matrix_symmetric(ctx, &sym);
+        if (rc) return rc;
+        if (!sym) {
+            set_error_text("a short-recurrence window needs a symmetric matrix");
+            return MEXK_ERR_INVALID;
+        }
     }
     return MEXK_OK;
 }
@@ -224,7 +267,7 @@ LiftArgs lift_args(mexk_context_t ctx, bool fp32) {
 // Arnoldi step j: w = A v_j, then orthogonalise into column j+1 and H(:, j).
 // The FP64 form finishes the step (H(j+1, j), normalised column); the mixed
 // form leaves H(j+1, j) to the next step's dot sweep or to finish_basis.
-int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t s) {
+int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t s, int window = 0) {
     const size_t ldv = static_cast<size_t>(ctx->ldv);
     int rc;
     if (fp32) {
@@ -232,7 +275,8 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
                                             ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32,
                                             &ctx->d_state->breakdown, s, true)))
             return rc;
-        const GramArgs g = gram_args(ctx, j, reortho);
+        GramArgs g = gram_args(ctx, j, reortho);
+        g.lo = window > 0 ? std::max(0, j + 1 - window) : 0;
         if ((rc = launch_gram_dot(g, s))) return rc;
         return launch_gram_update(g, s);
     }
@@ -255,12 +299,12 @@ int finish_basis(mexk_context_t ctx, int j, bool fp32, cudaStream_t s) {
 
 // One Krylov cycle: the unit that is captured into a graph.
 template <typename TV>
-int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, cudaStream_t s) {
+int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, cudaStream_t s) {
     const bool fp32 = sizeof(TV) == 4;
     TV* V = fp32 ? reinterpret_cast<TV*>(ctx->d_V32) : reinterpret_cast<TV*>(ctx->d_V);
     int rc;
     for (int j = 0; j < m; ++j)
-        if ((rc = enqueue_step(ctx, j, reortho, fp32, s))) return rc;
+        if ((rc = enqueue_step(ctx, j, reortho, fp32, s, window))) return rc;
     if ((rc = finish_basis(ctx, m - 1, fp32, s))) return rc;
     if (ctrl == MEXK_CTRL_REFERENCE) {
         ControlArgs c;
@@ -288,21 +332,21 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, cudaStream_t
     return launch_restart<TV>(ctx->n, ctx->ldv, ctx->d_y, V, ctx->d_state, s);
 }
 
-int enqueue_cycle_any(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, cudaStream_t s) {
-    return prec == MEXK_PREC_MIXED ? enqueue_cycle<float>(ctx, m, reortho, ctrl, s)
-                                   : enqueue_cycle<double>(ctx, m, reortho, ctrl, s);
+int enqueue_cycle_any(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, int window, cudaStream_t s) {
+    return prec == MEXK_PREC_MIXED ? enqueue_cycle<float>(ctx, m, reortho, ctrl, window, s)
+                                   : enqueue_cycle<double>(ctx, m, reortho, ctrl, 0, s);
 }
 
-int get_graph(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, cudaGraphExec_t* out) {
+int get_graph(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, int window, cudaGraphExec_t* out) {
     for (auto& g : ctx->graphs) {
-        if (g.m == m && g.prec == prec && g.reortho == reortho && g.ctrl == ctrl) {
+        if (g.m == m && g.prec == prec && g.reortho == reortho && g.ctrl == ctrl && g.window == window) {
             *out = g.exec;
             return MEXK_OK;
         }
     }
     cudaGraph_t graph = nullptr;
     MEXK_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_cycle_any(ctx, m, prec, reortho, ctrl, ctx->stream);
+    int rc = enqueue_cycle_any(ctx, m, prec, reortho, ctrl, window, ctx->stream);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
     if (rc != MEXK_OK) {
         if (graph) cudaGraphDestroy(graph);
@@ -319,7 +363,7 @@ int get_graph(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, cudaGr
         set_cuda_error(e, "cudaGraphInstantiate", __FILE__, __LINE__);
         return MEXK_ERR_CUDA;
     }
-    ctx->graphs.push_back({m, prec, reortho, ctrl, exec});
+    ctx->graphs.push_back({m, prec, reortho, ctrl, window, exec});
     *out = exec;
     return MEXK_OK;
 }
@@ -357,6 +401,7 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
     if (rc) return rc;
     if (p->precision == MEXK_PREC_MIXED && (rc = ensure_mixed(ctx))) return rc;
     if (s == nullptr) s = ctx->stream;
+    ctx->last_window = p->ortho_window;
     init_state(ctx->h_state, p, LOG_CAP);
     MEXK_CK(cudaMemcpyAsync(ctx->d_state, ctx->h_state, sizeof(DevState), cudaMemcpyHostToDevice, s));
     if (ctx->h_state->done) {
@@ -381,9 +426,11 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
             if (ctx->use_graph) {
                 // Graphs are captured on the context stream and launched on `s`.
                 cudaGraphExec_t exec = nullptr;
-                if ((rc = get_graph(ctx, m_cycle, p->precision, reortho, p->controller, &exec))) return rc;
+                if ((rc = get_graph(ctx, m_cycle, p->precision, reortho, p->controller, p->ortho_window, &exec)))
+                    return rc;
                 MEXK_CK(cudaGraphLaunch(exec, s));
-            } else if ((rc = enqueue_cycle_any(ctx, m_cycle, p->precision, reortho, p->controller, s))) {
+            } else if ((rc = enqueue_cycle_any(ctx, m_cycle, p->precision, reortho, p->controller, p->ortho_window,
+                                               s))) {
                 return rc;
             }
             MEXK_CK(cudaMemcpyAsync(ctx->h_state, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
@@ -824,7 +871,8 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
     MEXK_CK(cudaEventCreate(&e1));
     const size_t ldv = static_cast<size_t>(ctx->ldv);
     const GsArgs g = gs_args(ctx, j, 1, false);
-    const GramArgs ga = fp32 ? gram_args(ctx, j, 1) : GramArgs{};
+    GramArgs ga = fp32 ? gram_args(ctx, j, 1) : GramArgs{};
+    ga.lo = (fp32 && ctx->last_window > 0) ? std::max(0, j + 1 - ctx->last_window) : 0;
     const int grid = gs_grid_size(ctx->n, j + 1);
     double total = 0.0;
     rc = MEXK_OK;

@@ -246,6 +246,41 @@ int launch_narrow_values(const double* src, float* dst, size_t count, cudaStream
     return MEXK_OK;
 }
 
+// A == A^T exactly: every entry (r, c, v) has an entry (c, r, v). One thread
+// per row scans, for each of its entries, row c for column r.
+__global__ void symmetric_check_kernel(int n, const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
+                                       const double* __restrict__ values, int* __restrict__ ok) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        for (int e = row_ptr[r]; e < row_ptr[r + 1]; ++e) {
+            const int c = col_idx[e];
+            const double v = values[e];
+            bool found = false;
+            for (int f = row_ptr[c]; f < row_ptr[c + 1]; ++f)
+                if (col_idx[f] == r && values[f] == v) {
+                    found = true;
+                    break;
+                }
+            if (!found) {
+                atomicAnd(ok, 0);
+                return;
+            }
+        }
+    }
+}
+
+__global__ void set_one_kernel(int* p) { *p = 1; }
+
+int launch_symmetric_check(int n, const int* row_ptr, const int* col_idx, const double* values, int* ok,
+                           cudaStream_t s) {
+    set_one_kernel<<<1, 1, 0, s>>>(ok);
+    MEXK_CK_LAUNCH("set_one_kernel");
+    if (n <= 0) return MEXK_OK;
+    const int grid = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+    symmetric_check_kernel<<<grid, 256, 0, s>>>(n, row_ptr, col_idx, values, ok);
+    MEXK_CK_LAUNCH("symmetric_check_kernel");
+    return MEXK_OK;
+}
+
 // Free-standing C entry points: build the schedule on the host from a device
 // row_ptr copy. Meant for tests and one-off products; the solver keeps the
 // schedule resident.

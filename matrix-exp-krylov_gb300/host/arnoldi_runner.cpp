@@ -162,6 +162,7 @@ void ArnoldiRunner::compute_expmv(const std::vector<double>& v_host, std::vector
     p.reorthogonalize = params.reorthogonalize ? 1 : 0;
     p.precision = precision;
     p.controller = controller;
+    p.ortho_window = ortho_window;
     if (controller == MEXK_CTRL_LEARNED && !net_loaded) {
         const std::vector<float> w = load_controller_net();
         const int lrc = mexk_context_set_controller(dc.handle, w.data(), static_cast<int>(w.size()));

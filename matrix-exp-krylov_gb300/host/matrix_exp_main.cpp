@@ -5,7 +5,9 @@
 // tolerance 1e-6, v = 0.1, OUTPUT_Y_FILE dump and summary lines. It runs on
 // one GPU. Extra flags: --precision fp64|mixed (default fp64, the
 // reference's arithmetic), --controller reference|search|learned (default
-// the reference's heuristic) and --quiet (no [STEP]/[FLOPs] lines).
+// the reference's heuristic), --window W (mixed precision, symmetric A:
+// orthogonalise against the last W basis vectors) and --quiet (no
+// [STEP]/[FLOPs] lines).
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -45,6 +47,7 @@ int main(int argc, char* argv[]) {
     double t_cli = 1.0;
     int precision = MEXK_PREC_FP64;
     int controller = MEXK_CTRL_REFERENCE;
+    int window = 0;
     bool quiet = false;
 
     std::vector<std::string> args(argv + 1, argv + argc);
@@ -82,6 +85,10 @@ int main(int argc, char* argv[]) {
                 std::cerr << "Error: --controller must be reference, search or learned" << std::endl;
                 return EXIT_FAILURE;
             }
+            continue;
+        }
+        if (a == "--window" && i + 1 < args.size()) {
+            window = std::atoi(args[++i].c_str());
             continue;
         }
         if (a == "--quiet") {
@@ -188,6 +195,7 @@ int main(int argc, char* argv[]) {
     ArnoldiRunner runner(gpus_used, params, A.rows, A.cols, A.nnz);
     runner.precision = precision;
     runner.controller = controller;
+    runner.ortho_window = window;
     runner.verbose = !quiet;
     runner.init_all_devices(parts, std::vector<int>{0}, ghosts);
     std::vector<double> v(static_cast<size_t>(A.rows), 0.1);

@@ -32,7 +32,8 @@ class MexkError(RuntimeError):
 
 class Params(C.Structure):
     _fields_ = [("m", C.c_int), ("t", C.c_double), ("tol", C.c_double), ("max_restarts", C.c_int),
-                ("reorthogonalize", C.c_int), ("precision", C.c_int), ("controller", C.c_int)]
+                ("reorthogonalize", C.c_int), ("precision", C.c_int), ("controller", C.c_int),
+                ("ortho_window", C.c_int)]
 
 
 class Result(C.Structure):

@@ -25,10 +25,13 @@ CONTROLLERS = {"reference": 0, "search": 1, "learned": 2}
 
 
 def params(m, t, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64",
-           controller="reference") -> Params:
+           controller="reference", window=0) -> Params:
+    """window: 0 = orthogonalise against the whole basis (Arnoldi); W >= 2 =
+    against the last W vectors (mixed precision, symmetric A only)."""
     prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     ctrl = CONTROLLERS[controller] if isinstance(controller, str) else int(controller)
-    return Params(int(m), float(t), float(tol), int(max_restarts), int(bool(reorthogonalize)), prec, ctrl)
+    return Params(int(m), float(t), float(tol), int(max_restarts), int(bool(reorthogonalize)), prec, ctrl,
+                  int(window))
 
 
 class Context:
@@ -91,23 +94,23 @@ class Context:
             self.load_controller()
 
     def expmv(self, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64",
-              controller="reference"):
+              controller="reference", window=0):
         """y = exp(t A) v with host vectors. Returns (y, result dict)."""
         self._ensure_net(controller)
         v = np.ascontiguousarray(v, dtype=np.float64)
         if v.shape != (self.n,):
             raise ValueError("v must have length n")
         y = np.zeros(self.n)
-        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller)
+        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller, window)
         r = Result()
         check(lib().mexk_expmv(self._h, C.byref(p), _ptr(v, C.c_double), _ptr(y, C.c_double), C.byref(r)),
               "mexk_expmv")
         return y, r.as_dict()
 
     def expmv_device(self, v_ptr: int, y_ptr: int, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True,
-                     precision="fp64", stream: int = 0, controller="reference"):
+                     precision="fp64", stream: int = 0, controller="reference", window=0):
         self._ensure_net(controller)
-        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller)
+        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller, window)
         r = Result()
         check(lib().mexk_expmv_device(self._h, C.byref(p), C.c_void_p(v_ptr), C.c_void_p(y_ptr),
                                       C.c_void_p(stream), C.byref(r)), "mexk_expmv_device")

@@ -382,3 +382,42 @@ def test_search_controller_abort_path():
         steps = ctx.steps()
     assert res["converged"] == 0 and res["restarts_done"] == 0
     assert steps[-1][5] == 19 and len(steps) == 19
+
+
+# ------------------------------------------------------------------ short-recurrence window
+@pytest.mark.gpu
+@pytest.mark.parametrize("controller", ["reference", "search"])
+def test_window_on_symmetric_matrix(controller):
+    """Mixed precision, orthogonalisation against the last 2 basis vectors
+    (Lanczos' short recurrence) on symmetric heat matrices: within 1e-6 of
+    the full FP64 Arnoldi result."""
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    for N, t in ((96, 1e-5), (160, 3e-5)):
+        A = S.laplacian_2d(N, h=1.0 / 2049)
+        v = np.random.default_rng(N).uniform(0, 1, A.n)
+        with Context(A, m_alloc=30) as ctx:
+            y64, _ = ctx.expmv(v, t, 30, precision="fp64")
+            y, r = ctx.expmv(v, t, 30, precision="mixed", controller=controller, window=2)
+            assert r["converged"] == 1
+            assert rel(y, y64) <= 1e-6, (N, rel(y, y64))
+
+
+@pytest.mark.gpu
+def test_window_refused_for_nonsymmetric_matrix():
+    from mexk import synthetic as S
+    from mexk._lib import MexkError
+    from mexk.api import Context
+
+    A = S.random_diag_dominant(500, 6, seed=3)
+    v = np.ones(A.n)
+    with Context(A, m_alloc=30) as ctx:
+        with pytest.raises(MexkError, match="symmetric"):
+            ctx.expmv(v, 0.5, 30, precision="mixed", window=2)
+        with pytest.raises(MexkError):
+            ctx.expmv(v, 0.5, 30, precision="fp64", window=2)  # FP64 keeps full Arnoldi
+        with pytest.raises(MexkError):
+            ctx.expmv(v, 0.5, 30, precision="mixed", window=1)
+        y, r = ctx.expmv(v, 0.5, 30, precision="mixed")  # the context stays usable
+        assert r["converged"] == 1
