@@ -84,6 +84,197 @@ __device__ __forceinline__ const float4* col4(const float* V, size_t ldv, int c)
     return reinterpret_cast<const float4*>(V + static_cast<size_t>(c) * ldv);
 }
 
+// Sum over row blocks b < nrb of the partials of nv values, value v in slot
+// slot(v) (layout part[slot * GRAM_MAX_ROW_BLOCKS + b]), into out[v]; all
+// threads of the block call it. FP64 adds and shuffles take about 64 and 100
+// cycles of latency on this GPU (FP32: 4), so the sum is shaped for depth: g2
+// adjacent lanes share a value, each loads up to PR partials in one round and
+// adds them as a tree, then the lanes combine by an xor butterfly (every lane
+// ends with the same bits). The order depends only on nrb and nv.
+template <typename SlotFn>
+__device__ __forceinline__ void sum_partials(const double* part, int nrb, int nv, SlotFn slot, double* out) {
+    constexpr int PR = 12;
+    int g2 = 32;
+    while (g2 > 1 && g2 * nv > GT) g2 >>= 1;
+    const int t = threadIdx.x;
+    const int vi = t / g2, sub = t % g2;
+    double sum = 0.0;
+    if (vi < nv) {
+        const double* P = part + static_cast<size_t>(slot(vi)) * GRAM_MAX_ROW_BLOCKS;
+        for (int b0 = sub; b0 < nrb; b0 += PR * g2) {
+            double v[PR];
+#pragma unroll
+            for (int u = 0; u < PR; ++u) {
+                const int b = b0 + u * g2;
+                v[u] = b < nrb ? __ldcg(P + b) : 0.0;
+            }
+#pragma unroll
+            for (int h = 1; h < PR; h <<= 1)
+#pragma unroll
+                for (int u = 0; u + h < PR; u += 2 * h) v[u] += v[u + h];
+            sum += v[0];
+        }
+    }
+    for (int o = 1; o < g2; o <<= 1) sum += __shfl_xor_sync(FULL, sum, o);
+    if (vi < nv && sub == 0) out[vi] = sum;
+}
+
+// Last block of a grid whose nrb row blocks each wrote their partials of
+// step j (slots: a at column, b at GRAM_BOFF + column, |w|^2 at GRAM_NWOFF):
+// sums them and finishes the step (Gram row, h, H, coefficients, pre-scale).
+// All threads of the block call it. CAP: most columns the step may involve
+// (the staged Gram block is CAP x CAP). Column lo + i is handled by thread i
+// (warp 0, and warp 1 past 32 columns); the scalar chain of the new column
+// runs in warp 7, which has nothing else to do, so that no warp carries two
+// dependent FP64 chains.
+template <int CAP>
+__device__ __noinline__ void gram_finish(const GramArgs& g, int nrb) {
+    static_assert(GW == 8, "the scalar chain runs in warp 7");
+    DevState* st = g.st;
+    const int j = g.j;
+    const int k = j + 1;
+    const int lo = g.lo;
+    const int kw = k - lo;
+    const int jw = j - lo;  // previous columns inside the window
+    __shared__ double s_tot[2 * MEXK_M_MAX + 1];  // a (kw), b (kw), |w|^2
+    __shared__ double s_c[CAP], s_h[CAP], s_sc[CAP], s_y[CAP];
+    __shared__ double s_G[CAP][CAP + 1];  // G(lo:k, lo:k), row-major, padded, indexed from lo
+    __shared__ double s_sj, s_w2s;
+    __shared__ int s_bad;
+    const int t = threadIdx.x;
+    GramState* gs = g.gs;
+    double* G = gs->G;
+    // Stage 1: the previous columns' Gram block and scales, and the partial sums.
+    for (int e = t; e < jw * jw; e += GT) {
+        const int r = e % jw, c = e / jw;
+        s_G[r][c] = G[(lo + r) + static_cast<size_t>(lo + c) * GRAM_LD];
+    }
+    double sc_t = 0.0;
+    if (t < jw) sc_t = gs->s[lo + t];
+    const double ip_j = gs->ip[j];
+    sum_partials(g.part, nrb, 2 * kw + 1,
+                 [&](int v) { return v < kw ? lo + v : (v < 2 * kw ? GRAM_BOFF + lo + (v - kw) : GRAM_NWOFF); },
+                 s_tot);
+    __syncthreads();
+    // Stage 2: warp 7 lane 0: s_j = 1/|u_j| and H(j, j-1) = |u_j| / p_j (the
+    // breakdown test of main.cu:1911); threads i < jw meanwhile scale their
+    // column's b and a by s_i.
+    const size_t ldh = static_cast<size_t>(g.ldh);
+    if (t == GT - 32) {
+        const double bj = s_tot[2 * kw - 1];
+        const bool ok = bj > 0.0 && !isinf(bj);
+        const double sj = ok ? rsqrt(bj) : 0.0;
+        int bad = 0;
+        if (j >= 1) {
+            const double beta = sqrt(bj) * ip_j;
+            bad = !(beta >= 1e-14) || isinf(beta);
+            g.H[j + static_cast<size_t>(j - 1) * ldh] = bad ? 0.0 : beta;
+            if (bad) {
+                st->breakdown = 1;
+                st->k_used = j;
+            }
+        }
+        const double sj2 = sj * sj;
+        gs->s[j] = sj;
+        s_sj = sj;
+        s_w2s = sj2 * s_tot[2 * kw];
+        s_c[jw] = sj2 * s_tot[jw];  // c_j = s_j s_j a_j
+        s_sc[jw] = sj;
+        s_bad = bad;
+    } else if (t < jw) {
+        s_sc[t] = sc_t;
+        s_y[t] = sc_t * s_tot[t];
+        s_tot[kw + t] *= sc_t;  // s_i b_i
+    }
+    __syncthreads();
+    if (s_bad) return;
+    const double sj = s_sj;
+    // Stage 3: the Gram row of column j and c = s s_j a.
+    if (t < jw) {
+        const double gv = s_tot[kw + t] * sj;
+        G[(lo + t) + static_cast<size_t>(j) * GRAM_LD] = gv;
+        G[j + static_cast<size_t>(lo + t) * GRAM_LD] = gv;
+        s_G[t][jw] = gv;
+        s_G[jw][t] = gv;
+        s_c[t] = s_y[t] * sj;
+    } else if (t == jw) {
+        G[j + static_cast<size_t>(j) * GRAM_LD] = 1.0;
+        s_G[jw][jw] = 1.0;
+    }
+    __syncthreads();
+    // Stage 4: h = c - (G - I) c over the window (four running sums), H(:, j)
+    // with zeros outside the window, coefficients s h.
+    if (t < kw) {
+        double hv = s_c[t];
+        if (g.reortho) {
+            double e0 = 0.0, e1 = 0.0, e2 = 0.0, e3 = 0.0;
+            int q = 0;
+            for (; q + 3 < kw; q += 4) {
+                e0 = fma(q == t ? 0.0 : s_G[t][q], s_c[q], e0);
+                e1 = fma(q + 1 == t ? 0.0 : s_G[t][q + 1], s_c[q + 1], e1);
+                e2 = fma(q + 2 == t ? 0.0 : s_G[t][q + 2], s_c[q + 2], e2);
+                e3 = fma(q + 3 == t ? 0.0 : s_G[t][q + 3], s_c[q + 3], e3);
+            }
+            for (; q < kw; ++q) e0 = fma(q == t ? 0.0 : s_G[t][q], s_c[q], e0);
+            hv -= (e0 + e1) + (e2 + e3);
+        }
+        s_h[t] = hv;
+        g.H[(lo + t) + static_cast<size_t>(j) * ldh] = hv;
+        gs->coef[lo + t] = static_cast<float>(s_sc[t] * hv);
+    }
+    for (int r = t; r < lo; r += GT) g.H[r + static_cast<size_t>(j) * ldh] = 0.0;  // outside the window
+    __syncthreads();
+    // Stage 5 (warp 0): |w - V h|^2 = |w|^2 - 2 h.c + h^T G h, the pre-scale p
+    // of the new column and its inverse.
+    if (t < 32) {
+        double part = 0.0;
+        for (int i = t; i < kw; i += 32) {
+            double g0 = 0.0, g1 = 0.0, g2 = 0.0, g3 = 0.0;
+            int q = 0;
+            for (; q + 3 < kw; q += 4) {
+                g0 = fma(s_G[i][q], s_h[q], g0);
+                g1 = fma(s_G[i][q + 1], s_h[q + 1], g1);
+                g2 = fma(s_G[i][q + 2], s_h[q + 2], g2);
+                g3 = fma(s_G[i][q + 3], s_h[q + 3], g3);
+            }
+            for (; q < kw; ++q) g0 = fma(s_G[i][q], s_h[q], g0);
+            part += s_h[i] * (((g0 + g1) + (g2 + g3)) - 2.0 * s_c[i]);
+        }
+        for (int o = 1; o < 32 && o < kw; o <<= 1) part += __shfl_xor_sync(FULL, part, o);
+        if (t == 0) {
+            const double w2 = s_w2s;
+            const double u2 = w2 + part;
+            double p = 1.0, ip = 1.0;
+            if (u2 > 1e-8 * w2 && !isinf(u2)) {
+                p = rsqrt(u2);
+                ip = u2 * p;
+            } else if (w2 > 0.0 && !isinf(w2)) {
+                p = rsqrt(w2);
+                ip = w2 * p;
+            }
+            gs->ip[j + 1] = ip;
+            gs->wsc = static_cast<float>(sj);
+            gs->psc = static_cast<float>(p);
+        }
+    }
+}
+
+// Block stage of a dot sweep: the warps' FP32 totals of NV values (lane l of
+// warp q holds value l in s_red[q][l]) summed over the warps as an FP64
+// tree, then written by thread v to the row block's slot slot(v).
+template <int NV, typename SlotFn>
+__device__ __forceinline__ void write_block_partials(double (&s_red)[GW][NV], double* part, int rb, SlotFn slot) {
+    static_assert(GW == 8, "tree over eight warps");
+    __syncthreads();
+    const int q = threadIdx.x;
+    if (q < NV) {
+        const double t = ((s_red[0][q] + s_red[1][q]) + (s_red[2][q] + s_red[3][q])) +
+                         ((s_red[4][q] + s_red[5][q]) + (s_red[6][q] + s_red[7][q]));
+        const int sl = slot(q);
+        if (sl >= 0) part[static_cast<size_t>(sl) * GRAM_MAX_ROW_BLOCKS + rb] = t;
+    }
+}
+
 // Sweep 1. Block b handles column group b % ngroups (GG columns) over the rows
 // of row block b / ngroups; the groups of one row block are adjacent in launch
 // order, so w and u_j are fetched from DRAM once and re-read from L2.
@@ -127,7 +318,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
     }
     pdl_trigger();
 
-    // block stage: warp butterflies, then the warps in order, in FP64
+    // block stage: warp butterflies in FP32, then the warps in FP64
     __shared__ double s_red[GW][2 * GG + 1];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -139,140 +330,84 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
         s_red[warp][GG + lane] = rbv;
     }
     if (lane == 0) s_red[warp][2 * GG] = rw;
-    __syncthreads();
-    if (threadIdx.x < 2 * GG + 1) {
-        double t = 0.0;
-#pragma unroll
-        for (int q = 0; q < GW; ++q) t += s_red[q][threadIdx.x];
-        double* P = g.part + static_cast<size_t>(rb) * GRAM_STRIDE;
-        const int q = threadIdx.x;
-        if (q < GG) {
-            if (c0 + q < k) P[c0 + q] = t;
-        } else if (q < 2 * GG) {
-            if (c0 + q - GG < k) P[GRAM_BOFF + c0 + q - GG] = t;
-        } else if (grp == 0) {
-            P[GRAM_NWOFF] = t;
-        }
-    }
+    write_block_partials(s_red, g.part, rb, [&](int q) {
+        if (q < GG) return c0 + q < k ? c0 + q : -1;
+        if (q < 2 * GG) return c0 + q - GG < k ? GRAM_BOFF + c0 + q - GG : -1;
+        return grp == 0 ? GRAM_NWOFF : -1;
+    });
 
-    // grid stage: the last block sums the row blocks in order and finishes the step
+    // grid stage: the last block sums the row blocks and finishes the step
     __shared__ int s_flag;
     if (!grid_last_block(g.counter, &s_flag)) return;
-    __shared__ double s_a[MEXK_M_MAX + 1], s_b[MEXK_M_MAX + 1], s_c[MEXK_M_MAX + 1], s_h[MEXK_M_MAX + 1];
-    __shared__ double s_sc[MEXK_M_MAX + 1];
-    __shared__ double s_G[MEXK_M_MAX][MEXK_M_MAX + 1];  // G(0:k, 0:k), row-major, padded
-    __shared__ double s_scr[GT];
-    __shared__ double s_w2, s_sj;
-    __shared__ int s_bad;
-    const int t = threadIdx.x;
-    GramState* gs = g.gs;
-    double* G = gs->G;
-    {
-        // Every load of this stage is independent: the row-block partials
-        // (four running sums per thread, combined in a fixed order), the
-        // previous columns' Gram block and scales.
-        const int nv = 2 * kw + 1;
-        const int groups = GT / nv;
-        const int vi = t % nv;
-        const int gi = t / nv;
-        double sum = 0.0;
-        if (gi < groups) {
-            const int off = vi < kw ? lo + vi : (vi < 2 * kw ? GRAM_BOFF + lo + (vi - kw) : GRAM_NWOFF);
-            const double* P = g.part + off;
-            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-            int b = gi;
-            for (; b + 3 * groups < nrb; b += 4 * groups) {
-                a0 += __ldcg(P + static_cast<size_t>(b) * GRAM_STRIDE);
-                a1 += __ldcg(P + static_cast<size_t>(b + groups) * GRAM_STRIDE);
-                a2 += __ldcg(P + static_cast<size_t>(b + 2 * groups) * GRAM_STRIDE);
-                a3 += __ldcg(P + static_cast<size_t>(b + 3 * groups) * GRAM_STRIDE);
-            }
-            for (; b < nrb; b += groups) a0 += __ldcg(P + static_cast<size_t>(b) * GRAM_STRIDE);
-            sum = (a0 + a1) + (a2 + a3);
+    gram_finish<MEXK_M_MAX>(g, nrb);
+}
+
+// Sweep 1 for a step over at most two columns (the first two Arnoldi steps,
+// every step of a window of 2): w, u_j and u_{j-1} are each read once, two
+// rows per thread per iteration, one column group, and the grid is sized so
+// that the finish sums a few hundred partials in one round of loads.
+__global__ void __launch_bounds__(GT, 4) gram_dot2_kernel(GramArgs g) {
+    pdl_wait();
+    DevState* st = g.st;
+    if (st->breakdown || st->done) return;
+    const int j = g.j;
+    const int lo = g.lo;  // j - 1 or j
+    const bool two = lo < j;
+    const size_t ldv = static_cast<size_t>(g.ldv);
+    const float4* __restrict__ w4 = reinterpret_cast<const float4*>(g.w);
+    const float4* __restrict__ u4 = col4(g.V, ldv, j);
+    const float4* __restrict__ p4 = col4(g.V, ldv, two ? j - 1 : j);
+    // acc: a_{j-1}, a_j, b_{j-1}, b_j, |w|^2
+    float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    const int n4 = (g.n + 3) / 4;
+    const int stride = gridDim.x * GT;
+    int i = blockIdx.x * GT + threadIdx.x;
+    for (; i + stride < n4; i += 2 * stride) {
+        const float4 x0 = __ldcs(w4 + i), x1 = __ldcs(w4 + i + stride);
+        const float4 u0 = __ldcs(u4 + i), u1 = __ldcs(u4 + i + stride);
+        float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+        if (two) {
+            v0 = __ldcs(p4 + i);
+            v1 = __ldcs(p4 + i + stride);
         }
-        const int jw = j - lo;  // previous columns inside the window
-        for (int e = t; e < jw * jw; e += GT) {
-            const int r = lo + e % jw, c = lo + e / jw;
-            s_G[r][c] = G[r + static_cast<size_t>(c) * GRAM_LD];
+        acc[0] += dot4(v0, x0) + dot4(v1, x1);
+        acc[1] += dot4(u0, x0) + dot4(u1, x1);
+        acc[2] += dot4(v0, u0) + dot4(v1, u1);
+        acc[3] += dot4(u0, u0) + dot4(u1, u1);
+        acc[4] += dot4(x0, x0) + dot4(x1, x1);
+    }
+    if (i < n4) {
+        const float4 x0 = __ldcs(w4 + i);
+        const float4 u0 = __ldcs(u4 + i);
+        const float4 v0 = two ? __ldcs(p4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        acc[0] += dot4(v0, x0);
+        acc[1] += dot4(u0, x0);
+        acc[2] += dot4(v0, u0);
+        acc[3] += dot4(u0, u0);
+        acc[4] += dot4(x0, x0);
+    }
+    pdl_trigger();
+
+    __shared__ double s_red[GW][5];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const float r = warp_sum(acc[q]);
+        if (lane == 0) s_red[warp][q] = r;
+    }
+    write_block_partials(s_red, g.part, blockIdx.x, [&](int q) {
+        switch (q) {
+            case 0: return two ? j - 1 : -1;
+            case 1: return j;
+            case 2: return two ? GRAM_BOFF + j - 1 : -1;
+            case 3: return GRAM_BOFF + j;
+            default: return GRAM_NWOFF;
         }
-        if (t >= lo && t < j) s_sc[t] = gs->s[t];
-        s_scr[t] = sum;
-        __syncthreads();
-        if (t < nv) {
-            double tot = 0.0;
-            for (int q = 0; q < groups; ++q) tot += s_scr[q * nv + t];
-            if (t < kw) s_a[lo + t] = tot;
-            else if (t < 2 * kw) s_b[lo + t - kw] = tot;
-            else s_w2 = tot;
-        }
-        __syncthreads();
-    }
-    const size_t ldh = static_cast<size_t>(g.ldh);
-    if (t == 0) {
-        const double bj = s_b[j];
-        int bad = 0;
-        if (j >= 1) {
-            // the previous step's h_{j,j-1} = |u_j| / p_j; breakdown test as main.cu:1911
-            const double beta = sqrt(bj) / gs->p[j];
-            bad = !(beta >= 1e-14) || isinf(beta);
-            g.H[j + static_cast<size_t>(j - 1) * ldh] = bad ? 0.0 : beta;
-            if (bad) {
-                st->breakdown = 1;
-                st->k_used = j;
-            }
-        }
-        const double sj = (bj > 0.0 && !isinf(bj)) ? 1.0 / sqrt(bj) : 0.0;
-        gs->s[j] = sj;
-        s_sc[j] = sj;
-        s_sj = sj;
-        s_bad = bad;
-    }
-    __syncthreads();
-    if (s_bad) return;
-    const double sj = s_sj;
-    if (t >= lo && t < k) {
-        const double sc = s_sc[t];
-        const double gv = (t == j) ? 1.0 : sc * sj * s_b[t];
-        G[t + static_cast<size_t>(j) * GRAM_LD] = gv;
-        G[j + static_cast<size_t>(t) * GRAM_LD] = gv;
-        s_G[t][j] = gv;
-        s_G[j][t] = gv;
-        s_c[t] = sc * sj * s_a[t];
-    }
-    __syncthreads();
-    if (t < lo) {
-        g.H[t + static_cast<size_t>(j) * ldh] = 0.0;  // outside the window
-    } else if (t < k) {
-        double hv = s_c[t];
-        if (g.reortho) {
-            double e = 0.0;
-            for (int q = lo; q < k; ++q)
-                if (q != t) e = fma(s_G[t][q], s_c[q], e);
-            hv -= e;
-        }
-        s_h[t] = hv;
-        g.H[t + static_cast<size_t>(j) * ldh] = hv;
-        gs->coef[t] = static_cast<float>(s_sc[t] * hv);
-    }
-    __syncthreads();
-    // |w - V h|^2 = |w|^2 - 2 h.c + h^T G h  (pre-scale of the new column)
-    double part = 0.0;
-    if (t >= lo && t < k) {
-        double gh = 0.0;
-        for (int q = lo; q < k; ++q) gh = fma(s_G[t][q], s_h[q], gh);
-        part = s_h[t] * gh - 2.0 * s_h[t] * s_c[t];
-    }
-    part = block_sum(part, s_scr);
-    if (t == 0) {
-        const double w2 = sj * sj * s_w2;
-        const double u2 = w2 + part;
-        double p = 1.0;
-        if (u2 > 1e-8 * w2 && !isinf(u2)) p = 1.0 / sqrt(u2);
-        else if (w2 > 0.0 && !isinf(w2)) p = 1.0 / sqrt(w2);
-        gs->p[j + 1] = p;
-        gs->wsc = static_cast<float>(sj);
-        gs->psc = static_cast<float>(p);
-    }
+    });
+    __shared__ int s_flag;
+    if (!grid_last_block(g.counter, &s_flag)) return;
+    gram_finish<2>(g, gridDim.x);
 }
 
 // Sweep 2: u_{j+1} = psc * (wsc * w - sum_c coef_c u_c), written to column
@@ -342,22 +477,22 @@ __global__ void __launch_bounds__(GT) gram_norm_kernel(GramArgs g) {
         const float4 u = __ldg(u4 + i);
         acc += dot4(u, u);
     }
-    __shared__ double s_scr[GT];
-    const double bsum = block_sum(static_cast<double>(acc), s_scr);
-    if (threadIdx.x == 0) g.part[static_cast<size_t>(blockIdx.x) * GRAM_STRIDE] = bsum;
+    __shared__ double s_red[GW][1];
+    const float r = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5][0] = r;
+    write_block_partials(s_red, g.part, blockIdx.x, [](int) { return 0; });
     __shared__ int s_flag;
     if (!grid_last_block(g.counter, &s_flag)) return;
-    double tsum = 0.0;
-    for (int b = threadIdx.x; b < static_cast<int>(gridDim.x); b += GT)
-        tsum += __ldcg(&g.part[static_cast<size_t>(b) * GRAM_STRIDE]);
-    const double total = block_sum(tsum, s_scr);
+    __shared__ double s_tot[1];
+    sum_partials(g.part, gridDim.x, 1, [](int) { return 0; }, s_tot);
+    __syncthreads();
     if (threadIdx.x == 0) {
         GramState* gs = g.gs;
-        const double b = total;
-        const double beta = sqrt(b) / gs->p[jn];
+        const double b = s_tot[0];
+        const double beta = sqrt(b) * gs->ip[jn];
         const bool bad = !(beta >= 1e-14) || isinf(beta);
         if (jn < g.ldh) g.H[jn + static_cast<size_t>(g.j) * g.ldh] = bad ? 0.0 : beta;
-        gs->s[jn] = (b > 0.0 && !isinf(b)) ? 1.0 / sqrt(b) : 0.0;
+        gs->s[jn] = (b > 0.0 && !isinf(b)) ? rsqrt(b) : 0.0;
         gs->G[jn + static_cast<size_t>(jn) * GRAM_LD] = 1.0;
         if (bad) {
             st->breakdown = 1;
@@ -391,12 +526,20 @@ int device_sm_count() {
 int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
     if (a.j < 0 || a.j >= MEXK_M_MAX) return MEXK_ERR_INVALID;
     if (a.lo < 0 || a.lo > a.j) return MEXK_ERR_INVALID;
-    const int ngroups = (a.j + 1 - a.lo + GG - 1) / GG;
-    // One wave of 4 resident blocks per SM over all column groups (a partial
-    // second wave would run at half occupancy); 2 row blocks per SM at most.
-    int nrb = row_blocks(a.n, 2);
-    if (ngroups > 2) nrb = std::min(nrb, std::max(1, 4 * device_sm_count() / ngroups));
-    const cudaError_t e = launch_dependent(gram_dot_kernel, nrb * ngroups, GT, 0, s, a);
+    const int kw = a.j + 1 - a.lo;
+    cudaError_t e;
+    if (kw <= 2) {
+        // two rows per thread per iteration: 2 row blocks per SM keep ~100 bytes
+        // per thread in flight
+        e = launch_dependent(gram_dot2_kernel, row_blocks((a.n + 1) / 2, 2), GT, 0, s, a);
+    } else {
+        const int ngroups = (kw + GG - 1) / GG;
+        // One wave of 4 resident blocks per SM over all column groups (a partial
+        // second wave would run at half occupancy); 2 row blocks per SM at most.
+        int nrb = row_blocks(a.n, 2);
+        if (ngroups > 2) nrb = std::min(nrb, std::max(1, 4 * device_sm_count() / ngroups));
+        e = launch_dependent(gram_dot_kernel, nrb * ngroups, GT, 0, s, a);
+    }
     if (e != cudaSuccess) {
         set_cuda_error(e, "gram_dot_kernel", __FILE__, __LINE__);
         return MEXK_ERR_CUDA;

@@ -299,14 +299,14 @@ int launch_normalize(int n, int j, int ldv, const TV* w, TV* V, const DevState* 
 // ------------------------------------------------------------ Gram-corrected sweeps (FP32 basis)
 // Column c of the FP32 basis stores u_c; the basis vector is v_c = s[c] * u_c.
 constexpr int GRAM_LD = MEXK_M_MAX + 1;         // leading dimension of G
-constexpr int GRAM_STRIDE = 2 * MEXK_M_MAX + 8; // doubles per row-block partial
-constexpr int GRAM_BOFF = MEXK_M_MAX;           // partial slots: a [0,64), b [64,128), |w|^2 128
+constexpr int GRAM_SLOTS = 2 * MEXK_M_MAX + 8;  // partial slots: a [0,64), b [64,128), |w|^2 128
+constexpr int GRAM_BOFF = MEXK_M_MAX;
 constexpr int GRAM_NWOFF = 2 * MEXK_M_MAX;
 constexpr int GRAM_MAX_ROW_BLOCKS = 1024;
 struct GramState {
     double G[GRAM_LD * GRAM_LD];  // Gram matrix V^T V (unit diagonal), column-major
     double s[MEXK_M_MAX + 2];     // column scales 1/|u_c|
-    double p[MEXK_M_MAX + 2];     // pre-scale applied when column c was written
+    double ip[MEXK_M_MAX + 2];    // 1 / (pre-scale applied when column c was written)
     float coef[MEXK_M_MAX + 8];   // update coefficients s_c h_c of the current step
     float wsc, psc;               // update: u_{j+1} = psc * (wsc * w - sum coef_c u_c)
 };
@@ -317,7 +317,7 @@ struct GramArgs {
     const float* w;    // A u_j (unscaled), rows n..ldv-1 zero
     double* H;
     GramState* gs;
-    double* part;      // GRAM_MAX_ROW_BLOCKS x GRAM_STRIDE
+    double* part;      // GRAM_SLOTS x GRAM_MAX_ROW_BLOCKS: slot v of row block b at v * GRAM_MAX_ROW_BLOCKS + b
     unsigned int* counter;
     DevState* st;
 };

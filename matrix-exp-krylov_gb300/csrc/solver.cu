@@ -185,7 +185,7 @@ int reset_gram(mexk_context_t ctx, cudaStream_t s) {
     if (!init) {
         memset(&h0, 0, sizeof(h0));
         for (int i = 0; i < GRAM_LD; ++i) h0.G[i + i * GRAM_LD] = 1.0;
-        for (int i = 0; i < MEXK_M_MAX + 2; ++i) h0.s[i] = h0.p[i] = 1.0;
+        for (int i = 0; i < MEXK_M_MAX + 2; ++i) h0.s[i] = h0.ip[i] = 1.0;
         h0.wsc = h0.psc = 1.0f;
         init = true;
     }
@@ -203,7 +203,7 @@ int ensure_mixed(mexk_context_t ctx) {
     MEXK_CK(cudaMemset(ctx->d_V32, 0, sizeof(float) * static_cast<size_t>(ctx->ldv) * (ctx->m_alloc + 1)));
     MEXK_CK(cudaMemset(ctx->d_w32, 0, sizeof(float) * static_cast<size_t>(ctx->ldv)));
     if ((rc = dalloc(&ctx->d_gram, 1))) return rc;
-    if ((rc = dalloc(&ctx->d_gram_part, static_cast<size_t>(GRAM_MAX_ROW_BLOCKS) * GRAM_STRIDE))) return rc;
+    if ((rc = dalloc(&ctx->d_gram_part, static_cast<size_t>(GRAM_MAX_ROW_BLOCKS) * GRAM_SLOTS))) return rc;
     if ((rc = reset_gram(ctx, ctx->stream))) return rc;
     if ((rc = dalloc(&ctx->d_val32, static_cast<size_t>(ctx->nnz) + 4))) return rc;
     if ((rc = launch_narrow_values(ctx->d_val, ctx->d_val32, static_cast<size_t>(ctx->nnz), ctx->stream))) return rc;
