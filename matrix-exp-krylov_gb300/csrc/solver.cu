@@ -15,7 +15,7 @@
 // HBM layout per context (n rows, m_alloc maximum Krylov dimension):
 //   CSR        row_ptr int32[n+1], col_idx int32[nnz], values f64[nnz]
 //              (+ f32 copy of values for the mixed-precision form)
-//   row blocks int32[nblocks+1] SpMV schedule
+//   row blocks int2[nblocks+1] SpMV schedule {first row, first nonzero}
 //   basis V    column-major, leading dimension ldv = n rounded up to 64,
 //              m_alloc+1 columns, f64 (+ f32 basis for the mixed form, whose
 //              columns carry f64 scales, with the Gram matrix, in GramState)
@@ -73,7 +73,7 @@ struct mexk_context_s {
     int* d_col = nullptr;
     double* d_val = nullptr;
     float* d_val32 = nullptr;
-    int* d_blocks = nullptr;
+    int2* d_tiles = nullptr;
     double* d_V = nullptr;
     float* d_V32 = nullptr;
     double* d_w = nullptr;
@@ -271,18 +271,18 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
     const size_t ldv = static_cast<size_t>(ctx->ldv);
     int rc;
     if (fp32) {
-        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
+        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_row_ptr, ctx->d_col,
                                             ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32,
-                                            &ctx->d_state->breakdown, s, true)))
+                                            &ctx->d_state->breakdown, &ctx->d_state->status, s)))
             return rc;
         GramArgs g = gram_args(ctx, j, reortho);
         g.lo = window > 0 ? std::max(0, j + 1 - window) : 0;
         if ((rc = launch_gram_dot(g, s))) return rc;
         return launch_gram_update(g, s);
     }
-    if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
-                                          ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, &ctx->d_state->breakdown, s,
-                                          true)))
+    if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_row_ptr, ctx->d_col,
+                                          ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, &ctx->d_state->breakdown,
+                                          &ctx->d_state->status, s)))
         return rc;
     const GsArgs g = gs_args(ctx, j, reortho, false);
     const int grid = gs_grid_size(ctx->n, j + 1);
@@ -552,18 +552,20 @@ int mexk_context_upload_csr(mexk_context_t ctx, int rows, long long nnz, const i
     ctx->ldv = (rows + 63) / 64 * 64;
     ctx->ldh = m_alloc_max + 1;
     int rc;
-    if ((rc = dalloc(&ctx->d_row_ptr, rows + 1))) return rc;
+    if ((rc = dalloc(&ctx->d_row_ptr, static_cast<size_t>(rows) + 8))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_row_ptr, 0, sizeof(int) * (static_cast<size_t>(rows) + 8)));
     if ((rc = dalloc(&ctx->d_col, static_cast<size_t>(nnz) + 4))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_col + nnz, 0, sizeof(int) * 4));  // the SpMV gathers whole 16-byte groups
     if ((rc = dalloc(&ctx->d_val, static_cast<size_t>(nnz) + 4))) return rc;
     MEXK_CK(cudaMemcpy(ctx->d_row_ptr, row_ptr, sizeof(int) * (rows + 1), cudaMemcpyHostToDevice));
     if (nnz > 0) {
         MEXK_CK(cudaMemcpy(ctx->d_col, col_idx, sizeof(int) * nnz, cudaMemcpyHostToDevice));
         MEXK_CK(cudaMemcpy(ctx->d_val, values, sizeof(double) * nnz, cudaMemcpyHostToDevice));
     }
-    std::vector<int> blocks = build_row_blocks(rows, row_ptr);
-    ctx->nblocks = static_cast<int>(blocks.size()) - 1;
-    if ((rc = dalloc(&ctx->d_blocks, blocks.size()))) return rc;
-    MEXK_CK(cudaMemcpy(ctx->d_blocks, blocks.data(), sizeof(int) * blocks.size(), cudaMemcpyHostToDevice));
+    std::vector<int2> tiles = build_row_tiles(rows, row_ptr);
+    ctx->nblocks = static_cast<int>(tiles.size()) - 1;
+    if ((rc = dalloc(&ctx->d_tiles, tiles.size()))) return rc;
+    MEXK_CK(cudaMemcpy(ctx->d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice));
     const size_t vcount = static_cast<size_t>(ctx->ldv) * (m_alloc_max + 1);
     if ((rc = dalloc(&ctx->d_V, vcount))) return rc;
     MEXK_CK(cudaMemset(ctx->d_V, 0, sizeof(double) * vcount));
@@ -603,7 +605,7 @@ int mexk_context_destroy(mexk_context_t ctx) {
     dfree(ctx->d_col);
     dfree(ctx->d_val);
     dfree(ctx->d_val32);
-    dfree(ctx->d_blocks);
+    dfree(ctx->d_tiles);
     dfree(ctx->d_V);
     dfree(ctx->d_V32);
     dfree(ctx->d_w);
@@ -886,12 +888,12 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
         }
         switch (kind) {
             case MEXK_KERNEL_SPMV:
-                rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr, ctx->d_col,
-                                                      ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr, s,
-                                                      true)
-                          : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_blocks, ctx->d_row_ptr,
+                rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_row_ptr, ctx->d_col,
+                                                      ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr,
+                                                      &ctx->d_state->status, s)
+                          : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_row_ptr,
                                                         ctx->d_col, ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, nullptr,
-                                                        s, true);
+                                                        &ctx->d_state->status, s);
                 break;
             case MEXK_KERNEL_GS_DOT:
             case MEXK_KERNEL_GS_UPD_DOT:

@@ -7,7 +7,12 @@
 // contiguous range of values and column indices with coalesced loads,
 // whatever the row-length distribution (Laplacian stencils, Zipf rows).
 // Phase 1 multiplies value * x[col] into shared memory; phase 2 sums each
-// row's products. Rows of at most SEQ_ROW_MAX nonzeros are summed in column
+// row's products. In a context (padded, aligned arrays) each thread block is
+// persistent over a contiguous range of row blocks and double-buffers them:
+// while it multiplies and sums one row block, the bulk-copy engine (TMA,
+// cp.async.bulk) brings the next one's column indices, values and row
+// pointers into shared memory, so the matrix stream never waits on the
+// gather -> sum chain of a row block. Rows of at most SEQ_ROW_MAX nonzeros are summed in column
 // order by one thread, so their FP64 result equals the reference's serial
 // loop (main_cpu.cpp:388-397) bit for bit: one rounded product per nonzero,
 // added left to right. Longer rows (the power-law tails) are summed by one
@@ -18,7 +23,7 @@
 
 namespace mexk {
 
-std::vector<int> build_row_blocks(int n, const int* row_ptr) {
+std::vector<int> build_row_blocks(int n, const int* row_ptr, int tile, int tile_rows) {
     std::vector<int> blocks;
     blocks.reserve(static_cast<size_t>(n) / 64 + 2);
     blocks.push_back(0);
@@ -26,13 +31,13 @@ std::vector<int> build_row_blocks(int n, const int* row_ptr) {
     while (r < n) {
         const int start = r;
         const long long len0 = static_cast<long long>(row_ptr[r + 1]) - row_ptr[r];
-        if (len0 > SPMV_TILE) {
+        if (len0 > tile) {
             ++r;
         } else {
             long long acc = 0;
-            while (r < n && r - start < SPMV_TILE_ROWS) {
+            while (r < n && r - start < tile_rows) {
                 const long long len = static_cast<long long>(row_ptr[r + 1]) - row_ptr[r];
-                if (acc + len > SPMV_TILE) break;
+                if (acc + len > tile) break;
                 acc += len;
                 ++r;
             }
@@ -53,50 +58,17 @@ struct AccType<float> {
     using type = float;
 };
 
-// Four consecutive values starting at a 16-byte boundary.
-template <typename TA>
-struct Quad;
-template <>
-struct Quad<float> {
-    static __device__ __forceinline__ void ld(const float* p, float (&o)[4]) {
-        const float4 t = __ldcs(reinterpret_cast<const float4*>(p));
-        o[0] = t.x;
-        o[1] = t.y;
-        o[2] = t.z;
-        o[3] = t.w;
-    }
-};
-template <>
-struct Quad<double> {
-    static __device__ __forceinline__ void ld(const double* p, double (&o)[4]) {
-        const double2 t0 = __ldcs(reinterpret_cast<const double2*>(p));
-        const double2 t1 = __ldcs(reinterpret_cast<const double2*>(p) + 1);
-        o[0] = t0.x;
-        o[1] = t0.y;
-        o[2] = t1.x;
-        o[3] = t1.y;
-    }
-};
-
-// Groups of 4 nonzeros one thread covers in a tile (the tile's span, widened
-// down to a multiple of 4, has at most SPMV_TILE + 3 entries).
-constexpr int SPMV_QUADS = ((SPMV_TILE + 3 + 3) / 4 + SPMV_THREADS - 1) / SPMV_THREADS;
-
-// VEC: values and column indices are 16-byte aligned arrays padded by at
-// least 3 entries past nnz, so whole aligned groups of 4 may be loaded; every
-// thread issues all its column/value loads, then all its x gathers.
-template <typename TA, typename TX, bool VEC>
+// Free-standing form (any alignment): one row block per thread block.
+template <typename TA, typename TX>
 __global__ void __launch_bounds__(SPMV_THREADS)
     spmv_rowblock_kernel(int nblocks, const int* __restrict__ blocks, const int* __restrict__ row_ptr,
                          const int* __restrict__ col_idx, const TA* __restrict__ values,
-                         const TX* __restrict__ x, TX* __restrict__ y, const int* __restrict__ skip) {
+                         const TX* __restrict__ x, TX* __restrict__ y) {
     using TP = typename AccType<TX>::type;
     __shared__ TP prod[SPMV_TILE];
     __shared__ TP red[32];
     __shared__ int s_long[SPMV_TILE / (SEQ_ROW_MAX + 1) + 1];
     __shared__ int s_nlong;
-    pdl_wait();
-    if (skip != nullptr && *skip) return;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     for (int b = blockIdx.x; b < nblocks; b += gridDim.x) {
@@ -127,44 +99,11 @@ __global__ void __launch_bounds__(SPMV_THREADS)
             rz[q] = r < r1 ? row_ptr[r + 1] : 0;
         }
         // Phase 1: coalesced stream of (value, column) pairs.
-        if constexpr (VEC) {
-            const int base = e0 & ~3;
-            const int nq = (e1 - base + 3) >> 2;
-            int4 cq[SPMV_QUADS];
-            TA aq[SPMV_QUADS][4];
-#pragma unroll
-            for (int q = 0; q < SPMV_QUADS; ++q) {
-                const int g = tid + q * SPMV_THREADS;
-                if (g < nq) {
-                    cq[q] = __ldcs(reinterpret_cast<const int4*>(col_idx + base) + g);
-                    Quad<TA>::ld(values + base + 4 * g, aq[q]);
-                }
-            }
-            TP xq[SPMV_QUADS][4];
-#pragma unroll
-            for (int q = 0; q < SPMV_QUADS; ++q) {
-                const int g = tid + q * SPMV_THREADS;
-                const int e = base + 4 * g;
-                const int c4[4] = {cq[q].x, cq[q].y, cq[q].z, cq[q].w};
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    xq[q][i] = (g < nq && e + i >= e0 && e + i < e1) ? static_cast<TP>(__ldg(&x[c4[i]])) : TP(0);
-            }
-#pragma unroll
-            for (int q = 0; q < SPMV_QUADS; ++q) {
-                const int g = tid + q * SPMV_THREADS;
-                const int e = base + 4 * g;
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    if (g < nq && e + i >= e0 && e + i < e1) prod[e + i - e0] = static_cast<TP>(aq[q][i]) * xq[q][i];
-            }
-        } else {
 #pragma unroll 4
-            for (int e = tid; e < cnt; e += SPMV_THREADS) {
-                const int c = __ldcs(&col_idx[e0 + e]);
-                const TA a = __ldcs(&values[e0 + e]);
-                prod[e] = static_cast<TP>(a) * static_cast<TP>(__ldg(&x[c]));
-            }
+        for (int e = tid; e < cnt; e += SPMV_THREADS) {
+            const int c = __ldcs(&col_idx[e0 + e]);
+            const TA a = __ldcs(&values[e0 + e]);
+            prod[e] = static_cast<TP>(a) * static_cast<TP>(__ldg(&x[c]));
         }
         __syncthreads();
         // Phase 2: rows of at most SEQ_ROW_MAX nonzeros are summed left to
@@ -184,7 +123,6 @@ __global__ void __launch_bounds__(SPMV_THREADS)
             }
         }
         __syncthreads();
-        if (b + static_cast<int>(gridDim.x) >= nblocks) pdl_trigger();  // this block's last row block
         // Each lane sums its strided share in order, then a fixed butterfly:
         // the result does not depend on which warp takes the row.
         for (int i = tid >> 5; i < s_nlong; i += SPMV_THREADS / 32) {
@@ -200,34 +138,316 @@ __global__ void __launch_bounds__(SPMV_THREADS)
     }
 }
 
+// ------------------------------------------------------------ bulk-copy staging
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// One arrival (the issuing thread's) plus `bytes` of transaction count.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                     smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// L2 policy for data read once: evicted first, so that streaming the matrix
+// does not push the basis vectors the next kernels read out of L2.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+// Global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+// completing on `bar`.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                              uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+        "%4;" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Orders this thread's earlier shared-memory accesses before later bulk copies.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait for the phase of `bar` with the given parity: false after
+// about a second (the copies did not complete).
+__device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_ns() - t0 > 1000000000ull) return false;
+    return true;
+}
+
+// Shape of the context SpMV: threads per block, most nonzeros and rows per
+// row block, shared-memory buffers per block, resident blocks per SM the
+// register budget is set for.
+constexpr int ST_THREADS = 256;
+constexpr int ST_TILE = 2048;
+constexpr int ST_ROWS = 512;
+constexpr int ST_STAGES = 2;
+constexpr int ST_MINB = 5;
+
+// Shared-memory image of one row block: the 16-byte groups of column indices
+// and values its nonzeros span, then row_ptr from its first row rounded down
+// to a multiple of 4 through its end row.
+template <typename TA>
+struct TileStage {
+    static constexpr int QMAX = (ST_TILE + 6) / 4;  // groups of 4 a row block spans
+    static constexpr int COL = QMAX * 16;
+    static constexpr int VAL = QMAX * 4 * static_cast<int>(sizeof(TA));
+    static constexpr int RP = (ST_ROWS + 4 + 3) / 4 * 16;
+    static constexpr int BYTES = COL + VAL + RP;
+    static_assert(COL % 16 == 0 && VAL % 16 == 0 && RP % 16 == 0, "bulk copies need 16-byte pieces");
+};
+constexpr int ST_QUADS = (TileStage<float>::QMAX + ST_THREADS - 1) / ST_THREADS;
+constexpr int ST_RPT = (ST_ROWS + ST_THREADS - 1) / ST_THREADS;
+
+template <typename TA, typename TP>
+__device__ __forceinline__ void smem_quad(const TA* p, TP (&o)[4]);
+template <>
+__device__ __forceinline__ void smem_quad<float, float>(const float* p, float (&o)[4]) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    o[0] = t.x;
+    o[1] = t.y;
+    o[2] = t.z;
+    o[3] = t.w;
+}
+template <>
+__device__ __forceinline__ void smem_quad<double, double>(const double* p, double (&o)[4]) {
+    const double2 t0 = reinterpret_cast<const double2*>(p)[0];
+    const double2 t1 = reinterpret_cast<const double2*>(p)[1];
+    o[0] = t0.x;
+    o[1] = t0.y;
+    o[2] = t1.x;
+    o[3] = t1.y;
+}
+
+std::vector<int2> build_row_tiles(int n, const int* row_ptr) {
+    const std::vector<int> blocks = build_row_blocks(n, row_ptr, ST_TILE, ST_ROWS);
+    std::vector<int2> tiles(blocks.size());
+    for (size_t b = 0; b < blocks.size(); ++b) tiles[b] = make_int2(blocks[b], row_ptr[blocks[b]]);
+    return tiles;
+}
+
+// Context form. tiles[b] = {first row, first nonzero} of row block b (b <=
+// nblocks); col_idx/values 16-byte aligned with >= 3 entries past nnz, the
+// column indices there zero; row_ptr with >= n + 4 entries. Thread block g
+// takes row blocks [t0, t1) through ST_STAGES buffers: thread 0 issues the
+// bulk copies of row block i + ST_STAGES - 1 once every thread has finished
+// row block i - 1 (whose buffer it reuses). Every staged 16-byte group is
+// multiplied whole (its column indices are all valid, those outside the row
+// block included), the products overwrite the staged values, and the row
+// sums read only the row block's own. Row blocks of one long row are not
+// staged: the block streams them directly.
 template <typename TA, typename TX>
-int launch_spmv(int n, int nblocks, const int* blocks, const int* row_ptr, const int* col_idx,
-                const TA* values, const TX* x, TX* y, const int* skip_flag, cudaStream_t s, bool padded) {
+__global__ void __launch_bounds__(ST_THREADS, ST_MINB)
+    spmv_stream_kernel(int nblocks, const int2* __restrict__ tiles, const int* __restrict__ row_ptr,
+                       const int* __restrict__ col_idx, const TA* __restrict__ values, const TX* __restrict__ x,
+                       TX* __restrict__ y, const int* __restrict__ skip, int* __restrict__ status) {
+    using TP = typename AccType<TX>::type;
+    using SL = TileStage<TA>;
+    constexpr int S = ST_STAGES;
+    static_assert(sizeof(TA) == sizeof(TP), "products overwrite the staged values");
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar[S];
+    __shared__ TP red[32];
+    __shared__ int s_long[ST_TILE / (SEQ_ROW_MAX + 1) + 1];
+    __shared__ int s_nlong;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int g = blockIdx.x, G = gridDim.x;
+    const int per = nblocks / G, extra = nblocks % G;
+    const int t0 = g * per + (g < extra ? g : extra);
+    const int t1 = t0 + per + (g < extra ? 1 : 0);
+    auto staged = [&](int i) { return tiles[i + 1].y - tiles[i].y <= ST_TILE; };
+    auto issue = [&](int i, uint64_t pol) {  // thread 0
+        const int2 a = tiles[i], b = tiles[i + 1];
+        if (b.y - a.y > ST_TILE) return;
+        const int s = (i - t0) % S;
+        unsigned char* st = smem + s * SL::BYTES;
+        const int base = a.y & ~3;
+        const uint32_t nq = static_cast<uint32_t>((b.y - base + 3) >> 2);
+        const int rbase = a.x & ~3;
+        const uint32_t nrp = static_cast<uint32_t>((b.x + 1 - rbase + 3) & ~3);
+        const uint32_t bc = nq * 16u, bv = nq * 4u * static_cast<uint32_t>(sizeof(TA)), br = nrp * 4u;
+        mbar_arrive_expect_tx(&bar[s], bc + bv + br);
+        if (nq > 0) {
+            bulk_copy_g2s(st, col_idx + base, bc, &bar[s], pol);
+            bulk_copy_g2s(st + SL::COL, values + base, bv, &bar[s], pol);
+        }
+        bulk_copy_g2s(st + SL::COL + SL::VAL, row_ptr + rbase, br, &bar[s], pol);
+    };
+    uint64_t pol = 0;
+    if (tid == 0) {
+        pol = l2_evict_first_policy();
+        for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
+        mbar_init_fence();
+        // The matrix is never written by a kernel: its first row blocks are
+        // requested before waiting for the previous kernel of the stream.
+        for (int i = t0; i < t1 && i < t0 + S - 1; ++i) issue(i, pol);
+    }
+    __syncthreads();
+    pdl_wait();
+    const bool skipped = __syncthreads_or(skip != nullptr && *skip) != 0;
+    unsigned phase = 0;  // bit s: parity of the next completion of buffer s
+    int i = t0;
+    bool fail = false;
+    for (; i < t1 && !skipped; ++i) {
+        const bool st_i = staged(i);
+        const int sb = (i - t0) % S;
+        bool ok = true;
+        if (st_i) ok = mbar_wait(&bar[sb], (phase >> sb) & 1u);
+        // also: every thread has finished row block i - 1
+        if (__syncthreads_or(!ok)) {
+            fail = true;
+            break;
+        }
+        if (st_i) phase ^= 1u << sb;
+        if (tid == 0 && i + S - 1 < t1) issue(i + S - 1, pol);
+        if (i == t1 - 1) pdl_trigger();  // this block's last row block
+        const int2 ta = tiles[i], tb = tiles[i + 1];
+        const int r0 = ta.x, r1 = tb.x, e0 = ta.y, e1 = tb.y;
+        if (!st_i) {
+            // One long row: the block splits its nonzeros, then a tree sum.
+            TP s = 0;
+            for (int e = e0 + tid; e < e1; e += ST_THREADS)
+                s += static_cast<TP>(__ldcs(&values[e])) * static_cast<TP>(__ldg(&x[__ldcs(&col_idx[e])]));
+            s = block_sum(s, red);
+            if (tid == 0) y[r0] = static_cast<TX>(s);
+            continue;
+        }
+        unsigned char* st = smem + sb * SL::BYTES;
+        const int4* sc = reinterpret_cast<const int4*>(st);
+        TP* sv = reinterpret_cast<TP*>(st + SL::COL);  // values, then products (entry e at e - base)
+        const int* srp = reinterpret_cast<const int*>(st + SL::COL + SL::VAL);
+        const int base = e0 & ~3;
+        const int nq = (e1 - base + 3) >> 2;
+        const int rbase = r0 & ~3;
+        if (tid == 0) s_nlong = 0;
+        // Phase 1: every gather of the thread issued together.
+        int4 cq[ST_QUADS];
+#pragma unroll
+        for (int q = 0; q < ST_QUADS; ++q) {
+            const int gq = tid + q * ST_THREADS;
+            cq[q] = gq < nq ? sc[gq] : make_int4(0, 0, 0, 0);
+        }
+        TP xq[ST_QUADS][4];
+#pragma unroll
+        for (int q = 0; q < ST_QUADS; ++q) {
+            xq[q][0] = static_cast<TP>(__ldg(&x[cq[q].x]));
+            xq[q][1] = static_cast<TP>(__ldg(&x[cq[q].y]));
+            xq[q][2] = static_cast<TP>(__ldg(&x[cq[q].z]));
+            xq[q][3] = static_cast<TP>(__ldg(&x[cq[q].w]));
+        }
+#pragma unroll
+        for (int q = 0; q < ST_QUADS; ++q) {
+            const int gq = tid + q * ST_THREADS;
+            if (gq < nq) {
+                TP aq[4];
+                smem_quad<TA, TP>(sv + 4 * gq, aq);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) sv[4 * gq + k] = aq[k] * xq[q][k];
+            }
+        }
+        __syncthreads();
+        // Phase 2: rows of at most SEQ_ROW_MAX nonzeros left to right by one
+        // thread; longer rows to a list, one warp each.
+#pragma unroll
+        for (int q = 0; q < ST_RPT; ++q) {
+            const int r = r0 + tid + q * ST_THREADS;
+            if (r < r1) {
+                const int ra = srp[r - rbase], rz = srp[r + 1 - rbase];
+                if (rz - ra > SEQ_ROW_MAX) {
+                    s_long[atomicAdd(&s_nlong, 1)] = r;
+                } else {
+                    TP s = 0;
+                    for (int p = ra - base; p < rz - base; ++p) s += sv[p];
+                    y[r] = static_cast<TX>(s);
+                }
+            }
+        }
+        __syncthreads();
+        for (int li = tid >> 5; li < s_nlong; li += ST_THREADS / 32) {
+            const int r = s_long[li];
+            const int a = srp[r - rbase] - base;
+            const int z = srp[r + 1 - rbase] - base;
+            TP s = 0;
+            for (int p = a + lane; p < z; p += 32) s += sv[p];
+            s = warp_sum(s);
+            if (lane == 0) y[r] = static_cast<TX>(s);
+        }
+        // this thread's writes to the buffer before the next bulk copy into it
+        fence_proxy_async_smem();
+    }
+    if (skipped || fail) {
+        if (fail && tid == 0) atomicOr(status, ST_TIMEOUT);
+        // No copy may still be writing this block's shared memory when it
+        // exits: wait (bounded) for those issued and not consumed.
+        for (int k = i; k < t1 && k < i + S - 1; ++k) {
+            if (!staged(k)) continue;
+            const int sb = (k - t0) % S;
+            mbar_wait(&bar[sb], (phase >> sb) & 1u);
+            phase ^= 1u << sb;
+        }
+    }
+}
+
+template <typename TA, typename TX>
+int launch_spmv(int n, int nblocks, const int2* tiles, const int* row_ptr, const int* col_idx, const TA* values,
+                const TX* x, TX* y, const int* skip_flag, int* status, cudaStream_t s) {
     if (n <= 0 || nblocks <= 0) return MEXK_OK;
-    const int grid = nblocks < 1048576 ? nblocks : 1048576;
-    const bool vec = padded && reinterpret_cast<uintptr_t>(col_idx) % 16 == 0 &&
-                     reinterpret_cast<uintptr_t>(values) % 16 == 0;
-    if (vec)
-    {
-        const cudaError_t e = launch_dependent(spmv_rowblock_kernel<TA, TX, true>, grid, SPMV_THREADS, 0, s,
-                                               nblocks, blocks, row_ptr, col_idx, values, x, y, skip_flag);
-        if (e != cudaSuccess) {
-            set_cuda_error(e, "spmv_rowblock_kernel", __FILE__, __LINE__);
+    if (reinterpret_cast<uintptr_t>(col_idx) % 16 != 0 || reinterpret_cast<uintptr_t>(values) % 16 != 0 ||
+        reinterpret_cast<uintptr_t>(row_ptr) % 16 != 0) {
+        set_error_text("spmv: context arrays must be 16-byte aligned");
+        return MEXK_ERR_INVALID;
+    }
+    constexpr size_t smem = ST_STAGES * TileStage<TA>::BYTES;
+    auto kern = spmv_stream_kernel<TA, TX>;
+    static int resident = 0;  // thread blocks per SM (one device type per process)
+    if (resident == 0) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, ST_THREADS, smem);
+        if (e != cudaSuccess || resident < 1) {
+            resident = 0;
+            set_cuda_error(e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "spmv_stream_kernel setup", __FILE__,
+                           __LINE__);
             return MEXK_ERR_CUDA;
         }
-        return MEXK_OK;
     }
-    else
-        spmv_rowblock_kernel<TA, TX, false><<<grid, SPMV_THREADS, 0, s>>>(nblocks, blocks, row_ptr, col_idx,
-                                                                          values, x, y, skip_flag);
-    MEXK_CK_LAUNCH("spmv_rowblock_kernel");
+    const long long cap = static_cast<long long>(device_sm_count()) * resident;
+    const int grid = static_cast<int>(nblocks < cap ? nblocks : cap);
+    const cudaError_t e =
+        launch_dependent(kern, grid, ST_THREADS, smem, s, nblocks, tiles, row_ptr, col_idx, values, x, y, skip_flag,
+                         status);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "spmv_stream_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
     return MEXK_OK;
 }
 
-template int launch_spmv<double, double>(int, int, const int*, const int*, const int*, const double*,
-                                         const double*, double*, const int*, cudaStream_t, bool);
-template int launch_spmv<float, float>(int, int, const int*, const int*, const int*, const float*,
-                                       const float*, float*, const int*, cudaStream_t, bool);
+template int launch_spmv<double, double>(int, int, const int2*, const int*, const int*, const double*,
+                                         const double*, double*, const int*, int*, cudaStream_t);
+template int launch_spmv<float, float>(int, int, const int2*, const int*, const int*, const float*, const float*,
+                                       float*, const int*, int*, cudaStream_t);
 
 // FP32 copy of the FP64 matrix values for the mixed-precision form
 // (round to nearest).
@@ -297,8 +517,15 @@ static int spmv_standalone(int rows, const int* row_ptr, const int* col_idx, con
     int* d_blocks = nullptr;
     MEXK_CK(cudaMallocAsync(reinterpret_cast<void**>(&d_blocks), sizeof(int) * blocks.size(), s));
     MEXK_CK(cudaMemcpyAsync(d_blocks, blocks.data(), sizeof(int) * blocks.size(), cudaMemcpyHostToDevice, s));
-    int rc = launch_spmv<TA, TX>(rows, static_cast<int>(blocks.size()) - 1, d_blocks, row_ptr, col_idx,
-                                 values, x, y, nullptr, s, false);
+    const int nb = static_cast<int>(blocks.size()) - 1;
+    int rc = MEXK_OK;
+    spmv_rowblock_kernel<TA, TX><<<nb < 1048576 ? nb : 1048576, SPMV_THREADS, 0, s>>>(nb, d_blocks, row_ptr, col_idx,
+                                                                                     values, x, y);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) {
+        set_cuda_error(le, "spmv_rowblock_kernel", __FILE__, __LINE__);
+        rc = MEXK_ERR_CUDA;
+    }
     cudaError_t e = cudaFreeAsync(d_blocks, s);
     if (rc == MEXK_OK && e != cudaSuccess) {
         set_cuda_error(e, "cudaFreeAsync", __FILE__, __LINE__);
