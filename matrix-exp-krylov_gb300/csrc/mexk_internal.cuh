@@ -254,22 +254,28 @@ __device__ __forceinline__ void reduce_partials(const double* partials, int nblo
 // Row-block schedule: rows [blocks[b], blocks[b+1]) form block b. A block
 // holds <= tile nonzeros and <= tile_rows rows, or one longer row.
 std::vector<int> build_row_blocks(int n, const int* row_ptr, int tile = SPMV_TILE, int tile_rows = SPMV_TILE_ROWS);
-// The context SpMV's schedule, each block with its first nonzero: {first row, row_ptr[first row]}.
-std::vector<int2> build_row_tiles(int n, const int* row_ptr);
+// The context SpMV's schedule: tiles[b] = {first row, first nonzero, offset
+// of the block's 16-bit columns in col16 or -1, their base} (b <= nblocks),
+// and the narrow column copy of the blocks whose columns span <= 65536.
+struct SpmvSchedule {
+    std::vector<int4> tiles;
+    std::vector<uint16_t> col16;
+};
+SpmvSchedule build_spmv_schedule(int n, const int* row_ptr, const int* col_idx);
 
 int launch_narrow_values(const double* src, float* dst, size_t count, cudaStream_t s);
 // *ok = 1 when A equals its transpose exactly, else 0.
 int launch_symmetric_check(int n, const int* row_ptr, const int* col_idx, const double* values, int* ok,
                            cudaStream_t s);
 
-// Context SpMV over the schedule build_row_tiles made. col_idx, values and
-// row_ptr are 16-byte aligned; col_idx and values have at least 3 readable
+// Context SpMV over the schedule build_spmv_schedule made (tiles, col16 on
+// the device). col16, col_idx, values and row_ptr are 16-byte aligned; col_idx and values have at least 3 readable
 // entries past nnz, row_ptr at least n + 4 entries (row blocks are copied in
 // whole 16-byte groups). A bulk copy that never completes sets ST_TIMEOUT in
 // *status after a bounded wait; skip_flag (may be null) skips the product.
 template <typename TA, typename TX>
-int launch_spmv(int n, int nblocks, const int2* tiles, const int* row_ptr, const int* col_idx, const TA* values,
-                const TX* x, TX* y, const int* skip_flag, int* status, cudaStream_t s);
+int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, const int* row_ptr, const int* col_idx,
+                const TA* values, const TX* x, TX* y, const int* skip_flag, int* status, cudaStream_t s);
 
 // ------------------------------------------------------------ Gram-Schmidt
 enum GsMode : int { GS_DOT = 0, GS_UPD_DOT = 1, GS_UPD_NORM = 2 };

@@ -15,7 +15,8 @@
 // HBM layout per context (n rows, m_alloc maximum Krylov dimension):
 //   CSR        row_ptr int32[n+1], col_idx int32[nnz], values f64[nnz]
 //              (+ f32 copy of values for the mixed-precision form)
-//   row blocks int2[nblocks+1] SpMV schedule {first row, first nonzero}
+//   row blocks int4[nblocks+1] SpMV schedule {first row, first nonzero, 16-bit column offset, base}
+//   col16      uint16 columns of the row blocks whose columns span <= 65536
 //   basis V    column-major, leading dimension ldv = n rounded up to 64,
 //              m_alloc+1 columns, f64 (+ f32 basis for the mixed form, whose
 //              columns carry f64 scales, with the Gram matrix, in GramState)
@@ -73,7 +74,8 @@ struct mexk_context_s {
     int* d_col = nullptr;
     double* d_val = nullptr;
     float* d_val32 = nullptr;
-    int2* d_tiles = nullptr;
+    int4* d_tiles = nullptr;
+    uint16_t* d_col16 = nullptr;
     double* d_V = nullptr;
     float* d_V32 = nullptr;
     double* d_w = nullptr;
@@ -271,7 +273,7 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
     const size_t ldv = static_cast<size_t>(ctx->ldv);
     int rc;
     if (fp32) {
-        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_row_ptr, ctx->d_col,
+        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->d_row_ptr, ctx->d_col,
                                             ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32,
                                             &ctx->d_state->breakdown, &ctx->d_state->status, s)))
             return rc;
@@ -280,7 +282,7 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
         if ((rc = launch_gram_dot(g, s))) return rc;
         return launch_gram_update(g, s);
     }
-    if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_row_ptr, ctx->d_col,
+    if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->d_row_ptr, ctx->d_col,
                                           ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, &ctx->d_state->breakdown,
                                           &ctx->d_state->status, s)))
         return rc;
@@ -562,10 +564,14 @@ int mexk_context_upload_csr(mexk_context_t ctx, int rows, long long nnz, const i
         MEXK_CK(cudaMemcpy(ctx->d_col, col_idx, sizeof(int) * nnz, cudaMemcpyHostToDevice));
         MEXK_CK(cudaMemcpy(ctx->d_val, values, sizeof(double) * nnz, cudaMemcpyHostToDevice));
     }
-    std::vector<int2> tiles = build_row_tiles(rows, row_ptr);
-    ctx->nblocks = static_cast<int>(tiles.size()) - 1;
-    if ((rc = dalloc(&ctx->d_tiles, tiles.size()))) return rc;
-    MEXK_CK(cudaMemcpy(ctx->d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice));
+    const SpmvSchedule sched = build_spmv_schedule(rows, row_ptr, col_idx);
+    ctx->nblocks = static_cast<int>(sched.tiles.size()) - 1;
+    if ((rc = dalloc(&ctx->d_tiles, sched.tiles.size()))) return rc;
+    MEXK_CK(cudaMemcpy(ctx->d_tiles, sched.tiles.data(), sizeof(int4) * sched.tiles.size(), cudaMemcpyHostToDevice));
+    if ((rc = dalloc(&ctx->d_col16, sched.col16.size() + 8))) return rc;
+    if (!sched.col16.empty())
+        MEXK_CK(cudaMemcpy(ctx->d_col16, sched.col16.data(), sizeof(uint16_t) * sched.col16.size(),
+                           cudaMemcpyHostToDevice));
     const size_t vcount = static_cast<size_t>(ctx->ldv) * (m_alloc_max + 1);
     if ((rc = dalloc(&ctx->d_V, vcount))) return rc;
     MEXK_CK(cudaMemset(ctx->d_V, 0, sizeof(double) * vcount));
@@ -606,6 +612,7 @@ int mexk_context_destroy(mexk_context_t ctx) {
     dfree(ctx->d_val);
     dfree(ctx->d_val32);
     dfree(ctx->d_tiles);
+    dfree(ctx->d_col16);
     dfree(ctx->d_V);
     dfree(ctx->d_V32);
     dfree(ctx->d_w);
@@ -888,10 +895,10 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
         }
         switch (kind) {
             case MEXK_KERNEL_SPMV:
-                rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_row_ptr, ctx->d_col,
+                rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->d_row_ptr, ctx->d_col,
                                                       ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr,
                                                       &ctx->d_state->status, s)
-                          : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_row_ptr,
+                          : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->d_row_ptr,
                                                         ctx->d_col, ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, nullptr,
                                                         &ctx->d_state->status, s);
                 break;

@@ -21,6 +21,9 @@
 // served from L2 (x is one basis column, read right after it was written).
 #include "mexk_internal.cuh"
 
+#include <algorithm>
+#include <climits>
+
 namespace mexk {
 
 std::vector<int> build_row_blocks(int n, const int* row_ptr, int tile, int tile_rows) {
@@ -240,16 +243,45 @@ __device__ __forceinline__ void smem_quad<double, double>(const double* p, doubl
     o[3] = t1.y;
 }
 
-std::vector<int2> build_row_tiles(int n, const int* row_ptr) {
+SpmvSchedule build_spmv_schedule(int n, const int* row_ptr, const int* col_idx) {
+    SpmvSchedule s;
     const std::vector<int> blocks = build_row_blocks(n, row_ptr, ST_TILE, ST_ROWS);
-    std::vector<int2> tiles(blocks.size());
-    for (size_t b = 0; b < blocks.size(); ++b) tiles[b] = make_int2(blocks[b], row_ptr[blocks[b]]);
-    return tiles;
+    s.tiles.resize(blocks.size());
+    for (size_t b = 0; b + 1 < blocks.size(); ++b) {
+        const int r0 = blocks[b], r1 = blocks[b + 1];
+        const int e0 = row_ptr[r0], e1 = row_ptr[r1];
+        int off = -1, cbase = 0;
+        if (e1 > e0 && e1 - e0 <= ST_TILE) {
+            int lo = col_idx[e0], hi = col_idx[e0];
+            for (int e = e0 + 1; e < e1; ++e) {
+                lo = std::min(lo, col_idx[e]);
+                hi = std::max(hi, col_idx[e]);
+            }
+            if (static_cast<long long>(hi) - lo <= 65535) {
+                // positions e - base of the row block's 16-byte groups, 8 per 16 bytes
+                const int base = e0 & ~3;
+                const int nq = (e1 - base + 3) >> 2;
+                const size_t len = (static_cast<size_t>(4 * nq) + 7) & ~static_cast<size_t>(7);
+                if (s.col16.size() + len <= static_cast<size_t>(INT_MAX)) {
+                    off = static_cast<int>(s.col16.size());
+                    cbase = lo;
+                    s.col16.resize(s.col16.size() + len, 0);
+                    for (int e = e0; e < e1; ++e) s.col16[off + (e - base)] = static_cast<uint16_t>(col_idx[e] - lo);
+                }
+            }
+        }
+        s.tiles[b] = make_int4(r0, e0, off, cbase);
+    }
+    s.tiles.back() = make_int4(n, row_ptr[n], -1, 0);
+    return s;
 }
 
-// Context form. tiles[b] = {first row, first nonzero} of row block b (b <=
-// nblocks); col_idx/values 16-byte aligned with >= 3 entries past nnz, the
-// column indices there zero; row_ptr with >= n + 4 entries. Thread block g
+// Context form. tiles[b] = {first row, first nonzero, offset of its 16-bit
+// columns in col16 or -1, their base} of row block b (b <= nblocks);
+// col_idx/values 16-byte aligned with >= 3 entries past nnz, the column
+// indices there zero; row_ptr with >= n + 4 entries. A row block whose
+// columns span at most 65536 is staged from col16 (2 bytes per nonzero
+// instead of 4). Thread block g
 // takes row blocks [t0, t1) through ST_STAGES buffers: thread 0 issues the
 // bulk copies of row block i + ST_STAGES - 1 once every thread has finished
 // row block i - 1 (whose buffer it reuses). Every staged 16-byte group is
@@ -259,8 +291,9 @@ std::vector<int2> build_row_tiles(int n, const int* row_ptr) {
 // staged: the block streams them directly.
 template <typename TA, typename TX>
 __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
-    spmv_stream_kernel(int nblocks, const int2* __restrict__ tiles, const int* __restrict__ row_ptr,
-                       const int* __restrict__ col_idx, const TA* __restrict__ values, const TX* __restrict__ x,
+    spmv_stream_kernel(int nblocks, const int4* __restrict__ tiles, const uint16_t* __restrict__ col16,
+                       const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
+                       const TA* __restrict__ values, const TX* __restrict__ x,
                        TX* __restrict__ y, const int* __restrict__ skip, int* __restrict__ status) {
     using TP = typename AccType<TX>::type;
     using SL = TileStage<TA>;
@@ -279,7 +312,7 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
     const int t1 = t0 + per + (g < extra ? 1 : 0);
     auto staged = [&](int i) { return tiles[i + 1].y - tiles[i].y <= ST_TILE; };
     auto issue = [&](int i, uint64_t pol) {  // thread 0
-        const int2 a = tiles[i], b = tiles[i + 1];
+        const int4 a = tiles[i], b = tiles[i + 1];
         if (b.y - a.y > ST_TILE) return;
         const int s = (i - t0) % S;
         unsigned char* st = smem + s * SL::BYTES;
@@ -287,10 +320,14 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
         const uint32_t nq = static_cast<uint32_t>((b.y - base + 3) >> 2);
         const int rbase = a.x & ~3;
         const uint32_t nrp = static_cast<uint32_t>((b.x + 1 - rbase + 3) & ~3);
-        const uint32_t bc = nq * 16u, bv = nq * 4u * static_cast<uint32_t>(sizeof(TA)), br = nrp * 4u;
+        const uint32_t bc = a.z >= 0 ? (nq + 1u) / 2u * 16u : nq * 16u;
+        const uint32_t bv = nq * 4u * static_cast<uint32_t>(sizeof(TA)), br = nrp * 4u;
         mbar_arrive_expect_tx(&bar[s], bc + bv + br);
         if (nq > 0) {
-            bulk_copy_g2s(st, col_idx + base, bc, &bar[s], pol);
+            if (a.z >= 0)
+                bulk_copy_g2s(st, col16 + a.z, bc, &bar[s], pol);
+            else
+                bulk_copy_g2s(st, col_idx + base, bc, &bar[s], pol);
             bulk_copy_g2s(st + SL::COL, values + base, bv, &bar[s], pol);
         }
         bulk_copy_g2s(st + SL::COL + SL::VAL, row_ptr + rbase, br, &bar[s], pol);
@@ -323,7 +360,7 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
         if (st_i) phase ^= 1u << sb;
         if (tid == 0 && i + S - 1 < t1) issue(i + S - 1, pol);
         if (i == t1 - 1) pdl_trigger();  // this block's last row block
-        const int2 ta = tiles[i], tb = tiles[i + 1];
+        const int4 ta = tiles[i], tb = tiles[i + 1];
         const int r0 = ta.x, r1 = tb.x, e0 = ta.y, e1 = tb.y;
         if (!st_i) {
             // One long row: the block splits its nonzeros, then a tree sum.
@@ -335,7 +372,7 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
             continue;
         }
         unsigned char* st = smem + sb * SL::BYTES;
-        const int4* sc = reinterpret_cast<const int4*>(st);
+        const bool narrow = ta.z >= 0;
         TP* sv = reinterpret_cast<TP*>(st + SL::COL);  // values, then products (entry e at e - base)
         const int* srp = reinterpret_cast<const int*>(st + SL::COL + SL::VAL);
         const int base = e0 & ~3;
@@ -344,10 +381,23 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
         if (tid == 0) s_nlong = 0;
         // Phase 1: every gather of the thread issued together.
         int4 cq[ST_QUADS];
+        if (narrow) {
+            const uint2* sc = reinterpret_cast<const uint2*>(st);
+            const int cb = ta.w;
 #pragma unroll
-        for (int q = 0; q < ST_QUADS; ++q) {
-            const int gq = tid + q * ST_THREADS;
-            cq[q] = gq < nq ? sc[gq] : make_int4(0, 0, 0, 0);
+            for (int q = 0; q < ST_QUADS; ++q) {
+                const int gq = tid + q * ST_THREADS;
+                const uint2 w = gq < nq ? sc[gq] : make_uint2(0u, 0u);
+                cq[q] = make_int4(cb + static_cast<int>(w.x & 0xffffu), cb + static_cast<int>(w.x >> 16),
+                                  cb + static_cast<int>(w.y & 0xffffu), cb + static_cast<int>(w.y >> 16));
+            }
+        } else {
+            const int4* sc = reinterpret_cast<const int4*>(st);
+#pragma unroll
+            for (int q = 0; q < ST_QUADS; ++q) {
+                const int gq = tid + q * ST_THREADS;
+                cq[q] = gq < nq ? sc[gq] : make_int4(0, 0, 0, 0);
+            }
         }
         TP xq[ST_QUADS][4];
 #pragma unroll
@@ -411,11 +461,11 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
 }
 
 template <typename TA, typename TX>
-int launch_spmv(int n, int nblocks, const int2* tiles, const int* row_ptr, const int* col_idx, const TA* values,
-                const TX* x, TX* y, const int* skip_flag, int* status, cudaStream_t s) {
+int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, const int* row_ptr, const int* col_idx,
+                const TA* values, const TX* x, TX* y, const int* skip_flag, int* status, cudaStream_t s) {
     if (n <= 0 || nblocks <= 0) return MEXK_OK;
     if (reinterpret_cast<uintptr_t>(col_idx) % 16 != 0 || reinterpret_cast<uintptr_t>(values) % 16 != 0 ||
-        reinterpret_cast<uintptr_t>(row_ptr) % 16 != 0) {
+        reinterpret_cast<uintptr_t>(row_ptr) % 16 != 0 || reinterpret_cast<uintptr_t>(col16) % 16 != 0) {
         set_error_text("spmv: context arrays must be 16-byte aligned");
         return MEXK_ERR_INVALID;
     }
@@ -435,8 +485,8 @@ int launch_spmv(int n, int nblocks, const int2* tiles, const int* row_ptr, const
     const long long cap = static_cast<long long>(device_sm_count()) * resident;
     const int grid = static_cast<int>(nblocks < cap ? nblocks : cap);
     const cudaError_t e =
-        launch_dependent(kern, grid, ST_THREADS, smem, s, nblocks, tiles, row_ptr, col_idx, values, x, y, skip_flag,
-                         status);
+        launch_dependent(kern, grid, ST_THREADS, smem, s, nblocks, tiles, col16, row_ptr, col_idx, values, x, y,
+                         skip_flag, status);
     if (e != cudaSuccess) {
         set_cuda_error(e, "spmv_stream_kernel", __FILE__, __LINE__);
         return MEXK_ERR_CUDA;
@@ -444,10 +494,10 @@ int launch_spmv(int n, int nblocks, const int2* tiles, const int* row_ptr, const
     return MEXK_OK;
 }
 
-template int launch_spmv<double, double>(int, int, const int2*, const int*, const int*, const double*,
-                                         const double*, double*, const int*, int*, cudaStream_t);
-template int launch_spmv<float, float>(int, int, const int2*, const int*, const int*, const float*, const float*,
-                                       float*, const int*, int*, cudaStream_t);
+template int launch_spmv<double, double>(int, int, const int4*, const uint16_t*, const int*, const int*,
+                                         const double*, const double*, double*, const int*, int*, cudaStream_t);
+template int launch_spmv<float, float>(int, int, const int4*, const uint16_t*, const int*, const int*, const float*,
+                                       const float*, float*, const int*, int*, cudaStream_t);
 
 // FP32 copy of the FP64 matrix values for the mixed-precision form
 // (round to nearest).
