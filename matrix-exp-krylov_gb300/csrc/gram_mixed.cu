@@ -88,12 +88,11 @@ __device__ __forceinline__ const float4* col4(const float* V, size_t ldv, int c)
 // slot(v) (layout part[slot * GRAM_MAX_ROW_BLOCKS + b]), into out[v]; all
 // threads of the block call it. FP64 adds and shuffles take about 64 and 100
 // cycles of latency on this GPU (FP32: 4), so the sum is shaped for depth: g2
-// adjacent lanes share a value, each loads up to PR partials in one round and
+// adjacent lanes share a value, each loads PR partials per round and
 // adds them as a tree, then the lanes combine by an xor butterfly (every lane
 // ends with the same bits). The order depends only on nrb and nv.
-template <typename SlotFn>
+template <int PR, typename SlotFn>
 __device__ __forceinline__ void sum_partials(const double* part, int nrb, int nv, SlotFn slot, double* out) {
-    constexpr int PR = 12;
     int g2 = 32;
     while (g2 > 1 && g2 * nv > GT) g2 >>= 1;
     const int t = threadIdx.x;
@@ -117,6 +116,80 @@ __device__ __forceinline__ void sum_partials(const double* part, int nrb, int nv
     }
     for (int o = 1; o < g2; o <<= 1) sum += __shfl_xor_sync(FULL, sum, o);
     if (vi < nv && sub == 0) out[vi] = sum;
+}
+
+// The finish of a step over at most two columns (j - 1 and j; the first two
+// Arnoldi steps and every step of a window of 2): after the partial sums one
+// thread runs the whole chain (one rsqrt, a few products, one rsqrt) instead
+// of the general finish's five block-wide stages.
+__device__ __forceinline__ void gram_finish2(const GramArgs& g, int nrb) {
+    DevState* st = g.st;
+    const int j = g.j;
+    const int lo = g.lo;
+    const int kw = j + 1 - lo;
+    __shared__ double s_tot[5];  // a (kw), b (kw), |w|^2
+    const int t = threadIdx.x;
+    GramState* gs = g.gs;
+    double* G = gs->G;
+    const size_t ldh = static_cast<size_t>(g.ldh);
+    for (int r = t; r < lo; r += GT) g.H[r + static_cast<size_t>(j) * ldh] = 0.0;  // outside the window
+    const double s0 = kw == 2 ? gs->s[lo] : 0.0;
+    const double ip_j = gs->ip[j];
+    sum_partials<16>(g.part, nrb, 2 * kw + 1,
+                     [&](int v) { return v < kw ? lo + v : (v < 2 * kw ? GRAM_BOFF + lo + (v - kw) : GRAM_NWOFF); },
+                     s_tot);
+    __syncthreads();
+    if (t != 0) return;
+    const double bj = s_tot[2 * kw - 1];
+    const double sj = (bj > 0.0 && !isinf(bj)) ? rsqrt(bj) : 0.0;
+    if (j >= 1) {
+        // the previous step's h_{j,j-1} = |u_j| / p_j; breakdown test as main.cu:1911
+        const double beta = sqrt(bj) * ip_j;
+        const bool bad = !(beta >= 1e-14) || isinf(beta);
+        g.H[j + static_cast<size_t>(j - 1) * ldh] = bad ? 0.0 : beta;
+        if (bad) {
+            st->breakdown = 1;
+            st->k_used = j;
+            return;
+        }
+    }
+    gs->s[j] = sj;
+    G[j + static_cast<size_t>(j) * GRAM_LD] = 1.0;
+    const double sj2 = sj * sj;
+    const double cj = sj2 * s_tot[kw - 1];
+    double hj = cj, part;
+    if (kw == 2) {
+        const double g01 = (s0 * s_tot[kw]) * sj;  // G(j-1, j)
+        const double cp = (s0 * s_tot[0]) * sj;    // c_{j-1}
+        G[lo + static_cast<size_t>(j) * GRAM_LD] = g01;
+        G[j + static_cast<size_t>(lo) * GRAM_LD] = g01;
+        double hp = cp;
+        if (g.reortho) {
+            hp = cp - __dmul_rn(g01, cj);
+            hj = cj - __dmul_rn(g01, cp);
+        }
+        g.H[lo + static_cast<size_t>(j) * ldh] = hp;
+        gs->coef[lo] = static_cast<float>(s0 * hp);
+        const double gh0 = fma(g01, hj, hp), gh1 = hj + __dmul_rn(g01, hp);
+        part = hp * (gh0 - 2.0 * cp) + hj * (gh1 - 2.0 * cj);
+    } else {
+        part = hj * (hj - 2.0 * cj);
+    }
+    g.H[j + static_cast<size_t>(j) * ldh] = hj;
+    gs->coef[j] = static_cast<float>(sj * hj);
+    const double w2 = sj2 * s_tot[2 * kw];
+    const double u2 = w2 + part;
+    double p = 1.0, ip = 1.0;
+    if (u2 > 1e-8 * w2 && !isinf(u2)) {
+        p = rsqrt(u2);
+        ip = u2 * p;
+    } else if (w2 > 0.0 && !isinf(w2)) {
+        p = rsqrt(w2);
+        ip = w2 * p;
+    }
+    gs->ip[j + 1] = ip;
+    gs->wsc = static_cast<float>(sj);
+    gs->psc = static_cast<float>(p);
 }
 
 // Last block of a grid whose nrb row blocks each wrote their partials of
@@ -144,6 +217,7 @@ __device__ __noinline__ void gram_finish(const GramArgs& g, int nrb) {
     const int t = threadIdx.x;
     GramState* gs = g.gs;
     double* G = gs->G;
+    const size_t ldh = static_cast<size_t>(g.ldh);
     // Stage 1: the previous columns' Gram block and scales, and the partial sums.
     for (int e = t; e < jw * jw; e += GT) {
         const int r = e % jw, c = e / jw;
@@ -152,14 +226,13 @@ __device__ __noinline__ void gram_finish(const GramArgs& g, int nrb) {
     double sc_t = 0.0;
     if (t < jw) sc_t = gs->s[lo + t];
     const double ip_j = gs->ip[j];
-    sum_partials(g.part, nrb, 2 * kw + 1,
+    sum_partials<12>(g.part, nrb, 2 * kw + 1,
                  [&](int v) { return v < kw ? lo + v : (v < 2 * kw ? GRAM_BOFF + lo + (v - kw) : GRAM_NWOFF); },
                  s_tot);
     __syncthreads();
     // Stage 2: warp 7 lane 0: s_j = 1/|u_j| and H(j, j-1) = |u_j| / p_j (the
     // breakdown test of main.cu:1911); threads i < jw meanwhile scale their
     // column's b and a by s_i.
-    const size_t ldh = static_cast<size_t>(g.ldh);
     if (t == GT - 32) {
         const double bj = s_tot[2 * kw - 1];
         const bool ok = bj > 0.0 && !isinf(bj);
@@ -344,8 +417,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
 
 // Sweep 1 for a step over at most two columns (the first two Arnoldi steps,
 // every step of a window of 2): w, u_j and u_{j-1} are each read once, two
-// rows per thread per iteration, one column group, and the grid is sized so
-// that the finish sums a few hundred partials in one round of loads.
+// rows per thread per iteration, one column group.
 __global__ void __launch_bounds__(GT, 4) gram_dot2_kernel(GramArgs g) {
     pdl_wait();
     DevState* st = g.st;
@@ -407,7 +479,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot2_kernel(GramArgs g) {
     });
     __shared__ int s_flag;
     if (!grid_last_block(g.counter, &s_flag)) return;
-    gram_finish<2>(g, gridDim.x);
+    gram_finish2(g, gridDim.x);
 }
 
 // Sweep 2: u_{j+1} = psc * (wsc * w - sum_c coef_c u_c), written to column
@@ -484,7 +556,7 @@ __global__ void __launch_bounds__(GT) gram_norm_kernel(GramArgs g) {
     __shared__ int s_flag;
     if (!grid_last_block(g.counter, &s_flag)) return;
     __shared__ double s_tot[1];
-    sum_partials(g.part, gridDim.x, 1, [](int) { return 0; }, s_tot);
+    sum_partials<20>(g.part, gridDim.x, 1, [](int) { return 0; }, s_tot);
     __syncthreads();
     if (threadIdx.x == 0) {
         GramState* gs = g.gs;
@@ -529,9 +601,9 @@ int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
     const int kw = a.j + 1 - a.lo;
     cudaError_t e;
     if (kw <= 2) {
-        // two rows per thread per iteration: 2 row blocks per SM keep ~100 bytes
-        // per thread in flight
-        e = launch_dependent(gram_dot2_kernel, row_blocks((a.n + 1) / 2, 2), GT, 0, s, a);
+        // two rows per thread per iteration, 3 row blocks per SM (measured
+        // best of 2-6); the finish sums their partials in one round of loads
+        e = launch_dependent(gram_dot2_kernel, row_blocks((a.n + 1) / 2, 3), GT, 0, s, a);
     } else {
         const int ngroups = (kw + GG - 1) / GG;
         // One wave of 4 resident blocks per SM over all column groups (a partial
