@@ -417,7 +417,9 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
 
 // Sweep 1 for a step over at most two columns (the first two Arnoldi steps,
 // every step of a window of 2): w, u_j and u_{j-1} are each read once, two
-// rows per thread per iteration, one column group.
+// rows per thread per iteration, one column group. The loads keep their L2
+// lines (default policy): the update reads the same three vectors next, and
+// with the matrix streamed evict-first they are still in L2.
 __global__ void __launch_bounds__(GT, 4) gram_dot2_kernel(GramArgs g) {
     pdl_wait();
     DevState* st = g.st;
@@ -435,12 +437,12 @@ __global__ void __launch_bounds__(GT, 4) gram_dot2_kernel(GramArgs g) {
     const int stride = gridDim.x * GT;
     int i = blockIdx.x * GT + threadIdx.x;
     for (; i + stride < n4; i += 2 * stride) {
-        const float4 x0 = __ldcs(w4 + i), x1 = __ldcs(w4 + i + stride);
-        const float4 u0 = __ldcs(u4 + i), u1 = __ldcs(u4 + i + stride);
+        const float4 x0 = __ldg(w4 + i), x1 = __ldg(w4 + i + stride);
+        const float4 u0 = __ldg(u4 + i), u1 = __ldg(u4 + i + stride);
         float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
         if (two) {
-            v0 = __ldcs(p4 + i);
-            v1 = __ldcs(p4 + i + stride);
+            v0 = __ldg(p4 + i);
+            v1 = __ldg(p4 + i + stride);
         }
         acc[0] += dot4(v0, x0) + dot4(v1, x1);
         acc[1] += dot4(u0, x0) + dot4(u1, x1);
@@ -449,9 +451,9 @@ __global__ void __launch_bounds__(GT, 4) gram_dot2_kernel(GramArgs g) {
         acc[4] += dot4(x0, x0) + dot4(x1, x1);
     }
     if (i < n4) {
-        const float4 x0 = __ldcs(w4 + i);
-        const float4 u0 = __ldcs(u4 + i);
-        const float4 v0 = two ? __ldcs(p4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 x0 = __ldg(w4 + i);
+        const float4 u0 = __ldg(u4 + i);
+        const float4 v0 = two ? __ldg(p4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
         acc[0] += dot4(v0, x0);
         acc[1] += dot4(u0, x0);
         acc[2] += dot4(v0, u0);
@@ -492,6 +494,9 @@ __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
     __shared__ float s_sc[2];
     const int k = g.j + 1;
     const int lo = g.lo;
+    // a short window's columns were just read by the dot sweep and are still
+    // in L2 (default loads); a long basis is streamed (evict-first)
+    const bool keep = k - lo <= 4;
     const GramState* gs = g.gs;
     if (threadIdx.x < MEXK_M_MAX + UCH) s_coef[threadIdx.x] = threadIdx.x < k ? gs->coef[threadIdx.x] : 0.f;
     if (threadIdx.x == 0) {
@@ -515,7 +520,8 @@ __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
                 float4 v[UCH];
 #pragma unroll
                 for (int c = 0; c < UCH; ++c)
-                    v[c] = (cb + c < k) ? __ldcs(col4(g.V, ldv, cb + c) + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    v[c] = (cb + c < k) ? (keep ? __ldg(col4(g.V, ldv, cb + c) + i) : __ldcs(col4(g.V, ldv, cb + c) + i))
+                                        : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
                 for (int c = 0; c < UCH; ++c) {
                     const float h = s_coef[cb + c];
