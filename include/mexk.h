@@ -295,7 +295,7 @@ int mexk_batch_destroy(mexk_batch_t b);
 #define MEXK_KERNEL_GS_UPD_NORM 3 /* FP64: pass-2 update + norm */
 #define MEXK_KERNEL_NORMALIZE 4   /* FP64 */
 #define MEXK_KERNEL_LIFT 5
-#define MEXK_KERNEL_CONTROLLER 6
+#define MEXK_KERNEL_CONTROLLER 6   /* the step controller of the context's last solve */
 #define MEXK_KERNEL_GRAM_DOT 7    /* mixed: dots with w and the newest column, Gram correction */
 #define MEXK_KERNEL_GRAM_UPDATE 8 /* mixed: streaming update into the next column */
 #define MEXK_KERNEL_GRAM_NORM 9   /* mixed: norm of the last column (once per basis) */
@@ -308,8 +308,8 @@ int mexk_batch_destroy(mexk_batch_t b);
  * launch duration in milliseconds. No reference counterpart (the reference
  * times only the whole solve, METRIC total_compute_expmv_ms at main.cu:1570).
  * A kind marked FP64 or mixed returns MEXK_ERR_UNSUPPORTED for the other
- * precision. The mixed sweeps use the ortho_window of the context's last
- * solve. */
+ * precision. The mixed sweeps use the ortho_window, and the controller kind
+ * the controller, of the context's last solve. */
 int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int iters, double* ms_per_launch);
 
 #ifdef __cplusplus

@@ -30,13 +30,27 @@ namespace {
 
 constexpr int EXPM_THREADS = 512;
 
+// FP64 adds and FMAs take about 64 cycles of latency on this GPU (FP32: 4),
+// and these k <= 64 matrices leave most of the block idle, so every dot
+// product runs as four independent chains combined at the end.
+__device__ __forceinline__ double dot_k(int k, const double* X, int ldx, const double* Y) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int l = 0;
+    for (; l + 3 < k; l += 4) {
+        s0 = fma(X[l * ldx], Y[l], s0);
+        s1 = fma(X[(l + 1) * ldx], Y[l + 1], s1);
+        s2 = fma(X[(l + 2) * ldx], Y[l + 2], s2);
+        s3 = fma(X[(l + 3) * ldx], Y[l + 3], s3);
+    }
+    for (; l < k; ++l) s0 = fma(X[l * ldx], Y[l], s0);
+    return (s0 + s1) + (s2 + s3);
+}
+
 __device__ void mm(int k, const double* X, const double* Y, double* Z) {
     const int kk = k * k;
     for (int e = threadIdx.x; e < kk; e += blockDim.x) {
         const int i = e % k, j = e / k;
-        double s = 0.0;
-        for (int l = 0; l < k; ++l) s = fma(X[i + l * k], Y[l + j * k], s);
-        Z[e] = s;
+        Z[e] = dot_k(k, X + i, k, Y + j * k);
     }
     __syncthreads();
 }
@@ -151,14 +165,24 @@ struct ExpmBuf {
 
 // exp of the k-by-k matrix in B.A (ld k); returns the buffer holding the
 // result. All threads of the block must call it.
+// 1-norm column sums of the k-by-k matrix in A (thread j < k: column j).
+__device__ __forceinline__ double col_abs_sum(int k, const double* A, int j) {
+    double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+    int i = 0;
+    for (; i + 3 < k; i += 4) {
+        c0 += fabs(A[i + j * k]);
+        c1 += fabs(A[i + 1 + j * k]);
+        c2 += fabs(A[i + 2 + j * k]);
+        c3 += fabs(A[i + 3 + j * k]);
+    }
+    for (; i < k; ++i) c0 += fabs(A[i + j * k]);
+    return (c0 + c1) + (c2 + c3);
+}
+
 __device__ double* expm_block(const ExpmBuf& B, int k, int* status) {
     __shared__ int s_deg, s_sq;
     __shared__ double s_b[14];
-    if (threadIdx.x < k) {
-        double cs = 0.0;
-        for (int i = 0; i < k; ++i) cs += fabs(B.A[i + threadIdx.x * k]);
-        B.red[threadIdx.x] = cs;
-    }
+    if (threadIdx.x < k) B.red[threadIdx.x] = col_abs_sum(k, B.A, threadIdx.x);
     __syncthreads();
     if (threadIdx.x == 0) {
         double l1 = 0.0;
@@ -259,6 +283,86 @@ __device__ double* expm_block(const ExpmBuf& B, int k, int* status) {
         F = t;
     }
     return R;
+}
+
+// 1/i!, i = 0..18: the factorials are exact in double, one rounding each.
+constexpr double fact_d(int n) { return n <= 1 ? 1.0 : n * fact_d(n - 1); }
+__constant__ double kInvFact[19] = {
+    1.0 / fact_d(0),  1.0 / fact_d(1),  1.0 / fact_d(2),  1.0 / fact_d(3),  1.0 / fact_d(4),
+    1.0 / fact_d(5),  1.0 / fact_d(6),  1.0 / fact_d(7),  1.0 / fact_d(8),  1.0 / fact_d(9),
+    1.0 / fact_d(10), 1.0 / fact_d(11), 1.0 / fact_d(12), 1.0 / fact_d(13), 1.0 / fact_d(14),
+    1.0 / fact_d(15), 1.0 / fact_d(16), 1.0 / fact_d(17), 1.0 / fact_d(18)};
+
+// exp of the k-by-k matrix in B.A (ld k) by the degree-18 Taylor polynomial
+// with scaling and squaring: X = A / 2^s with |X|_1 <= 1, so the truncated
+// terms sum to at most sum_{i>18} 1/i! < 8.5e-18 (below double rounding);
+// T_18(X) by Paterson-Stockmeyer with X^2, X^3, X^4 and a Horner recurrence
+// in X^4 (7 products, no linear solve), then s squarings. A product-only
+// chain suits this GPU's FP64 latency far better than the Pade solve; the
+// candidate-step controller uses it (the reference controller keeps Pade,
+// as the reference does). Returns the buffer holding the result; all
+// threads of the block must call it.
+__device__ double* expm_taylor_block(const ExpmBuf& B, int k) {
+    __shared__ int s_sq;
+    if (threadIdx.x < k) B.red[threadIdx.x] = col_abs_sum(k, B.A, threadIdx.x);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double l1 = 0.0;
+        for (int j = threadIdx.x; j < k; j += 32) l1 = fmax(l1, B.red[j]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) l1 = fmax(l1, __shfl_xor_sync(0xffffffffu, l1, o));
+        if (threadIdx.x == 0) {
+            int sq = 0;
+            if (l1 > 1.0 && !isinf(l1)) {
+                (void)frexp(l1, &sq);  // l1 / 2^sq in [0.5, 1)
+            }
+            s_sq = sq;
+        }
+    }
+    __syncthreads();
+    const int sq = s_sq;
+    const int kk = k * k;
+    if (sq > 0) {
+        for (int e = threadIdx.x; e < kk; e += blockDim.x) B.A[e] = ldexp(B.A[e], -sq);
+        __syncthreads();
+    }
+    const double* X = B.A;
+    double* X2 = B.A2;
+    double* X3 = B.A4;
+    double* X4 = B.A6;
+    mm(k, X, X, X2);
+    mm(k, X2, X, X3);
+    mm(k, X2, X2, X4);
+    const double* c = kInvFact;
+    // Z = c16 I + c17 X + c18 X^2
+    double* Z = B.T;
+    double* W = B.U;
+    for (int e = threadIdx.x; e < kk; e += blockDim.x) {
+        double z = c[17] * X[e] + c[18] * X2[e];
+        if ((e % k) == (e / k)) z = z + c[16];
+        Z[e] = z;
+    }
+    __syncthreads();
+    // Z = B_q + X^4 Z, B_q = c_{4q} I + c_{4q+1} X + c_{4q+2} X^2 + c_{4q+3} X^3
+    for (int q = 3; q >= 0; --q) {
+        for (int e = threadIdx.x; e < kk; e += blockDim.x) {
+            const int i = e % k, j = e / k;
+            double b = c[4 * q + 1] * X[e] + c[4 * q + 2] * X2[e] + c[4 * q + 3] * X3[e];
+            if (i == j) b = b + c[4 * q];
+            W[e] = dot_k(k, X4 + i, k, Z + j * k) + b;
+        }
+        __syncthreads();
+        double* t = Z;
+        Z = W;
+        W = t;
+    }
+    for (int r = 0; r < sq; ++r) {
+        mm(k, Z, Z, W);
+        double* t = Z;
+        Z = W;
+        W = t;
+    }
+    return Z;
 }
 
 __device__ ExpmBuf carve(double* smem, int k) {
@@ -535,7 +639,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         tau = tau < rem ? tau : rem;
         for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = tau * a.H[(e % k) + (e / k) * ldh];
         __syncthreads();
-        double* R = expm_block(B, k, &st->status);
+        double* R = expm_taylor_block(B, k);
         double* c = a.cand + static_cast<size_t>(blockIdx.x) * CAND_STRIDE;
         for (int i = threadIdx.x; i < k; i += blockDim.x) c[2 + i] = R[i];
         if (threadIdx.x == 0) {
@@ -584,7 +688,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         const double dt = s_tau;
         for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = dt * a.H[(e % k) + (e / k) * ldh];
         __syncthreads();
-        R = expm_block(B, k, &st->status);
+        R = expm_taylor_block(B, k);
         if (threadIdx.x == 0) {
             err = bd ? 0.0 : fabs(a.H[k + (k - 1) * ldh] * R[k - 1]) * st->v_norm;
             write_log(st, a.log, dt, err, k, rejects);

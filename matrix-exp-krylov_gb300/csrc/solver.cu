@@ -70,6 +70,7 @@ struct mexk_context_s {
     int nblocks = 0;
     int symmetric = -1;  // A == A^T exactly: -1 not yet checked
     int last_window = 0; // ortho_window of the last solve (kernel profiling follows it)
+    int last_controller = MEXK_CTRL_REFERENCE;  // controller of the last solve (likewise)
     int* d_row_ptr = nullptr;
     int* d_col = nullptr;
     double* d_val = nullptr;
@@ -299,6 +300,32 @@ int finish_basis(mexk_context_t ctx, int j, bool fp32, cudaStream_t s) {
     return fp32 ? launch_gram_norm(gram_args(ctx, j, 1), s) : MEXK_OK;
 }
 
+// The cycle's step controller over the k x k Hessenberg (k = m, or the
+// breakdown size): the reference's (Pade exponential per attempt) or the
+// candidate-step search (with the learned centre for MEXK_CTRL_LEARNED).
+int enqueue_controller(mexk_context_t ctx, int m, int ctrl, mexk_step_t* log, cudaStream_t s) {
+    if (ctrl == MEXK_CTRL_REFERENCE) {
+        ControlArgs c;
+        c.st = ctx->d_state;
+        c.H = ctx->d_H;
+        c.ldh = ctx->ldh;
+        c.coef = ctx->d_coef;
+        c.log = log;
+        return launch_controller(c, m, s);
+    }
+    SearchArgs c;
+    c.st = ctx->d_state;
+    c.H = ctx->d_H;
+    c.ldh = ctx->ldh;
+    c.coef = ctx->d_coef;
+    c.log = log;
+    c.cand = ctx->d_cand;
+    c.counter = ctx->d_counter + 1;
+    c.mlp = ctrl == MEXK_CTRL_LEARNED ? ctx->d_mlp : nullptr;
+    c.m_cap = ctx->m_alloc < ctx->n - 1 ? ctx->m_alloc : ctx->n - 1;
+    return launch_controller_search(c, m, s);
+}
+
 // One Krylov cycle: the unit that is captured into a graph.
 template <typename TV>
 int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, cudaStream_t s) {
@@ -308,27 +335,7 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, 
     for (int j = 0; j < m; ++j)
         if ((rc = enqueue_step(ctx, j, reortho, fp32, s, window))) return rc;
     if ((rc = finish_basis(ctx, m - 1, fp32, s))) return rc;
-    if (ctrl == MEXK_CTRL_REFERENCE) {
-        ControlArgs c;
-        c.st = ctx->d_state;
-        c.H = ctx->d_H;
-        c.ldh = ctx->ldh;
-        c.coef = ctx->d_coef;
-        c.log = ctx->d_log;
-        if ((rc = launch_controller(c, m, s))) return rc;
-    } else {
-        SearchArgs c;
-        c.st = ctx->d_state;
-        c.H = ctx->d_H;
-        c.ldh = ctx->ldh;
-        c.coef = ctx->d_coef;
-        c.log = ctx->d_log;
-        c.cand = ctx->d_cand;
-        c.counter = ctx->d_counter + 1;
-        c.mlp = ctrl == MEXK_CTRL_LEARNED ? ctx->d_mlp : nullptr;
-        c.m_cap = ctx->m_alloc < ctx->n - 1 ? ctx->m_alloc : ctx->n - 1;
-        if ((rc = launch_controller_search(c, m, s))) return rc;
-    }
+    if ((rc = enqueue_controller(ctx, m, ctrl, ctx->d_log, s))) return rc;
     const LiftArgs l = lift_args(ctx, fp32);
     if ((rc = launch_lift<TV>(l, gs_grid_size(ctx->n, 1), s))) return rc;
     return launch_restart<TV>(ctx->n, ctx->ldv, ctx->d_y, V, ctx->d_state, s);
@@ -404,6 +411,7 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
     if (p->precision == MEXK_PREC_MIXED && (rc = ensure_mixed(ctx))) return rc;
     if (s == nullptr) s = ctx->stream;
     ctx->last_window = p->ortho_window;
+    ctx->last_controller = p->controller;
     init_state(ctx->h_state, p, LOG_CAP);
     MEXK_CK(cudaMemcpyAsync(ctx->d_state, ctx->h_state, sizeof(DevState), cudaMemcpyHostToDevice, s));
     if (ctx->h_state->done) {
@@ -930,16 +938,9 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
                           : launch_lift<double>(l, gs_grid_size(ctx->n, 1), s);
                 break;
             }
-            case MEXK_KERNEL_CONTROLLER: {
-                ControlArgs c;
-                c.st = ctx->d_state;
-                c.H = ctx->d_H;
-                c.ldh = ctx->ldh;
-                c.coef = ctx->d_coef;
-                c.log = nullptr;
-                rc = launch_controller(c, j + 1, s);
+            case MEXK_KERNEL_CONTROLLER:
+                rc = enqueue_controller(ctx, j + 1, ctx->last_controller, nullptr, s);
                 break;
-            }
         }
         if (rc != MEXK_OK) break;
         ce = cudaEventRecord(e1, s);
