@@ -104,9 +104,10 @@ class ClockSampler:
 # ------------------------------------------------------------------ bytes model
 # DRAM bytes (read + written) of one spmv_stream_kernel<float, float> launch
 # as ncu counted them on the 1536^2 heat grid (nnz = 11,790,336, n = 2,359,296):
-# 113.51 MB read + 3.82 MB written (the rest of y is still in L2 when the
-# kernel ends). The same stencil's traffic grows with its nonzeros.
-SPMV_F32_TRAFFIC_HEAT1536 = (113.513216e6 + 3.816704e6, 11790336)
+# 89.87 MB read + 3.00 MB written (16-bit column offsets; the rest of y is
+# still in L2 when the kernel ends). The same stencil's traffic grows with
+# its nonzeros.
+SPMV_F32_TRAFFIC_HEAT1536 = (89.869312e6 + 3.002624e6, 11790336)
 
 def kernel_bytes(kind, n, nnz, k, fp32, window=0):
     """Algorithmic HBM bytes of one launch (per-kernel minimum traffic); with a
