@@ -260,6 +260,7 @@ std::vector<int> build_row_blocks(int n, const int* row_ptr, int tile = SPMV_TIL
 struct SpmvSchedule {
     std::vector<int4> tiles;
     std::vector<uint16_t> col16;
+    bool all_narrow = true;  // every staged row block has 16-bit columns
 };
 SpmvSchedule build_spmv_schedule(int n, const int* row_ptr, const int* col_idx);
 
@@ -274,8 +275,9 @@ int launch_symmetric_check(int n, const int* row_ptr, const int* col_idx, const 
 // whole 16-byte groups). A bulk copy that never completes sets ST_TIMEOUT in
 // *status after a bounded wait; skip_flag (may be null) skips the product.
 template <typename TA, typename TX>
-int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, const int* row_ptr, const int* col_idx,
-                const TA* values, const TX* x, TX* y, const int* skip_flag, int* status, cudaStream_t s);
+int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bool all_narrow, const int* row_ptr,
+                const int* col_idx, const TA* values, const TX* x, TX* y, const int* skip_flag, int* status,
+                cudaStream_t s);
 
 // ------------------------------------------------------------ Gram-Schmidt
 enum GsMode : int { GS_DOT = 0, GS_UPD_DOT = 1, GS_UPD_NORM = 2 };

@@ -77,6 +77,7 @@ struct mexk_context_s {
     float* d_val32 = nullptr;
     int4* d_tiles = nullptr;
     uint16_t* d_col16 = nullptr;
+    bool spmv_narrow = false;  // every staged SpMV row block has 16-bit columns
     double* d_V = nullptr;
     float* d_V32 = nullptr;
     double* d_w = nullptr;
@@ -274,7 +275,7 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
     const size_t ldv = static_cast<size_t>(ctx->ldv);
     int rc;
     if (fp32) {
-        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->d_row_ptr, ctx->d_col,
+        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow, ctx->d_row_ptr, ctx->d_col,
                                             ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32,
                                             &ctx->d_state->breakdown, &ctx->d_state->status, s)))
             return rc;
@@ -283,7 +284,7 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
         if ((rc = launch_gram_dot(g, s))) return rc;
         return launch_gram_update(g, s);
     }
-    if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->d_row_ptr, ctx->d_col,
+    if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow, ctx->d_row_ptr, ctx->d_col,
                                           ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, &ctx->d_state->breakdown,
                                           &ctx->d_state->status, s)))
         return rc;
@@ -574,6 +575,7 @@ int mexk_context_upload_csr(mexk_context_t ctx, int rows, long long nnz, const i
     }
     const SpmvSchedule sched = build_spmv_schedule(rows, row_ptr, col_idx);
     ctx->nblocks = static_cast<int>(sched.tiles.size()) - 1;
+    ctx->spmv_narrow = sched.all_narrow;
     if ((rc = dalloc(&ctx->d_tiles, sched.tiles.size()))) return rc;
     MEXK_CK(cudaMemcpy(ctx->d_tiles, sched.tiles.data(), sizeof(int4) * sched.tiles.size(), cudaMemcpyHostToDevice));
     if ((rc = dalloc(&ctx->d_col16, sched.col16.size() + 8))) return rc;
@@ -903,10 +905,10 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
         }
         switch (kind) {
             case MEXK_KERNEL_SPMV:
-                rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->d_row_ptr, ctx->d_col,
+                rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow, ctx->d_row_ptr, ctx->d_col,
                                                       ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr,
                                                       &ctx->d_state->status, s)
-                          : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->d_row_ptr,
+                          : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow, ctx->d_row_ptr,
                                                         ctx->d_col, ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, nullptr,
                                                         &ctx->d_state->status, s);
                 break;

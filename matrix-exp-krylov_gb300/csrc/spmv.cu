@@ -205,22 +205,26 @@ __device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 constexpr int ST_THREADS = 256;
 constexpr int ST_TILE = 2048;
 constexpr int ST_ROWS = 512;
-constexpr int ST_STAGES = 2;
+constexpr int ST_STAGES = 2;  // buffers (measured: 3 and 4 slower, 39.6 / 45.3 us against 38.0 on heat2048 FP32)
 constexpr int ST_MINB = 5;
 
 // Shared-memory image of one row block: the 16-byte groups of column indices
-// and values its nonzeros span, then row_ptr from its first row rounded down
-// to a multiple of 4 through its end row.
-template <typename TA>
+// (32-bit, or 16-bit offsets when NARROW: every staged row block of the
+// matrix has them) and values its nonzeros span, then row_ptr from its first
+// row rounded down to a multiple of 4 through its end row. The compact NARROW
+// image leaves more of the SM's shared storage to L1, which serves the x
+// gathers (heat2048 FP32: 38.0 against 38.8 us).
+template <typename TA, bool NARROW>
 struct TileStage {
     static constexpr int QMAX = (ST_TILE + 6) / 4;  // groups of 4 a row block spans
-    static constexpr int COL = QMAX * 16;
+    static constexpr int COL = NARROW ? (QMAX * 8 + 15) / 16 * 16 : QMAX * 16;
     static constexpr int VAL = QMAX * 4 * static_cast<int>(sizeof(TA));
     static constexpr int RP = (ST_ROWS + 4 + 3) / 4 * 16;
     static constexpr int BYTES = COL + VAL + RP;
+    static constexpr int STAGES = ST_STAGES;
     static_assert(COL % 16 == 0 && VAL % 16 == 0 && RP % 16 == 0, "bulk copies need 16-byte pieces");
 };
-constexpr int ST_QUADS = (TileStage<float>::QMAX + ST_THREADS - 1) / ST_THREADS;
+constexpr int ST_QUADS = (TileStage<float, false>::QMAX + ST_THREADS - 1) / ST_THREADS;
 constexpr int ST_RPT = (ST_ROWS + ST_THREADS - 1) / ST_THREADS;
 
 template <typename TA, typename TP>
@@ -251,8 +255,8 @@ SpmvSchedule build_spmv_schedule(int n, const int* row_ptr, const int* col_idx) 
         const int r0 = blocks[b], r1 = blocks[b + 1];
         const int e0 = row_ptr[r0], e1 = row_ptr[r1];
         int off = -1, cbase = 0;
-        if (e1 > e0 && e1 - e0 <= ST_TILE) {
-            int lo = col_idx[e0], hi = col_idx[e0];
+        if (e1 - e0 <= ST_TILE) {
+            int lo = e1 > e0 ? col_idx[e0] : 0, hi = lo;
             for (int e = e0 + 1; e < e1; ++e) {
                 lo = std::min(lo, col_idx[e]);
                 hi = std::max(hi, col_idx[e]);
@@ -271,6 +275,7 @@ SpmvSchedule build_spmv_schedule(int n, const int* row_ptr, const int* col_idx) 
             }
         }
         s.tiles[b] = make_int4(r0, e0, off, cbase);
+        if (e1 - e0 <= ST_TILE && off < 0) s.all_narrow = false;
     }
     s.tiles.back() = make_int4(n, row_ptr[n], -1, 0);
     return s;
@@ -282,22 +287,22 @@ SpmvSchedule build_spmv_schedule(int n, const int* row_ptr, const int* col_idx) 
 // indices there zero; row_ptr with >= n + 4 entries. A row block whose
 // columns span at most 65536 is staged from col16 (2 bytes per nonzero
 // instead of 4). Thread block g
-// takes row blocks [t0, t1) through ST_STAGES buffers: thread 0 issues the
-// bulk copies of row block i + ST_STAGES - 1 once every thread has finished
+// takes row blocks [t0, t1) through SL::STAGES buffers: thread 0 issues the
+// bulk copies of row block i + STAGES - 1 once every thread has finished
 // row block i - 1 (whose buffer it reuses). Every staged 16-byte group is
 // multiplied whole (its column indices are all valid, those outside the row
 // block included), the products overwrite the staged values, and the row
 // sums read only the row block's own. Row blocks of one long row are not
 // staged: the block streams them directly.
-template <typename TA, typename TX>
+template <typename TA, typename TX, bool NARROW>
 __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
     spmv_stream_kernel(int nblocks, const int4* __restrict__ tiles, const uint16_t* __restrict__ col16,
                        const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
                        const TA* __restrict__ values, const TX* __restrict__ x,
                        TX* __restrict__ y, const int* __restrict__ skip, int* __restrict__ status) {
     using TP = typename AccType<TX>::type;
-    using SL = TileStage<TA>;
-    constexpr int S = ST_STAGES;
+    using SL = TileStage<TA, NARROW>;
+    constexpr int S = SL::STAGES;
     static_assert(sizeof(TA) == sizeof(TP), "products overwrite the staged values");
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar[S];
@@ -320,11 +325,12 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
         const uint32_t nq = static_cast<uint32_t>((b.y - base + 3) >> 2);
         const int rbase = a.x & ~3;
         const uint32_t nrp = static_cast<uint32_t>((b.x + 1 - rbase + 3) & ~3);
-        const uint32_t bc = a.z >= 0 ? (nq + 1u) / 2u * 16u : nq * 16u;
+        const bool nar = NARROW || a.z >= 0;
+        const uint32_t bc = nar ? (nq + 1u) / 2u * 16u : nq * 16u;
         const uint32_t bv = nq * 4u * static_cast<uint32_t>(sizeof(TA)), br = nrp * 4u;
         mbar_arrive_expect_tx(&bar[s], bc + bv + br);
         if (nq > 0) {
-            if (a.z >= 0)
+            if (nar)
                 bulk_copy_g2s(st, col16 + a.z, bc, &bar[s], pol);
             else
                 bulk_copy_g2s(st, col_idx + base, bc, &bar[s], pol);
@@ -372,7 +378,7 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
             continue;
         }
         unsigned char* st = smem + sb * SL::BYTES;
-        const bool narrow = ta.z >= 0;
+        const bool narrow = NARROW || ta.z >= 0;
         TP* sv = reinterpret_cast<TP*>(st + SL::COL);  // values, then products (entry e at e - base)
         const int* srp = reinterpret_cast<const int*>(st + SL::COL + SL::VAL);
         const int base = e0 & ~3;
@@ -460,17 +466,12 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
     }
 }
 
-template <typename TA, typename TX>
-int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, const int* row_ptr, const int* col_idx,
-                const TA* values, const TX* x, TX* y, const int* skip_flag, int* status, cudaStream_t s) {
-    if (n <= 0 || nblocks <= 0) return MEXK_OK;
-    if (reinterpret_cast<uintptr_t>(col_idx) % 16 != 0 || reinterpret_cast<uintptr_t>(values) % 16 != 0 ||
-        reinterpret_cast<uintptr_t>(row_ptr) % 16 != 0 || reinterpret_cast<uintptr_t>(col16) % 16 != 0) {
-        set_error_text("spmv: context arrays must be 16-byte aligned");
-        return MEXK_ERR_INVALID;
-    }
-    constexpr size_t smem = ST_STAGES * TileStage<TA>::BYTES;
-    auto kern = spmv_stream_kernel<TA, TX>;
+template <typename TA, typename TX, bool NARROW>
+int launch_spmv_as(int nblocks, const int4* tiles, const uint16_t* col16, const int* row_ptr, const int* col_idx,
+                   const TA* values, const TX* x, TX* y, const int* skip_flag, int* status, cudaStream_t s) {
+    using SL = TileStage<TA, NARROW>;
+    constexpr size_t smem = SL::STAGES * SL::BYTES;
+    auto kern = spmv_stream_kernel<TA, TX, NARROW>;
     static int resident = 0;  // thread blocks per SM (one device type per process)
     if (resident == 0) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -484,9 +485,8 @@ int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, co
     }
     const long long cap = static_cast<long long>(device_sm_count()) * resident;
     const int grid = static_cast<int>(nblocks < cap ? nblocks : cap);
-    const cudaError_t e =
-        launch_dependent(kern, grid, ST_THREADS, smem, s, nblocks, tiles, col16, row_ptr, col_idx, values, x, y,
-                         skip_flag, status);
+    const cudaError_t e = launch_dependent(kern, grid, ST_THREADS, smem, s, nblocks, tiles, col16, row_ptr, col_idx,
+                                           values, x, y, skip_flag, status);
     if (e != cudaSuccess) {
         set_cuda_error(e, "spmv_stream_kernel", __FILE__, __LINE__);
         return MEXK_ERR_CUDA;
@@ -494,10 +494,26 @@ int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, co
     return MEXK_OK;
 }
 
-template int launch_spmv<double, double>(int, int, const int4*, const uint16_t*, const int*, const int*,
+template <typename TA, typename TX>
+int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bool all_narrow, const int* row_ptr,
+                const int* col_idx, const TA* values, const TX* x, TX* y, const int* skip_flag, int* status,
+                cudaStream_t s) {
+    if (n <= 0 || nblocks <= 0) return MEXK_OK;
+    if (reinterpret_cast<uintptr_t>(col_idx) % 16 != 0 || reinterpret_cast<uintptr_t>(values) % 16 != 0 ||
+        reinterpret_cast<uintptr_t>(row_ptr) % 16 != 0 || reinterpret_cast<uintptr_t>(col16) % 16 != 0) {
+        set_error_text("spmv: context arrays must be 16-byte aligned");
+        return MEXK_ERR_INVALID;
+    }
+    return all_narrow ? launch_spmv_as<TA, TX, true>(nblocks, tiles, col16, row_ptr, col_idx, values, x, y,
+                                                      skip_flag, status, s)
+                      : launch_spmv_as<TA, TX, false>(nblocks, tiles, col16, row_ptr, col_idx, values, x, y,
+                                                       skip_flag, status, s);
+}
+
+template int launch_spmv<double, double>(int, int, const int4*, const uint16_t*, bool, const int*, const int*,
                                          const double*, const double*, double*, const int*, int*, cudaStream_t);
-template int launch_spmv<float, float>(int, int, const int4*, const uint16_t*, const int*, const int*, const float*,
-                                       const float*, float*, const int*, int*, cudaStream_t);
+template int launch_spmv<float, float>(int, int, const int4*, const uint16_t*, bool, const int*, const int*,
+                                       const float*, const float*, float*, const int*, int*, cudaStream_t);
 
 // FP32 copy of the FP64 matrix values for the mixed-precision form
 // (round to nearest).
