@@ -153,6 +153,9 @@ struct ArnoldiRunner {
 
     void init_all_devices(const std::vector<CSRHost>& partitions, const std::vector<int>& device_ids,
                           const std::vector<CSRHost::GhostMap>& ghost_maps_in);
+    // Extension: adopt a context that already holds A (mexk_context_load_bincsr
+    // with m_alloc >= params.m); the same checks and messages as init_all_devices.
+    void init_from_context(mexk_context_t ctx, int device_id = 0);
     // y_host must hold total_rows entries (the reference writes without resizing).
     void compute_expmv(const std::vector<double>& v_host, std::vector<double>& y_host);
     void destroy();

@@ -155,6 +155,34 @@ int mexk_arnoldi_step(mexk_context_t ctx, int j, int reorthogonalize, int precis
 int mexk_context_set_basis(mexk_context_t ctx, int precision, const double* V_host, int ncols);
 int mexk_context_get_basis(mexk_context_t ctx, int precision, double* V_host, int ncols);
 
+/* ---- Binary CSR v1 files ---------------------------------------------- */
+typedef struct {
+    long long rows, cols, nnz;
+    int index_dtype;    /* 1 = u32, 2 = u64 */
+    int value_dtype;    /* 1 = f32, 2 = f64 */
+    unsigned int flags; /* bit 0 sorted, bit 1 no duplicates, bit 2 symmetric upper */
+    int checks_passed;  /* load: 1 header, 2 indptr, 3 column range, 4 sorted / no-duplicate flags */
+    double max_abs;     /* max |a_ij| over the entries (NaN skipped); set by the load */
+    double seconds;     /* wall time of the load */
+} mexk_bincsr_info_t;
+
+/* Reads and checks the 64-byte header of a .bincsr file on the host (no
+ * device work), with the checks and messages of CSRHost::from_binary_csr
+ * (main.cu:265-330): MEXK_ERR_INVALID and mexk_last_error_detail() text on
+ * failure. */
+int mexk_bincsr_probe(const char* path, mexk_bincsr_info_t* info);
+
+/* Loads a .bincsr file straight into the context (replaces
+ * CSRHost::from_binary_csr + DeviceContext::alloc_from, main.cu:265-523 and
+ * 873-1067, for a square matrix). The file is memory-mapped and streamed to
+ * the device through pinned buffers; u64 indices are narrowed and f32 values
+ * widened there, and the reference loader's checks (indptr, column range,
+ * sorted / no-duplicate flags) run there too, reporting its first failure
+ * with its message (MEXK_ERR_INVALID). Files with the symmetric_upper flag,
+ * and non-square or empty matrices, return MEXK_ERR_UNSUPPORTED: CSRHost
+ * loads them on the host (and the runner reports what it cannot solve). */
+int mexk_context_load_bincsr(mexk_context_t ctx, const char* path, int m_alloc_max, mexk_bincsr_info_t* info);
+
 /* E = exp(A) for a k-by-k FP64 matrix (device pointers, column-major,
  * leading dimensions lda/lde), single thread block Pade scaling-and-squaring
  * (replaces Eigen's MatrixXd::exp at main.cu:33-36). k <= MEXK_M_MAX. */

@@ -254,15 +254,29 @@ __device__ __forceinline__ void reduce_partials(const double* partials, int nblo
 // Row-block schedule: rows [blocks[b], blocks[b+1]) form block b. A block
 // holds <= tile nonzeros and <= tile_rows rows, or one longer row.
 std::vector<int> build_row_blocks(int n, const int* row_ptr, int tile = SPMV_TILE, int tile_rows = SPMV_TILE_ROWS);
-// The context SpMV's schedule: tiles[b] = {first row, first nonzero, offset
-// of the block's 16-bit columns in col16 or -1, their base} (b <= nblocks),
-// and the narrow column copy of the blocks whose columns span <= 65536.
+// The context SpMV's schedule, on the device: d_tiles[b] = {first row, first
+// nonzero, offset of the block's 16-bit columns in d_col16 or -1, their base}
+// (b <= nblocks), and the 16-bit column copy of the blocks whose columns span
+// <= 65536 (made by a kernel from the device columns d_col; row_ptr is the
+// host copy). The caller owns (cudaFree) d_tiles and d_col16.
 struct SpmvSchedule {
-    std::vector<int4> tiles;
-    std::vector<uint16_t> col16;
+    int nblocks = 0;
+    int4* d_tiles = nullptr;
+    uint16_t* d_col16 = nullptr;
     bool all_narrow = true;  // every staged row block has 16-bit columns
 };
-SpmvSchedule build_spmv_schedule(int n, const int* row_ptr, const int* col_idx);
+int build_spmv_schedule(int n, const int* row_ptr, const int* d_col, SpmvSchedule* out, cudaStream_t s);
+
+// Upload stages shared by mexk_context_upload_csr and the .bincsr loader:
+// begin sets the sizes and allocates the context's CSR arrays (padded, zero
+// tails); the caller fills row_ptr[0..rows], col_idx and values; finish
+// builds the SpMV schedule from the device columns (row_ptr: the host copy)
+// and allocates the solver's buffers.
+int context_csr_begin(mexk_context_t ctx, int rows, long long nnz, int m_alloc_max, int** d_row_ptr, int** d_col,
+                      double** d_val);
+int context_csr_finish(mexk_context_t ctx, const int* row_ptr);
+// Makes the context's device current; *s = its stream.
+int context_stream(mexk_context_t ctx, cudaStream_t* s);
 
 int launch_narrow_values(const double* src, float* dst, size_t count, cudaStream_t s);
 // *ok = 1 when A equals its transpose exactly, else 0.

@@ -480,6 +480,89 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
 }  // namespace
 
 // ====================================================================== C ABI
+namespace mexk {
+
+int context_csr_begin(mexk_context_t ctx, int rows, long long nnz, int m_alloc_max, int** d_row_ptr, int** d_col,
+                      double** d_val) {
+    if (!ctx || rows < 1 || nnz < 0) return MEXK_ERR_INVALID;
+    if (ctx->uploaded) return MEXK_ERR_NOT_READY;
+    if (m_alloc_max < 1 || m_alloc_max > MEXK_M_MAX) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    dfree(ctx->d_row_ptr);  // left by an upload that failed
+    dfree(ctx->d_col);
+    dfree(ctx->d_val);
+    ctx->n = rows;
+    ctx->nnz = nnz;
+    ctx->m_alloc = m_alloc_max;
+    // Column stride: a multiple of 64 elements, so every column starts on a
+    // 256-byte boundary and the vectorised sweeps cover whole 16-byte groups.
+    ctx->ldv = (rows + 63) / 64 * 64;
+    ctx->ldh = m_alloc_max + 1;
+    int rc;
+    // row_ptr, col_idx and values padded (zero tails): the SpMV copies whole
+    // 16-byte groups
+    if ((rc = dalloc(&ctx->d_row_ptr, static_cast<size_t>(rows) + 8))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_row_ptr, 0, sizeof(int) * (static_cast<size_t>(rows) + 8)));
+    if ((rc = dalloc(&ctx->d_col, static_cast<size_t>(nnz) + 4))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_col + nnz, 0, sizeof(int) * 4));
+    if ((rc = dalloc(&ctx->d_val, static_cast<size_t>(nnz) + 4))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_val + nnz, 0, sizeof(double) * 4));
+    *d_row_ptr = ctx->d_row_ptr;
+    *d_col = ctx->d_col;
+    *d_val = ctx->d_val;
+    return MEXK_OK;
+}
+
+int context_stream(mexk_context_t ctx, cudaStream_t* s) {
+    MEXK_CK(cudaSetDevice(ctx->device));
+    *s = ctx->stream;
+    return MEXK_OK;
+}
+
+int context_csr_finish(mexk_context_t ctx, const int* row_ptr) {
+    int rc;
+    dfree(ctx->d_tiles);
+    dfree(ctx->d_col16);
+    SpmvSchedule sched;
+    rc = build_spmv_schedule(ctx->n, row_ptr, ctx->d_col, &sched, ctx->stream);
+    ctx->d_tiles = sched.d_tiles;
+    ctx->d_col16 = sched.d_col16;
+    if (rc) return rc;
+    ctx->nblocks = sched.nblocks;
+    ctx->spmv_narrow = sched.all_narrow;
+    const int m_alloc_max = ctx->m_alloc;
+    const size_t vcount = static_cast<size_t>(ctx->ldv) * (m_alloc_max + 1);
+    if ((rc = dalloc(&ctx->d_V, vcount))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_V, 0, sizeof(double) * vcount));
+    if ((rc = dalloc(&ctx->d_w, ctx->ldv))) return rc;
+    if ((rc = dalloc(&ctx->d_y, ctx->ldv))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_w, 0, sizeof(double) * ctx->ldv));
+    MEXK_CK(cudaMemset(ctx->d_y, 0, sizeof(double) * ctx->ldv));
+    const size_t hcount = static_cast<size_t>(ctx->ldh) * m_alloc_max;
+    if ((rc = dalloc(&ctx->d_H, hcount))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_H, 0, sizeof(double) * hcount));
+    if ((rc = dalloc(&ctx->d_h1, MEXK_M_MAX + 2))) return rc;
+    if ((rc = dalloc(&ctx->d_h2, MEXK_M_MAX + 2))) return rc;
+    if ((rc = dalloc(&ctx->d_coef, MEXK_M_MAX + 2))) return rc;
+    if ((rc = dalloc(&ctx->d_cand, static_cast<size_t>(SEARCH_CAND) * CAND_STRIDE))) return rc;
+    if ((rc = dalloc(&ctx->d_partials, static_cast<size_t>(PARTIAL_BLOCKS) * RED_STRIDE))) return rc;
+    if ((rc = dalloc(&ctx->d_counter, 4))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_counter, 0, sizeof(unsigned int) * 4));
+    if ((rc = dalloc(&ctx->d_state, 1))) return rc;
+    if ((rc = dalloc(&ctx->d_log, LOG_CAP))) return rc;
+    cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&ctx->h_state), sizeof(DevState));
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "cudaMallocHost", __FILE__, __LINE__);
+        return MEXK_ERR_ALLOC;
+    }
+    memset(ctx->h_state, 0, sizeof(DevState));
+    MEXK_CK(cudaMemcpy(ctx->d_state, ctx->h_state, sizeof(DevState), cudaMemcpyHostToDevice));
+    ctx->uploaded = true;
+    return MEXK_OK;
+}
+
+}  // namespace mexk
+
 extern "C" {
 
 const char* mexk_error_string(int code) {
@@ -554,62 +637,16 @@ int mexk_context_upload_csr(mexk_context_t ctx, int rows, long long nnz, const i
             set_error_text("column index out of range");
             return MEXK_ERR_INVALID;
         }
-    MEXK_CK(cudaSetDevice(ctx->device));
-    ctx->n = rows;
-    ctx->nnz = nnz;
-    ctx->m_alloc = m_alloc_max;
-    // Column stride: a multiple of 64 elements, so every column starts on a
-    // 256-byte boundary and the vectorised sweeps cover whole 16-byte groups.
-    ctx->ldv = (rows + 63) / 64 * 64;
-    ctx->ldh = m_alloc_max + 1;
-    int rc;
-    if ((rc = dalloc(&ctx->d_row_ptr, static_cast<size_t>(rows) + 8))) return rc;
-    MEXK_CK(cudaMemset(ctx->d_row_ptr, 0, sizeof(int) * (static_cast<size_t>(rows) + 8)));
-    if ((rc = dalloc(&ctx->d_col, static_cast<size_t>(nnz) + 4))) return rc;
-    MEXK_CK(cudaMemset(ctx->d_col + nnz, 0, sizeof(int) * 4));  // the SpMV gathers whole 16-byte groups
-    if ((rc = dalloc(&ctx->d_val, static_cast<size_t>(nnz) + 4))) return rc;
-    MEXK_CK(cudaMemcpy(ctx->d_row_ptr, row_ptr, sizeof(int) * (rows + 1), cudaMemcpyHostToDevice));
+    int *d_rp = nullptr, *d_ci = nullptr;
+    double* d_va = nullptr;
+    int rc = context_csr_begin(ctx, rows, nnz, m_alloc_max, &d_rp, &d_ci, &d_va);
+    if (rc) return rc;
+    MEXK_CK(cudaMemcpy(d_rp, row_ptr, sizeof(int) * (rows + 1), cudaMemcpyHostToDevice));
     if (nnz > 0) {
-        MEXK_CK(cudaMemcpy(ctx->d_col, col_idx, sizeof(int) * nnz, cudaMemcpyHostToDevice));
-        MEXK_CK(cudaMemcpy(ctx->d_val, values, sizeof(double) * nnz, cudaMemcpyHostToDevice));
+        MEXK_CK(cudaMemcpy(d_ci, col_idx, sizeof(int) * nnz, cudaMemcpyHostToDevice));
+        MEXK_CK(cudaMemcpy(d_va, values, sizeof(double) * nnz, cudaMemcpyHostToDevice));
     }
-    const SpmvSchedule sched = build_spmv_schedule(rows, row_ptr, col_idx);
-    ctx->nblocks = static_cast<int>(sched.tiles.size()) - 1;
-    ctx->spmv_narrow = sched.all_narrow;
-    if ((rc = dalloc(&ctx->d_tiles, sched.tiles.size()))) return rc;
-    MEXK_CK(cudaMemcpy(ctx->d_tiles, sched.tiles.data(), sizeof(int4) * sched.tiles.size(), cudaMemcpyHostToDevice));
-    if ((rc = dalloc(&ctx->d_col16, sched.col16.size() + 8))) return rc;
-    if (!sched.col16.empty())
-        MEXK_CK(cudaMemcpy(ctx->d_col16, sched.col16.data(), sizeof(uint16_t) * sched.col16.size(),
-                           cudaMemcpyHostToDevice));
-    const size_t vcount = static_cast<size_t>(ctx->ldv) * (m_alloc_max + 1);
-    if ((rc = dalloc(&ctx->d_V, vcount))) return rc;
-    MEXK_CK(cudaMemset(ctx->d_V, 0, sizeof(double) * vcount));
-    if ((rc = dalloc(&ctx->d_w, ctx->ldv))) return rc;
-    if ((rc = dalloc(&ctx->d_y, ctx->ldv))) return rc;
-    MEXK_CK(cudaMemset(ctx->d_w, 0, sizeof(double) * ctx->ldv));
-    MEXK_CK(cudaMemset(ctx->d_y, 0, sizeof(double) * ctx->ldv));
-    const size_t hcount = static_cast<size_t>(ctx->ldh) * m_alloc_max;
-    if ((rc = dalloc(&ctx->d_H, hcount))) return rc;
-    MEXK_CK(cudaMemset(ctx->d_H, 0, sizeof(double) * hcount));
-    if ((rc = dalloc(&ctx->d_h1, MEXK_M_MAX + 2))) return rc;
-    if ((rc = dalloc(&ctx->d_h2, MEXK_M_MAX + 2))) return rc;
-    if ((rc = dalloc(&ctx->d_coef, MEXK_M_MAX + 2))) return rc;
-    if ((rc = dalloc(&ctx->d_cand, static_cast<size_t>(SEARCH_CAND) * CAND_STRIDE))) return rc;
-    if ((rc = dalloc(&ctx->d_partials, static_cast<size_t>(PARTIAL_BLOCKS) * RED_STRIDE))) return rc;
-    if ((rc = dalloc(&ctx->d_counter, 4))) return rc;
-    MEXK_CK(cudaMemset(ctx->d_counter, 0, sizeof(unsigned int) * 4));
-    if ((rc = dalloc(&ctx->d_state, 1))) return rc;
-    if ((rc = dalloc(&ctx->d_log, LOG_CAP))) return rc;
-    cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&ctx->h_state), sizeof(DevState));
-    if (e != cudaSuccess) {
-        set_cuda_error(e, "cudaMallocHost", __FILE__, __LINE__);
-        return MEXK_ERR_ALLOC;
-    }
-    memset(ctx->h_state, 0, sizeof(DevState));
-    MEXK_CK(cudaMemcpy(ctx->d_state, ctx->h_state, sizeof(DevState), cudaMemcpyHostToDevice));
-    ctx->uploaded = true;
-    return MEXK_OK;
+    return context_csr_finish(ctx, row_ptr);
 }
 
 int mexk_context_destroy(mexk_context_t ctx) {

@@ -247,38 +247,89 @@ __device__ __forceinline__ void smem_quad<double, double>(const double* p, doubl
     o[3] = t1.y;
 }
 
-SpmvSchedule build_spmv_schedule(int n, const int* row_ptr, const int* col_idx) {
-    SpmvSchedule s;
-    const std::vector<int> blocks = build_row_blocks(n, row_ptr, ST_TILE, ST_ROWS);
-    s.tiles.resize(blocks.size());
-    for (size_t b = 0; b + 1 < blocks.size(); ++b) {
-        const int r0 = blocks[b], r1 = blocks[b + 1];
-        const int e0 = row_ptr[r0], e1 = row_ptr[r1];
-        int off = -1, cbase = 0;
-        if (e1 - e0 <= ST_TILE) {
-            int lo = e1 > e0 ? col_idx[e0] : 0, hi = lo;
-            for (int e = e0 + 1; e < e1; ++e) {
-                lo = std::min(lo, col_idx[e]);
-                hi = std::max(hi, col_idx[e]);
-            }
-            if (static_cast<long long>(hi) - lo <= 65535) {
-                // positions e - base of the row block's 16-byte groups, 8 per 16 bytes
-                const int base = e0 & ~3;
-                const int nq = (e1 - base + 3) >> 2;
-                const size_t len = (static_cast<size_t>(4 * nq) + 7) & ~static_cast<size_t>(7);
-                if (s.col16.size() + len <= static_cast<size_t>(INT_MAX)) {
-                    off = static_cast<int>(s.col16.size());
-                    cbase = lo;
-                    s.col16.resize(s.col16.size() + len, 0);
-                    for (int e = e0; e < e1; ++e) s.col16[off + (e - base)] = static_cast<uint16_t>(col_idx[e] - lo);
-                }
-            }
-        }
-        s.tiles[b] = make_int4(r0, e0, off, cbase);
-        if (e1 - e0 <= ST_TILE && off < 0) s.all_narrow = false;
+// One warp per staged row block: the span of its columns; when it is at most
+// 65536, the columns minus their minimum go to the block's slot of col16 (at
+// the positions e - (first nonzero rounded down to 4) of its 16-byte groups;
+// the slot was zeroed), else the block keeps 32-bit columns (z = -1).
+__global__ void narrow_columns_kernel(int nblocks, int4* __restrict__ tiles, const int* __restrict__ col_idx,
+                                      uint16_t* __restrict__ col16, int* __restrict__ all_narrow) {
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (b >= nblocks) return;
+    const int4 t = tiles[b];
+    if (t.z < 0) return;  // one long row: streamed directly
+    const int e0 = t.y, e1 = tiles[b + 1].y;
+    int lo = INT_MAX, hi = INT_MIN;
+    for (int e = e0 + lane; e < e1; e += 32) {
+        const int c = col_idx[e];
+        lo = min(lo, c);
+        hi = max(hi, c);
     }
-    s.tiles.back() = make_int4(n, row_ptr[n], -1, 0);
-    return s;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (e1 == e0) lo = hi = 0;
+    if (static_cast<long long>(hi) - lo > 65535) {
+        if (lane == 0) {
+            tiles[b].z = -1;
+            atomicAnd(all_narrow, 0);
+        }
+        return;
+    }
+    const int base = e0 & ~3;
+    for (int e = e0 + lane; e < e1; e += 32) col16[t.z + (e - base)] = static_cast<uint16_t>(col_idx[e] - lo);
+    if (lane == 0) tiles[b].w = lo;
+}
+
+int build_spmv_schedule(int n, const int* row_ptr, const int* d_col, SpmvSchedule* out, cudaStream_t s) {
+    const std::vector<int> blocks = build_row_blocks(n, row_ptr, ST_TILE, ST_ROWS);
+    const int nb = static_cast<int>(blocks.size()) - 1;
+    std::vector<int4> tiles(blocks.size());
+    size_t slots = 0;
+    for (int b = 0; b < nb; ++b) {
+        const int r0 = blocks[b], e0 = row_ptr[r0], e1 = row_ptr[blocks[b + 1]];
+        int off = -1;
+        if (e1 - e0 <= ST_TILE) {
+            const int base = e0 & ~3;
+            const size_t nq = static_cast<size_t>(e1 - base + 3) >> 2;
+            if (slots + 4 * nq + 8 > static_cast<size_t>(INT_MAX)) return MEXK_ERR_UNSUPPORTED;
+            off = static_cast<int>(slots);
+            slots += (4 * nq + 7) & ~static_cast<size_t>(7);
+        }
+        tiles[b] = make_int4(r0, e0, off, 0);
+    }
+    tiles[nb] = make_int4(n, row_ptr[n], -1, 0);
+    out->nblocks = nb;
+    out->all_narrow = true;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&out->d_tiles), sizeof(int4) * tiles.size());
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&out->d_col16), sizeof(uint16_t) * (slots + 8));
+    int* d_flag = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&d_flag), sizeof(int));
+    if (e != cudaSuccess) {
+        cudaFree(d_flag);
+        set_cuda_error(e, "cudaMalloc", __FILE__, __LINE__);
+        return MEXK_ERR_ALLOC;
+    }
+    const int one = 1;
+    int flag = 1;
+    e = cudaMemcpyAsync(out->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(out->d_col16, 0, sizeof(uint16_t) * (slots + 8), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_flag, &one, sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nb > 0) {
+        narrow_columns_kernel<<<(nb + 7) / 8, 256, 0, s>>>(nb, out->d_tiles, d_col, out->d_col16, d_flag);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_flag);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "SpMV schedule", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
+    out->all_narrow = flag != 0;
+    return MEXK_OK;
 }
 
 // Context form. tiles[b] = {first row, first nonzero, offset of its 16-bit

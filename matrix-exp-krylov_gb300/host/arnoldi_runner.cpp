@@ -103,14 +103,10 @@ ArnoldiRunner::ArnoldiRunner(int n_gpus, const ArnoldiParams& arnoldi_params, in
     ts_params.m_step = 0;
 }
 
-void ArnoldiRunner::init_all_devices(const std::vector<CSRHost>& partitions, const std::vector<int>& device_ids,
-                                     const std::vector<CSRHost::GhostMap>& ghost_maps_in) {
-    ghost_maps = ghost_maps_in;
-    if (static_cast<int>(device_ids.size()) != num_gpus) {
-        std::cerr << "ERROR: device_ids size (" << device_ids.size() << ") must match num_gpus (" << num_gpus << ")"
-                  << std::endl;
-        std::exit(EXIT_FAILURE);
-    }
+namespace {
+
+// The checks init_all_devices makes before any allocation (main.cu:1308-1330).
+void check_runner_shape(const ArnoldiParams& params, int global_rows, int global_cols) {
     if (params.m >= global_rows) {
         std::cerr << "ERROR: Requested Arnoldi m=" << params.m << " must be less than global_rows=" << global_rows
                   << std::endl;
@@ -125,6 +121,31 @@ void ArnoldiRunner::init_all_devices(const std::vector<CSRHost>& partitions, con
                   << std::endl;
         std::exit(EXIT_FAILURE);
     }
+}
+
+}  // namespace
+
+void ArnoldiRunner::init_from_context(mexk_context_t ctx, int device_id) {
+    check_runner_shape(params, global_rows, global_cols);
+    DeviceContext& dc = device_contexts[0];
+    dc.device_id = device_id;
+    dc.handle = ctx;
+    dc.local_rows = global_rows;
+    dc.local_nnz = static_cast<int>(global_nnz);
+    dc.allocated_m_max = std::max(params.m, ts_params.m_max > 0 ? ts_params.m_max : params.m);
+    std::cout << "GPU " << dc.device_id << " allocating: local_rows=" << dc.local_rows
+              << ", local_nnz=" << dc.local_nnz << std::endl;
+}
+
+void ArnoldiRunner::init_all_devices(const std::vector<CSRHost>& partitions, const std::vector<int>& device_ids,
+                                     const std::vector<CSRHost::GhostMap>& ghost_maps_in) {
+    ghost_maps = ghost_maps_in;
+    if (static_cast<int>(device_ids.size()) != num_gpus) {
+        std::cerr << "ERROR: device_ids size (" << device_ids.size() << ") must match num_gpus (" << num_gpus << ")"
+                  << std::endl;
+        std::exit(EXIT_FAILURE);
+    }
+    check_runner_shape(params, global_rows, global_cols);
     // Row partitions hold global column indices: stacking them restores A.
     CSRHost full;
     full.rows = 0;

@@ -6,8 +6,12 @@
 // one GPU. Extra flags: --precision fp64|mixed (default fp64, the
 // reference's arithmetic), --controller reference|search|learned (default
 // the reference's heuristic), --window W (mixed precision, symmetric A:
-// orthogonalise against the last W basis vectors) and --quiet (no
-// [STEP]/[FLOPs] lines).
+// orthogonalise against the last W basis vectors), --quiet (no
+// [STEP]/[FLOPs] lines) and --host-load. A .bincsr input is loaded straight
+// into the device context (mexk_context_load_bincsr: mapped, streamed,
+// checked on the device) with the host loader's output and messages;
+// --host-load, symmetric_upper files and non-square matrices take the host
+// loader (CSRHost::from_binary_csr).
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -49,6 +53,7 @@ int main(int argc, char* argv[]) {
     int controller = MEXK_CTRL_REFERENCE;
     int window = 0;
     bool quiet = false;
+    bool host_load = false;
 
     std::vector<std::string> args(argv + 1, argv + argc);
     size_t pos = 0;
@@ -95,6 +100,10 @@ int main(int argc, char* argv[]) {
             quiet = true;
             continue;
         }
+        if (a == "--host-load") {
+            host_load = true;
+            continue;
+        }
         if (pos == 0) {
             if (a.find('.') != std::string::npos || a.find('/') != std::string::npos ||
                 a.rfind(".mtx") != std::string::npos) {
@@ -130,13 +139,40 @@ int main(int argc, char* argv[]) {
     const int gpus_used = 1;  // single-device build: one partition
 
     CSRHost A;
+    mexk_context_t loaded_ctx = nullptr;  // .bincsr loaded straight into the device context
+    double loaded_max_abs = 0.0;
     if (use_file) {
         std::cout << "Loading matrix from file: " << matrix_file << std::endl;
         const bool is_bin = ends_with(matrix_file, ".bincsr");
         const bool is_mtx = ends_with(matrix_file, ".mtx") || ends_with(matrix_file, ".mtx.gz");
         bool loaded = false;
         if (is_bin || has_bincsr_magic(matrix_file)) {
-            A.from_binary_csr(matrix_file);
+            mexk_bincsr_info_t info{};
+            const bool direct = !host_load && mexk_bincsr_probe(matrix_file.c_str(), &info) == MEXK_OK &&
+                                (info.flags & 4u) == 0 && info.rows == info.cols && info.rows > 1;
+            if (direct) {
+                const int rows = static_cast<int>(info.rows);
+                int m_alloc = m_param > 0 ? m_param : std::min(30, std::max(5, rows - 1));
+                m_alloc = std::max(1, std::min(std::min(m_alloc, rows - 1), MEXK_M_MAX));
+                int rc = mexk_context_create(0, &loaded_ctx);
+                if (rc == MEXK_OK) rc = mexk_context_load_bincsr(loaded_ctx, matrix_file.c_str(), m_alloc, &info);
+                if (info.checks_passed >= 3)  // the host loader prints this line before the row checks
+                    std::cout << "Binary CSR header: version=1 flags=0x" << std::hex << info.flags << std::dec
+                              << " index_dtype=" << (info.index_dtype == 1 ? "u32" : "u64")
+                              << " value_dtype=" << (info.value_dtype == 1 ? "f32" : "f64")
+                              << " symmetric_upper=no" << std::endl;
+                if (rc != MEXK_OK) {
+                    std::cerr << mexk_last_error_detail() << std::endl;
+                    if (loaded_ctx) mexk_context_destroy(loaded_ctx);
+                    return EXIT_FAILURE;
+                }
+                A.rows = rows;
+                A.cols = static_cast<int>(info.cols);
+                A.nnz = info.nnz;
+                loaded_max_abs = info.max_abs;
+            } else {
+                A.from_binary_csr(matrix_file);
+            }
             loaded = true;
             std::cout << "Detected Binary CSR v1 input" << std::endl;
         } else if (is_mtx) {
@@ -168,7 +204,7 @@ int main(int argc, char* argv[]) {
     }
 
     // t clamp: keep t*max|A_ij| <= 10 (main.cu:2227-2242).
-    double max_abs = 0.0;
+    double max_abs = loaded_max_abs;
     for (double v : A.values) max_abs = std::max(max_abs, std::abs(v));
     if (max_abs <= 0.0) max_abs = 1.0;
     double t_safe = t_cli;
@@ -179,11 +215,14 @@ int main(int argc, char* argv[]) {
         t_safe = t_limit;
     }
 
-    std::vector<CSRHost> parts = A.partition_rows(gpus_used);
-    std::cout << "Partitioned matrix across " << gpus_used << " GPUs" << std::endl;
+    std::vector<CSRHost> parts;
     std::vector<CSRHost::GhostMap> ghosts(gpus_used);
-    for (int i = 0; i < gpus_used; ++i) ghosts[i] = A.build_owner_ghost_maps(parts, i, gpus_used);
-    validate_ghost_maps(ghosts, gpus_used);
+    if (!loaded_ctx) {
+        parts = A.partition_rows(gpus_used);
+        for (int i = 0; i < gpus_used; ++i) ghosts[i] = A.build_owner_ghost_maps(parts, i, gpus_used);
+    }
+    std::cout << "Partitioned matrix across " << gpus_used << " GPUs" << std::endl;
+    if (!loaded_ctx) validate_ghost_maps(ghosts, gpus_used);
 
     int m_val = m_param;
     if (m_val <= 0) m_val = std::min(30, std::max(5, A.rows - 1));
@@ -197,7 +236,10 @@ int main(int argc, char* argv[]) {
     runner.controller = controller;
     runner.ortho_window = window;
     runner.verbose = !quiet;
-    runner.init_all_devices(parts, std::vector<int>{0}, ghosts);
+    if (loaded_ctx)
+        runner.init_from_context(loaded_ctx, 0);
+    else
+        runner.init_all_devices(parts, std::vector<int>{0}, ghosts);
     std::vector<double> v(static_cast<size_t>(A.rows), 0.1);
     std::vector<double> y(static_cast<size_t>(A.rows), 0.0);
     runner.compute_expmv(v, y);

@@ -50,6 +50,12 @@ class Step(C.Structure):
                 ("accepts", C.c_int), ("rejects", C.c_int)]
 
 
+class BincsrInfo(C.Structure):
+    _fields_ = [("rows", C.c_longlong), ("cols", C.c_longlong), ("nnz", C.c_longlong), ("index_dtype", C.c_int),
+                ("value_dtype", C.c_int), ("flags", C.c_uint), ("checks_passed", C.c_int), ("max_abs", C.c_double),
+                ("seconds", C.c_double)]
+
+
 class BatchParams(C.Structure):
     _fields_ = [("m", C.c_int), ("tol", C.c_double), ("max_restarts", C.c_int), ("reorthogonalize", C.c_int),
                 ("basis_bytes", C.c_longlong), ("autotune", C.c_int)]
@@ -112,6 +118,8 @@ _PROTOS = {
     "mexk_mlp_adam_step": ([_VP, _VP, _VP, _VP, _VP, C.c_int, C.c_int, C.c_float, _VP, _VP, _VP], C.c_int),
     "mexk_controller_predict": ([_VP, _VP, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_double, _VP, _VP], C.c_int),
+    "mexk_bincsr_probe": ([C.c_char_p, C.POINTER(BincsrInfo)], C.c_int),
+    "mexk_context_load_bincsr": ([_VP, C.c_char_p, C.c_int, C.POINTER(BincsrInfo)], C.c_int),
 }
 
 KERNELS = {"spmv": 0, "gs_dot": 1, "gs_upd_dot": 2, "gs_upd_norm": 3, "normalize": 4, "lift": 5, "controller": 6,

@@ -9,6 +9,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -41,6 +42,8 @@ class Context:
         self._h = C.c_void_p()
         self._net_loaded = False
         check(lib().mexk_context_create(device, C.byref(self._h)), "mexk_context_create")
+        if A is None:  # filled by from_bincsr
+            return
         self.n = int(A.n)
         self.nnz = int(A.nnz)
         self.m_alloc = int(m_alloc)
@@ -53,6 +56,25 @@ class Context:
         except Exception:
             self.close()
             raise
+
+    @classmethod
+    def from_bincsr(cls, path, m_alloc: int = 30, device: int = 0):
+        """A context loaded straight from a Binary CSR v1 file
+        (mexk_context_load_bincsr); .load_info holds the header fields,
+        max |a_ij| and the load's wall time."""
+        from ._lib import BincsrInfo
+
+        ctx = cls(None, m_alloc, device)
+        info = BincsrInfo()
+        try:
+            check(lib().mexk_context_load_bincsr(ctx._h, os.fsencode(str(path)), int(m_alloc), C.byref(info)),
+                  "mexk_context_load_bincsr")
+        except Exception:
+            ctx.close()
+            raise
+        ctx.n, ctx.nnz, ctx.m_alloc = int(info.rows), int(info.nnz), int(m_alloc)
+        ctx.load_info = {f: getattr(info, f) for f, _ in info._fields_}
+        return ctx
 
     @property
     def handle(self):

@@ -52,7 +52,8 @@ def test_struct_layouts_match_header(tmp_path):
     """ctypes mirrors of the header structs: sizes and offsets equal what a C
     compiler sees in include/mexk.h."""
     src = tmp_path / "layout.c"
-    fields = {"mexk_params_t": _lib.Params, "mexk_result_t": _lib.Result, "mexk_step_t": _lib.Step}
+    fields = {"mexk_params_t": _lib.Params, "mexk_result_t": _lib.Result, "mexk_step_t": _lib.Step,
+              "mexk_bincsr_info_t": _lib.BincsrInfo}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "mexk.h"', "int main(void) {"]
     for cname, py in fields.items():
         lines.append(f'printf("%zu\\n", sizeof({cname}));')

@@ -184,3 +184,38 @@ def test_loader_matches_reference_loader(tmp_path, oracle_mod):
         rc, out, csr = load(path, tmp_path)
         assert rc == 0
         assert np.array_equal(csr[0], rp) and np.array_equal(csr[1], ci) and np.array_equal(csr[2], va)
+
+
+# ------------------------------------------------------------------ header probe (C ABI, no GPU)
+HEADER_BAD = [b for b in BAD if b[0] in ("too small", "magic", "version", "index dtype", "value dtype", "reserved",
+                                         "int32", "size")]
+
+
+@pytest.mark.parametrize("name,data,msg", HEADER_BAD, ids=[b[0] for b in HEADER_BAD])
+def test_bincsr_probe_rejects(tmp_path, name, data, msg):
+    """mexk_bincsr_probe: the header checks of the host loader, its messages."""
+    import ctypes as C
+
+    from mexk._lib import BincsrInfo, lib
+
+    p = tmp_path / "bad.bincsr"
+    p.write_bytes(data)
+    info = BincsrInfo()
+    assert lib().mexk_bincsr_probe(str(p).encode(), C.byref(info)) == 1
+    assert msg in lib().mexk_last_error_detail().decode()
+
+
+def test_bincsr_probe_reads_header(tmp_path):
+    import ctypes as C
+
+    from mexk._lib import BincsrInfo, lib
+
+    A = small_matrix()
+    p = tmp_path / "a.bincsr"
+    B.write_bincsr(p, A.row_ptr, A.col_idx, A.values, index_dtype="u64", value_dtype="f32", flags=B.FLAG_SORTED)
+    info = BincsrInfo()
+    assert lib().mexk_bincsr_probe(str(p).encode(), C.byref(info)) == 0
+    assert (info.rows, info.cols, info.nnz) == (A.n, A.n, A.nnz)
+    assert (info.index_dtype, info.value_dtype, info.flags, info.checks_passed) == (2, 1, 1, 1)
+    assert lib().mexk_bincsr_probe(str(tmp_path / "missing.bincsr").encode(), C.byref(info)) == 1
+    assert "Could not open binary CSR file" in lib().mexk_last_error_detail().decode()
