@@ -716,6 +716,58 @@ def run_solve_once(local_rank, grid=2048):
             print(prec, ctrl, window, res, flush=True)
 
 
+def run_load(args):
+    """The .bincsr load path: the heat2048 matrix (u32 indices, f64 values, as
+    the reference's generator writes it) and the config-2 power-law matrix
+    (u32, f32 values), written to a temporary directory (so read from the
+    page cache), loaded by the host loader + upload (CSRHost::from_binary_csr
+    then mexk_context_upload_csr, timed by csr_tool --time) and straight into
+    a context (mexk_context_load_bincsr). Best of `steps` loads each."""
+    import shutil
+    import subprocess
+    import tempfile
+
+    from mexk import bincsr as B
+    from mexk import synthetic as S
+    from mexk._lib import BUILD
+    from mexk.api import Context
+
+    tool = os.path.join(BUILD, "csr_tool")
+    tmp = tempfile.mkdtemp(prefix="mexk_load_")
+    out = {}
+    try:
+        for name, make, idt, vdt in (("heat2048", lambda: S.laplacian_2d(2048), "u32", "f64"),
+                                     ("powerlaw_cfg2", lambda: S.config2().A, "u32", "f32")):
+            A = make()
+            path = os.path.join(tmp, name + ".bincsr")
+            B.write_bincsr(path, A.row_ptr, A.col_idx, A.values, index_dtype=idt, value_dtype=vdt)
+            size = os.path.getsize(path)
+            del A
+            host, fast, fast_inner = [], [], []
+            for _ in range(max(1, args.steps)):
+                r = subprocess.run([tool, path, "--time"], capture_output=True, text=True, check=True)
+                kv = dict(x.split("=") for x in r.stdout.split() if "=" in x)
+                host.append((float(kv["host_load_s"]), float(kv["upload_s"])))
+                t0 = time.perf_counter()
+                with Context.from_bincsr(path, m_alloc=30) as ctx:
+                    fast_inner.append(ctx.load_info["seconds"])
+                fast.append(time.perf_counter() - t0)
+            h = min(host, key=lambda x: x[0] + x[1])
+            out[name] = {"file_bytes": size, "index_dtype": idt, "value_dtype": vdt,
+                         "host_loader_s": round(h[0], 4), "host_upload_s": round(h[1], 4),
+                         "host_total_s": round(h[0] + h[1], 4),
+                         "direct_s": round(min(fast_inner), 4), "direct_with_context_s": round(min(fast), 4),
+                         "direct_gbs": round(size / min(fast_inner) / 1e9, 2),
+                         "speedup": round((h[0] + h[1]) / min(fast_inner), 1)}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    h = out["heat2048"]
+    print(json.dumps({"metric": "bincsr load GB/s (file bytes / wall s, page-cache resident)",
+                      "value": h["direct_gbs"], "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+                      "higher_is_better": True, "data": "synthetic", "config": {"workload": "load"},
+                      "files": out, "host_cores": os.cpu_count()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -727,7 +779,8 @@ def main():
     ap.add_argument("--window", type=int, default=0, help="with --precision: short-recurrence window (0 = Arnoldi)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--solve-once", action="store_true", help="one untimed FP64 + mixed solve (for ncu)")
-    ap.add_argument("--workload", default="heat2048", choices=["heat2048", "batch", "convdiff", "powerlaw"])
+    ap.add_argument("--workload", default="heat2048",
+                    choices=["heat2048", "batch", "convdiff", "powerlaw", "load"])
     ap.add_argument("--problems", type=int, default=256, help="batch workload: number of problems")
     ap.add_argument("--sample", type=int, default=8, help="batch workload: problems in the serial FP64 sample")
     ap.add_argument("--grid", type=int, default=2048, help="--solve-once: heat-equation grid size")
@@ -747,6 +800,9 @@ def main():
         return
     if args.workload == "powerlaw" and args.impl == "ours":
         run_powerlaw(args)
+        return
+    if args.workload == "load" and args.impl == "ours":
+        run_load(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

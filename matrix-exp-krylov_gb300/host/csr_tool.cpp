@@ -2,6 +2,10 @@
 // program does (format detection, validation, exit codes) and writes the
 // resulting CSR arrays as raw little-endian files <out>.rowptr (int32),
 // <out>.col (int32) and <out>.val (float64). Used by the loader tests.
+// csr_tool MATRIX --time instead times the host loader and the upload of its
+// CSR into a device context (mexk_context_upload_csr, m = 30):
+// "host_load_s=... upload_s=...".
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -20,6 +24,7 @@ int main(int argc, char** argv) {
         return 2;
     }
     const std::string path = argv[1], out = argv[2];
+    const auto t0 = std::chrono::steady_clock::now();
     CSRHost A;
     std::ifstream f(path, std::ios::binary);
     unsigned char h[8] = {0};
@@ -31,6 +36,22 @@ int main(int argc, char** argv) {
     else {
         std::cerr << "Error: Could not detect matrix format for file " << path << std::endl;
         return 1;
+    }
+    if (out == "--time") {
+        const auto t1 = std::chrono::steady_clock::now();
+        mexk_context_t ctx = nullptr;
+        int rc = mexk_context_create(0, &ctx);
+        if (rc == MEXK_OK)
+            rc = mexk_context_upload_csr(ctx, A.rows, A.nnz, A.row_ptr.data(), A.col_idx.data(), A.values.data(), 30);
+        const auto t2 = std::chrono::steady_clock::now();
+        if (ctx) mexk_context_destroy(ctx);
+        if (rc != MEXK_OK) {
+            std::cerr << "upload failed: " << mexk_last_error_detail() << std::endl;
+            return 1;
+        }
+        std::cout << "host_load_s=" << std::chrono::duration<double>(t1 - t0).count()
+                  << " upload_s=" << std::chrono::duration<double>(t2 - t1).count() << std::endl;
+        return 0;
     }
     std::ofstream(out + ".rowptr", std::ios::binary)
         .write(reinterpret_cast<const char*>(A.row_ptr.data()), sizeof(int) * A.row_ptr.size());
