@@ -24,11 +24,14 @@
 
 #include <math.h>
 
+#include <cooperative_groups.h>
+
 namespace mexk {
 
 namespace {
 
 constexpr int EXPM_THREADS = 512;
+constexpr int SEARCH_CLUSTER = 4;  // thread blocks (SMs) per candidate exponential: 32 x 4 of the 152 SMs
 
 // FP64 adds and FMAs take about 64 cycles of latency on this GPU (FP32: 4),
 // and these k <= 64 matrices leave most of the block idle, so every dot
@@ -293,6 +296,51 @@ __constant__ double kInvFact[19] = {
     1.0 / fact_d(10), 1.0 / fact_d(11), 1.0 / fact_d(12), 1.0 / fact_d(13), 1.0 / fact_d(14),
     1.0 / fact_d(15), 1.0 / fact_d(16), 1.0 / fact_d(17), 1.0 / fact_d(18)};
 
+// Who computes the k x k products of the Taylor chain. BlockProducts: this
+// thread block, all columns. ClusterProducts: the thread blocks of a cluster,
+// each holding full copies of the matrices, compute a share of every
+// product's columns and write it into every block's copy (distributed shared
+// memory), then a cluster barrier. GB300 executes about 2 FP64 FMAs per clock
+// per SM, so a 31 x 31 product takes ~7 us on one SM; a cluster of 4 spreads
+// it over 4 SMs with the same arithmetic (each element one dot_k).
+struct BlockProducts {
+    int k;
+    __device__ void cols(int* j0, int* j1) const {
+        *j0 = 0;
+        *j1 = k;
+    }
+    __device__ void put(double* Z, int idx, double v) const { Z[idx] = v; }
+    __device__ void sync() const { __syncthreads(); }
+};
+struct ClusterProducts {
+    int k;
+    __device__ void cols(int* j0, int* j1) const {
+        const cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+        const int r = static_cast<int>(cl.block_rank()), c = static_cast<int>(cl.num_blocks());
+        *j0 = r * k / c;
+        *j1 = (r + 1) * k / c;
+    }
+    __device__ void put(double* Z, int idx, double v) const {
+        const cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+        const unsigned c = cl.num_blocks();
+        for (unsigned p = 0; p < c; ++p) cl.map_shared_rank(Z, p)[idx] = v;
+    }
+    __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
+};
+
+// Z = X Y (k x k), columns shared out as P says.
+template <typename P>
+__device__ void mm_p(const P& pr, int k, const double* X, const double* Y, double* Z) {
+    int j0, j1;
+    pr.cols(&j0, &j1);
+    const int cnt = k * (j1 - j0);
+    for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+        const int i = e % k, j = j0 + e / k;
+        pr.put(Z, i + j * k, dot_k(k, X + i, k, Y + j * k));
+    }
+    pr.sync();
+}
+
 // exp of the k-by-k matrix in B.A (ld k) by the degree-18 Taylor polynomial
 // with scaling and squaring: X = A / 2^s with |X|_1 <= 1, so the truncated
 // terms sum to at most sum_{i>18} 1/i! < 8.5e-18 (below double rounding);
@@ -300,9 +348,11 @@ __constant__ double kInvFact[19] = {
 // in X^4 (7 products, no linear solve), then s squarings. A product-only
 // chain suits this GPU's FP64 latency far better than the Pade solve; the
 // candidate-step controller uses it (the reference controller keeps Pade,
-// as the reference does). Returns the buffer holding the result; all
-// threads of the block must call it.
-__device__ double* expm_taylor_block(const ExpmBuf& B, int k) {
+// as the reference does). Returns the buffer holding the result; every
+// thread of the block (of every block of the cluster) must call it, with
+// the same B.A.
+template <typename P>
+__device__ double* expm_taylor(const ExpmBuf& B, int k, const P& pr) {
     __shared__ int s_sq;
     if (threadIdx.x < k) B.red[threadIdx.x] = col_abs_sum(k, B.A, threadIdx.x);
     __syncthreads();
@@ -324,17 +374,18 @@ __device__ double* expm_taylor_block(const ExpmBuf& B, int k) {
     const int kk = k * k;
     if (sq > 0) {
         for (int e = threadIdx.x; e < kk; e += blockDim.x) B.A[e] = ldexp(B.A[e], -sq);
-        __syncthreads();
     }
+    // every block's copy of X must be final before a product writes into it
+    pr.sync();
     const double* X = B.A;
     double* X2 = B.A2;
     double* X3 = B.A4;
     double* X4 = B.A6;
-    mm(k, X, X, X2);
-    mm(k, X2, X, X3);
-    mm(k, X2, X2, X4);
+    mm_p(pr, k, X, X, X2);
+    mm_p(pr, k, X2, X, X3);
+    mm_p(pr, k, X2, X2, X4);
     const double* c = kInvFact;
-    // Z = c16 I + c17 X + c18 X^2
+    // Z = c16 I + c17 X + c18 X^2 (every block its full copy)
     double* Z = B.T;
     double* W = B.U;
     for (int e = threadIdx.x; e < kk; e += blockDim.x) {
@@ -342,28 +393,34 @@ __device__ double* expm_taylor_block(const ExpmBuf& B, int k) {
         if ((e % k) == (e / k)) z = z + c[16];
         Z[e] = z;
     }
-    __syncthreads();
+    pr.sync();
     // Z = B_q + X^4 Z, B_q = c_{4q} I + c_{4q+1} X + c_{4q+2} X^2 + c_{4q+3} X^3
+    int j0, j1;
+    pr.cols(&j0, &j1);
+    const int cnt = k * (j1 - j0);
     for (int q = 3; q >= 0; --q) {
-        for (int e = threadIdx.x; e < kk; e += blockDim.x) {
-            const int i = e % k, j = e / k;
-            double b = c[4 * q + 1] * X[e] + c[4 * q + 2] * X2[e] + c[4 * q + 3] * X3[e];
+        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+            const int i = e % k, j = j0 + e / k;
+            const int idx = i + j * k;
+            double b = c[4 * q + 1] * X[idx] + c[4 * q + 2] * X2[idx] + c[4 * q + 3] * X3[idx];
             if (i == j) b = b + c[4 * q];
-            W[e] = dot_k(k, X4 + i, k, Z + j * k) + b;
+            pr.put(W, idx, dot_k(k, X4 + i, k, Z + j * k) + b);
         }
-        __syncthreads();
+        pr.sync();
         double* t = Z;
         Z = W;
         W = t;
     }
     for (int r = 0; r < sq; ++r) {
-        mm(k, Z, Z, W);
+        mm_p(pr, k, Z, Z, W);
         double* t = Z;
         Z = W;
         W = t;
     }
     return Z;
 }
+
+__device__ double* expm_taylor_block(const ExpmBuf& B, int k) { return expm_taylor(B, k, BlockProducts{k}); }
 
 __device__ ExpmBuf carve(double* smem, int k) {
     ExpmBuf B;
@@ -576,11 +633,12 @@ __device__ void write_log(DevState* st, mexk_step_t* log, double dt, double err,
 }
 
 // Candidate steps tau_g = center * 2^((g - 24)/4), g = 0..31 (1/64 .. 3.4 x the
-// centre), each clamped to the remaining time. Every block evaluates one
-// candidate's exponential and residual estimate; the last block to finish
+// centre), each clamped to the remaining time. Every cluster of
+// SEARCH_CLUSTER blocks evaluates one candidate's exponential (the products
+// shared out over its SMs) and residual estimate; the last block to finish
 // takes the largest passing step (its exponential is reused for the lift),
 // or, if none passes, continues below the smallest candidate with the
-// reference's shrink rule.
+// reference's shrink rule (on its own).
 __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchArgs a, int m) {
     extern __shared__ double smem[];
     __shared__ int s_k, s_bd, s_flag, s_best, s_dec, s_mnext;
@@ -626,7 +684,8 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         // prediction (2^-1 .. 2^0.875), 16..31 on the quarter-octave grid the
         // search uses around twice the previous step (2^-4 .. 2^-0.25 of it),
         // so a poor prediction degrades to a coarser search.
-        const int g = static_cast<int>(blockIdx.x);
+        const int g = static_cast<int>(blockIdx.x) / SEARCH_CLUSTER;
+        const bool lead = blockIdx.x % SEARCH_CLUSTER == 0;
         double tau;
         if (a.mlp != nullptr && g < SEARCH_CAND / 2) {
             tau = s_center * exp2(0.125 * (g - 8));
@@ -639,10 +698,11 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         tau = tau < rem ? tau : rem;
         for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = tau * a.H[(e % k) + (e / k) * ldh];
         __syncthreads();
-        double* R = expm_taylor_block(B, k);
-        double* c = a.cand + static_cast<size_t>(blockIdx.x) * CAND_STRIDE;
-        for (int i = threadIdx.x; i < k; i += blockDim.x) c[2 + i] = R[i];
-        if (threadIdx.x == 0) {
+        double* R = expm_taylor(B, k, ClusterProducts{k});
+        double* c = a.cand + static_cast<size_t>(g) * CAND_STRIDE;
+        if (lead)
+            for (int i = threadIdx.x; i < k; i += blockDim.x) c[2 + i] = R[i];
+        if (lead && threadIdx.x == 0) {
             c[0] = bd ? 0.0 : fabs(a.H[k + (k - 1) * ldh] * R[k - 1]) * st->v_norm;
             c[1] = tau;
         }
@@ -650,7 +710,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
     if (!grid_last_block(a.counter, &s_flag)) return;
     if (threadIdx.x == 0) {
         int best = -1;
-        for (int g = 0; g < static_cast<int>(gridDim.x); ++g) {
+        for (int g = 0; g < static_cast<int>(gridDim.x) / SEARCH_CLUSTER; ++g) {
             const double* c = a.cand + static_cast<size_t>(g) * CAND_STRIDE;
             if (__ldcg(&c[0]) <= tol_eff && (best < 0 || __ldcg(&c[1]) > __ldcg(&a.cand[best * CAND_STRIDE + 1])))
                 best = g;
@@ -712,8 +772,23 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
 }  // namespace
 
 int launch_controller_search(const SearchArgs& a, int m, cudaStream_t s) {
-    controller_search_kernel<<<SEARCH_CAND, EXPM_THREADS, expm_smem_bytes(m), s>>>(a, m);
-    MEXK_CK_LAUNCH("controller_search_kernel");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(SEARCH_CAND * SEARCH_CLUSTER);
+    cfg.blockDim = dim3(EXPM_THREADS);
+    cfg.dynamicSmemBytes = expm_smem_bytes(m);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = SEARCH_CLUSTER;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, controller_search_kernel, a, m);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "controller_search_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
     return MEXK_OK;
 }
 
