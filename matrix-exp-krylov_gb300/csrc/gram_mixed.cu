@@ -542,6 +542,61 @@ __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
     pdl_trigger();
 }
 
+// Sweep 2 of a step over at most two columns: u_{j+1} = psc * (wsc * w -
+// (cp u_{j-1} + cj u_j)), the products summed in the order of
+// gram_update_kernel (bit-identical), two rows per thread per iteration for
+// more loads in flight (the three vectors come from L2).
+__global__ void __launch_bounds__(GT, 4) gram_update2_kernel(GramArgs g) {
+    pdl_wait();
+    DevState* st = g.st;
+    if (st->breakdown || st->done) return;
+    const int j = g.j;
+    const bool two = g.lo < j;
+    const GramState* gs = g.gs;
+    const float cp = two ? gs->coef[g.lo] : 0.f, cj = gs->coef[j];
+    const float wsc = gs->wsc, psc = gs->psc;
+    const size_t ldv = static_cast<size_t>(g.ldv);
+    const float4* __restrict__ w4 = reinterpret_cast<const float4*>(g.w);
+    const float4* __restrict__ u4 = col4(g.V, ldv, j);
+    const float4* __restrict__ p4 = col4(g.V, ldv, two ? j - 1 : j);
+    float4* __restrict__ out = reinterpret_cast<float4*>(g.V + static_cast<size_t>(j + 1) * ldv);
+    const int n4 = (g.n + 3) / 4;
+    const int stride = gridDim.x * GT;
+    auto one = [&](const float4& x, const float4& u, const float4& v) {
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (two) {
+            s.x = fmaf(v.x, cp, s.x);
+            s.y = fmaf(v.y, cp, s.y);
+            s.z = fmaf(v.z, cp, s.z);
+            s.w = fmaf(v.w, cp, s.w);
+        }
+        s.x = fmaf(u.x, cj, s.x);
+        s.y = fmaf(u.y, cj, s.y);
+        s.z = fmaf(u.z, cj, s.z);
+        s.w = fmaf(u.w, cj, s.w);
+        float4 r;
+        r.x = fmaf(x.x, wsc, -s.x) * psc;
+        r.y = fmaf(x.y, wsc, -s.y) * psc;
+        r.z = fmaf(x.z, wsc, -s.z) * psc;
+        r.w = fmaf(x.w, wsc, -s.w) * psc;
+        return r;
+    };
+    int i = blockIdx.x * GT + threadIdx.x;
+    for (; i + stride < n4; i += 2 * stride) {
+        const float4 x0 = __ldg(w4 + i), x1 = __ldg(w4 + i + stride);
+        const float4 u0 = __ldg(u4 + i), u1 = __ldg(u4 + i + stride);
+        const float4 v0 = two ? __ldg(p4 + i) : u0, v1 = two ? __ldg(p4 + i + stride) : u1;
+        out[i] = one(x0, u0, v0);
+        out[i + stride] = one(x1, u1, v1);
+    }
+    if (i < n4) {
+        const float4 x0 = __ldg(w4 + i), u0 = __ldg(u4 + i);
+        const float4 v0 = two ? __ldg(p4 + i) : u0;
+        out[i] = one(x0, u0, v0);
+    }
+    pdl_trigger();
+}
+
 // |u_{j+1}|^2 by grid reduction; the last block sets H(j+1, j), s_{j+1} and
 // the breakdown flag (main.cu:1911).
 __global__ void __launch_bounds__(GT) gram_norm_kernel(GramArgs g) {
@@ -627,7 +682,9 @@ int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
 
 int launch_gram_update(const GramArgs& a, cudaStream_t s) {
     if (a.j < 0 || a.j >= MEXK_M_MAX || a.lo < 0 || a.lo > a.j) return MEXK_ERR_INVALID;
-    const cudaError_t e = launch_dependent(gram_update_kernel, row_blocks(a.n, 4), GT, 0, s, a);
+    const cudaError_t e = a.j + 1 - a.lo <= 2
+                              ? launch_dependent(gram_update2_kernel, row_blocks((a.n + 1) / 2, 4), GT, 0, s, a)
+                              : launch_dependent(gram_update_kernel, row_blocks(a.n, 4), GT, 0, s, a);
     if (e != cudaSuccess) {
         set_cuda_error(e, "gram_update_kernel", __FILE__, __LINE__);
         return MEXK_ERR_CUDA;
