@@ -117,6 +117,8 @@ def kernel_bytes(kind, n, nnz, k, fp32, window=0):
         k = min(k, window)
     if kind == "spmv":
         return nnz * (s + 4) + 4 * (n + 1) + 2 * n * s  # values+cols, row_ptr, x once, y
+    if kind == "spmv_dots":  # the SpMV, then u_{j-1} read for the dots (u_j is x)
+        return nnz * (s + 4) + 4 * (n + 1) + 3 * n * s
     if kind in ("gs_dot", "gram_dot"):
         return k * n * s + n * s  # V_k, w
     if kind in ("gs_upd_dot", "gs_upd_norm", "gram_update"):
@@ -139,6 +141,20 @@ def cgs2_step_bytes(n, k, fp32):
 
 STEP_KINDS = {"fp64": ["spmv", "gs_dot", "gs_upd_dot", "gs_upd_norm", "normalize"],
               "mixed": ["spmv", "gram_dot", "gram_update"]}
+
+
+def step_kinds(precision, j, window=0):
+    """Kernels of Arnoldi step j as a solve runs them: in mixed precision a
+    step j >= 1 over two columns (every step of a window of 2, step 1 of full
+    Arnoldi) takes its dot products from the SpMV (spmv_dots) and needs no
+    dot sweep."""
+    if precision == "mixed":
+        lo = max(0, j + 1 - window) if window else 0
+        if j >= 1 and j + 1 - lo <= 2:
+            return ["spmv_dots", "gram_update"]
+    return STEP_KINDS[precision]
+
+
 CYCLE_KINDS = {"fp64": ["controller", "lift"], "mixed": ["controller", "lift", "gram_norm"]}
 
 
@@ -146,33 +162,35 @@ def profile_cycle(ctx, m, n, nnz, precision, iters=2, window=0):
     """CUDA-event timing of every kernel kind of one Krylov cycle (the sweeps
     as the context's last solve ran them: with its window, if any)."""
     fp32 = precision == "mixed"
-    kinds = STEP_KINDS[precision]
     once = CYCLE_KINDS[precision]
-    per = {k: {"ms": 0.0, "bytes": 0.0, "launches": 0} for k in kinds + once}
+    per = {}
+
+    def add(kind, j, k):
+        ms = ctx.profile_kernel(kind, j, iters, precision)
+        p = per.setdefault(kind, {"ms": 0.0, "bytes": 0.0, "launches": 0})
+        p["ms"] += ms
+        p["bytes"] += kernel_bytes(kind, n, nnz, k, fp32, window)
+        p["launches"] += 1
+
     # The controller first: it runs on the Hessenberg matrix the last solve left.
     for kind in once:
-        ms = ctx.profile_kernel(kind, m - 1, iters, precision)
-        per[kind]["ms"] += ms
-        per[kind]["bytes"] += kernel_bytes(kind, n, nnz, m, fp32, window)
-        per[kind]["launches"] += 1
+        add(kind, m - 1, m)
     for j in range(m):
-        for kind in kinds:
-            ms = ctx.profile_kernel(kind, j, iters, precision)
-            per[kind]["ms"] += ms
-            per[kind]["bytes"] += kernel_bytes(kind, n, nnz, j + 1, fp32, window)
-            per[kind]["launches"] += 1
+        for kind in step_kinds(precision, j, window):
+            add(kind, j, j + 1)
     return per
 
 
-def launches_per_solve(ctx, precision, res, m):
-    """Kernels one solve launches: the start vector (2), then per cycle m steps
-    of (SpMV + sweeps) and the cycle's controller, lift and restart (+ the
-    mixed form's last-column norm). Cycle sizes come from the attempt log."""
-    per_step, per_cycle = (3, 4) if precision == "mixed" else (5, 3)
+def launches_per_solve(ctx, precision, res, m, window=0):
+    """Kernels one solve launches: the start vector (2), then per cycle its
+    steps (SpMV + sweeps, step_kinds) and the cycle's controller, lift and
+    restart (+ the mixed form's last-column norm). Cycle sizes come from the
+    attempt log."""
     sizes = [int(s[3]) for s in ctx.steps()]
     if len(sizes) != res["cycles"]:  # rejects reuse their cycle's basis
         sizes = [m] * res["cycles"]
-    return 2 + sum(per_step * k + per_cycle for k in sizes)
+    per_cycle = 4 if precision == "mixed" else 3
+    return 2 + sum(sum(len(step_kinds(precision, j, window)) for j in range(k)) + per_cycle for k in sizes)
 
 
 def gs_cgs2_equivalent(per, n, m, precision):
@@ -313,7 +331,7 @@ def run_ours(args, rank, world, local_rank):
             for _ in range(K):
                 res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), P.t, m, precision=precision,
                                        controller=controller, window=window)
-                launches += launches_per_solve(ctx, precision, res, m)
+                launches += launches_per_solve(ctx, precision, res, m, window)
             e1.record(stream)
             torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)

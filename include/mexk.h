@@ -327,7 +327,8 @@ int mexk_batch_destroy(mexk_batch_t b);
 #define MEXK_KERNEL_GRAM_DOT 7    /* mixed: dots with w and the newest column, Gram correction */
 #define MEXK_KERNEL_GRAM_UPDATE 8 /* mixed: streaming update into the next column */
 #define MEXK_KERNEL_GRAM_NORM 9   /* mixed: norm of the last column (once per basis) */
-#define MEXK_KERNEL_KINDS 10
+#define MEXK_KERNEL_SPMV_DOTS 10  /* mixed, steps j >= 1 over two columns: SpMV + the step's dots and finish */
+#define MEXK_KERNEL_KINDS 11
 
 /* Times `iters` launches of one solver kernel for Arnoldi step j (k = j+1
  * basis columns) on the context stream with a CUDA event pair around each

@@ -40,7 +40,7 @@
 // sum across warps, blocks and the grid in FP64 in a fixed order, so every
 // result is deterministic. The FP64 path keeps explicit CGS2 sweeps
 // (gram_schmidt.cu), whose rounding follows the reference's passes.
-#include "mexk_internal.cuh"
+#include "gram_step.cuh"
 
 #include <math.h>
 
@@ -84,114 +84,6 @@ __device__ __forceinline__ const float4* col4(const float* V, size_t ldv, int c)
     return reinterpret_cast<const float4*>(V + static_cast<size_t>(c) * ldv);
 }
 
-// Sum over row blocks b < nrb of the partials of nv values, value v in slot
-// slot(v) (layout part[slot * GRAM_MAX_ROW_BLOCKS + b]), into out[v]; all
-// threads of the block call it. FP64 adds and shuffles take about 64 and 100
-// cycles of latency on this GPU (FP32: 4), so the sum is shaped for depth: g2
-// adjacent lanes share a value, each loads PR partials per round and
-// adds them as a tree, then the lanes combine by an xor butterfly (every lane
-// ends with the same bits). The order depends only on nrb and nv.
-template <int PR, typename SlotFn>
-__device__ __forceinline__ void sum_partials(const double* part, int nrb, int nv, SlotFn slot, double* out) {
-    int g2 = 32;
-    while (g2 > 1 && g2 * nv > GT) g2 >>= 1;
-    const int t = threadIdx.x;
-    const int vi = t / g2, sub = t % g2;
-    double sum = 0.0;
-    if (vi < nv) {
-        const double* P = part + static_cast<size_t>(slot(vi)) * GRAM_MAX_ROW_BLOCKS;
-        for (int b0 = sub; b0 < nrb; b0 += PR * g2) {
-            double v[PR];
-#pragma unroll
-            for (int u = 0; u < PR; ++u) {
-                const int b = b0 + u * g2;
-                v[u] = b < nrb ? __ldcg(P + b) : 0.0;
-            }
-#pragma unroll
-            for (int h = 1; h < PR; h <<= 1)
-#pragma unroll
-                for (int u = 0; u + h < PR; u += 2 * h) v[u] += v[u + h];
-            sum += v[0];
-        }
-    }
-    for (int o = 1; o < g2; o <<= 1) sum += __shfl_xor_sync(FULL, sum, o);
-    if (vi < nv && sub == 0) out[vi] = sum;
-}
-
-// The finish of a step over at most two columns (j - 1 and j; the first two
-// Arnoldi steps and every step of a window of 2): after the partial sums one
-// thread runs the whole chain (one rsqrt, a few products, one rsqrt) instead
-// of the general finish's five block-wide stages.
-__device__ __forceinline__ void gram_finish2(const GramArgs& g, int nrb) {
-    DevState* st = g.st;
-    const int j = g.j;
-    const int lo = g.lo;
-    const int kw = j + 1 - lo;
-    __shared__ double s_tot[5];  // a (kw), b (kw), |w|^2
-    const int t = threadIdx.x;
-    GramState* gs = g.gs;
-    double* G = gs->G;
-    const size_t ldh = static_cast<size_t>(g.ldh);
-    for (int r = t; r < lo; r += GT) g.H[r + static_cast<size_t>(j) * ldh] = 0.0;  // outside the window
-    const double s0 = kw == 2 ? gs->s[lo] : 0.0;
-    const double ip_j = gs->ip[j];
-    sum_partials<16>(g.part, nrb, 2 * kw + 1,
-                     [&](int v) { return v < kw ? lo + v : (v < 2 * kw ? GRAM_BOFF + lo + (v - kw) : GRAM_NWOFF); },
-                     s_tot);
-    __syncthreads();
-    if (t != 0) return;
-    const double bj = s_tot[2 * kw - 1];
-    const double sj = (bj > 0.0 && !isinf(bj)) ? rsqrt(bj) : 0.0;
-    if (j >= 1) {
-        // the previous step's h_{j,j-1} = |u_j| / p_j; breakdown test as main.cu:1911
-        const double beta = sqrt(bj) * ip_j;
-        const bool bad = !(beta >= 1e-14) || isinf(beta);
-        g.H[j + static_cast<size_t>(j - 1) * ldh] = bad ? 0.0 : beta;
-        if (bad) {
-            st->breakdown = 1;
-            st->k_used = j;
-            return;
-        }
-    }
-    gs->s[j] = sj;
-    G[j + static_cast<size_t>(j) * GRAM_LD] = 1.0;
-    const double sj2 = sj * sj;
-    const double cj = sj2 * s_tot[kw - 1];
-    double hj = cj, part;
-    if (kw == 2) {
-        const double g01 = (s0 * s_tot[kw]) * sj;  // G(j-1, j)
-        const double cp = (s0 * s_tot[0]) * sj;    // c_{j-1}
-        G[lo + static_cast<size_t>(j) * GRAM_LD] = g01;
-        G[j + static_cast<size_t>(lo) * GRAM_LD] = g01;
-        double hp = cp;
-        if (g.reortho) {
-            hp = cp - __dmul_rn(g01, cj);
-            hj = cj - __dmul_rn(g01, cp);
-        }
-        g.H[lo + static_cast<size_t>(j) * ldh] = hp;
-        gs->coef[lo] = static_cast<float>(s0 * hp);
-        const double gh0 = fma(g01, hj, hp), gh1 = hj + __dmul_rn(g01, hp);
-        part = hp * (gh0 - 2.0 * cp) + hj * (gh1 - 2.0 * cj);
-    } else {
-        part = hj * (hj - 2.0 * cj);
-    }
-    g.H[j + static_cast<size_t>(j) * ldh] = hj;
-    gs->coef[j] = static_cast<float>(sj * hj);
-    const double w2 = sj2 * s_tot[2 * kw];
-    const double u2 = w2 + part;
-    double p = 1.0, ip = 1.0;
-    if (u2 > 1e-8 * w2 && !isinf(u2)) {
-        p = rsqrt(u2);
-        ip = u2 * p;
-    } else if (w2 > 0.0 && !isinf(w2)) {
-        p = rsqrt(w2);
-        ip = w2 * p;
-    }
-    gs->ip[j + 1] = ip;
-    gs->wsc = static_cast<float>(sj);
-    gs->psc = static_cast<float>(p);
-}
-
 // Last block of a grid whose nrb row blocks each wrote their partials of
 // step j (slots: a at column, b at GRAM_BOFF + column, |w|^2 at GRAM_NWOFF):
 // sums them and finishes the step (Gram row, h, H, coefficients, pre-scale).
@@ -226,9 +118,8 @@ __device__ __noinline__ void gram_finish(const GramArgs& g, int nrb) {
     double sc_t = 0.0;
     if (t < jw) sc_t = gs->s[lo + t];
     const double ip_j = gs->ip[j];
-    sum_partials<12>(g.part, nrb, 2 * kw + 1,
-                 [&](int v) { return v < kw ? lo + v : (v < 2 * kw ? GRAM_BOFF + lo + (v - kw) : GRAM_NWOFF); },
-                 s_tot);
+    step_sum_partials<12>(g.part, 2 * kw + 1, [&](int v) { return step2_slot(v, kw, lo); },
+                          [&](int) { return nrb; }, s_tot);
     __syncthreads();
     // Stage 2: warp 7 lane 0: s_j = 1/|u_j| and H(j, j-1) = |u_j| / p_j (the
     // breakdown test of main.cu:1911); threads i < jw meanwhile scale their
@@ -332,22 +223,6 @@ __device__ __noinline__ void gram_finish(const GramArgs& g, int nrb) {
     }
 }
 
-// Block stage of a dot sweep: the warps' FP32 totals of NV values (lane l of
-// warp q holds value l in s_red[q][l]) summed over the warps as an FP64
-// tree, then written by thread v to the row block's slot slot(v).
-template <int NV, typename SlotFn>
-__device__ __forceinline__ void write_block_partials(double (&s_red)[GW][NV], double* part, int rb, SlotFn slot) {
-    static_assert(GW == 8, "tree over eight warps");
-    __syncthreads();
-    const int q = threadIdx.x;
-    if (q < NV) {
-        const double t = ((s_red[0][q] + s_red[1][q]) + (s_red[2][q] + s_red[3][q])) +
-                         ((s_red[4][q] + s_red[5][q]) + (s_red[6][q] + s_red[7][q]));
-        const int sl = slot(q);
-        if (sl >= 0) part[static_cast<size_t>(sl) * GRAM_MAX_ROW_BLOCKS + rb] = t;
-    }
-}
-
 // Sweep 1. Block b handles column group b % ngroups (GG columns) over the rows
 // of row block b / ngroups; the groups of one row block are adjacent in launch
 // order, so w and u_j are fetched from DRAM once and re-read from L2.
@@ -403,7 +278,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
         s_red[warp][GG + lane] = rbv;
     }
     if (lane == 0) s_red[warp][2 * GG] = rw;
-    write_block_partials(s_red, g.part, rb, [&](int q) {
+    step_write_partials(s_red, g.part, rb, [&](int q) {
         if (q < GG) return c0 + q < k ? c0 + q : -1;
         if (q < 2 * GG) return c0 + q - GG < k ? GRAM_BOFF + c0 + q - GG : -1;
         return grp == 0 ? GRAM_NWOFF : -1;
@@ -470,7 +345,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot2_kernel(GramArgs g) {
         const float r = warp_sum(acc[q]);
         if (lane == 0) s_red[warp][q] = r;
     }
-    write_block_partials(s_red, g.part, blockIdx.x, [&](int q) {
+    step_write_partials(s_red, g.part, blockIdx.x, [&](int q) {
         switch (q) {
             case 0: return two ? j - 1 : -1;
             case 1: return j;
@@ -481,7 +356,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot2_kernel(GramArgs g) {
     });
     __shared__ int s_flag;
     if (!grid_last_block(g.counter, &s_flag)) return;
-    gram_finish2(g, gridDim.x);
+    step2_finish(g, gridDim.x, gridDim.x);
 }
 
 // Sweep 2: u_{j+1} = psc * (wsc * w - sum_c coef_c u_c), written to column
@@ -581,20 +456,37 @@ __global__ void __launch_bounds__(GT, 4) gram_update2_kernel(GramArgs g) {
         r.w = fmaf(x.w, wsc, -s.w) * psc;
         return r;
     };
+    // step j+1's b: u_j . u_{j+1} and |u_{j+1}|^2 (FP32 per thread)
+    float bu = 0.f, bb = 0.f;
     int i = blockIdx.x * GT + threadIdx.x;
     for (; i + stride < n4; i += 2 * stride) {
         const float4 x0 = __ldg(w4 + i), x1 = __ldg(w4 + i + stride);
         const float4 u0 = __ldg(u4 + i), u1 = __ldg(u4 + i + stride);
         const float4 v0 = two ? __ldg(p4 + i) : u0, v1 = two ? __ldg(p4 + i + stride) : u1;
-        out[i] = one(x0, u0, v0);
-        out[i + stride] = one(x1, u1, v1);
+        const float4 r0 = one(x0, u0, v0), r1 = one(x1, u1, v1);
+        out[i] = r0;
+        out[i + stride] = r1;
+        bu += dot4(u0, r0) + dot4(u1, r1);
+        bb += dot4(r0, r0) + dot4(r1, r1);
     }
     if (i < n4) {
         const float4 x0 = __ldg(w4 + i), u0 = __ldg(u4 + i);
         const float4 v0 = two ? __ldg(p4 + i) : u0;
-        out[i] = one(x0, u0, v0);
+        const float4 r0 = one(x0, u0, v0);
+        out[i] = r0;
+        bu += dot4(u0, r0);
+        bb += dot4(r0, r0);
     }
     pdl_trigger();
+    if (g.write_b) {
+        __shared__ double s_red[GW][2];
+        const float ru = warp_sum(bu), rb = warp_sum(bb);
+        if ((threadIdx.x & 31) == 0) {
+            s_red[threadIdx.x >> 5][0] = ru;
+            s_red[threadIdx.x >> 5][1] = rb;
+        }
+        step_write_partials(s_red, g.part, blockIdx.x, [&](int q) { return GRAM_BOFF + j + q; });
+    }
 }
 
 // |u_{j+1}|^2 by grid reduction; the last block sets H(j+1, j), s_{j+1} and
@@ -613,11 +505,11 @@ __global__ void __launch_bounds__(GT) gram_norm_kernel(GramArgs g) {
     __shared__ double s_red[GW][1];
     const float r = warp_sum(acc);
     if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5][0] = r;
-    write_block_partials(s_red, g.part, blockIdx.x, [](int) { return 0; });
+    step_write_partials(s_red, g.part, blockIdx.x, [](int) { return 0; });
     __shared__ int s_flag;
     if (!grid_last_block(g.counter, &s_flag)) return;
     __shared__ double s_tot[1];
-    sum_partials<20>(g.part, gridDim.x, 1, [](int) { return 0; }, s_tot);
+    step_sum_partials<20>(g.part, 1, [](int) { return 0; }, [&](int) { return static_cast<int>(gridDim.x); }, s_tot);
     __syncthreads();
     if (threadIdx.x == 0) {
         GramState* gs = g.gs;
@@ -680,10 +572,12 @@ int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
     return MEXK_OK;
 }
 
+int gram_update2_blocks(int n) { return row_blocks((n + 1) / 2, 4); }
+
 int launch_gram_update(const GramArgs& a, cudaStream_t s) {
     if (a.j < 0 || a.j >= MEXK_M_MAX || a.lo < 0 || a.lo > a.j) return MEXK_ERR_INVALID;
     const cudaError_t e = a.j + 1 - a.lo <= 2
-                              ? launch_dependent(gram_update2_kernel, row_blocks((a.n + 1) / 2, 4), GT, 0, s, a)
+                              ? launch_dependent(gram_update2_kernel, gram_update2_blocks(a.n), GT, 0, s, a)
                               : launch_dependent(gram_update_kernel, row_blocks(a.n, 4), GT, 0, s, a);
     if (e != cudaSuccess) {
         set_cuda_error(e, "gram_update_kernel", __FILE__, __LINE__);

@@ -288,10 +288,14 @@ int launch_symmetric_check(int n, const int* row_ptr, const int* col_idx, const 
 // entries past nnz, row_ptr at least n + 4 entries (row blocks are copied in
 // whole 16-byte groups). A bulk copy that never completes sets ST_TIMEOUT in
 // *status after a bounded wait; skip_flag (may be null) skips the product.
+struct GramArgs;
+// dots (FP32, a step j >= 1 over columns j-1 and j): the SpMV also
+// accumulates that step's a = U^T w and |w|^2 and its last block finishes the
+// step (the b partials come from the previous step's update, write_b).
 template <typename TA, typename TX>
 int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bool all_narrow, const int* row_ptr,
                 const int* col_idx, const TA* values, const TX* x, TX* y, const int* skip_flag, int* status,
-                cudaStream_t s);
+                cudaStream_t s, const GramArgs* dots = nullptr);
 
 // ------------------------------------------------------------ Gram-Schmidt
 enum GsMode : int { GS_DOT = 0, GS_UPD_DOT = 1, GS_UPD_NORM = 2 };
@@ -310,6 +314,11 @@ struct GsArgs {
     double* h2;       // second-pass coefficients (k)
     double* partials; // grid partials
     unsigned int* counter;
+    // Steps over <= 2 columns whose dot products the SpMV accumulates: the
+    // update of step j also writes step j+1's b partials (write_b), over
+    // b_blocks row blocks (the count step j+1's finish reads).
+    int write_b = 0;
+    int b_blocks = 0;
     DevState* st;     // may be null (standalone use): no flags read/written
     double* beta_out; // standalone use: |w| after the last pass
 };
@@ -346,11 +355,18 @@ struct GramArgs {
     GramState* gs;
     double* part;      // GRAM_SLOTS x GRAM_MAX_ROW_BLOCKS: slot v of row block b at v * GRAM_MAX_ROW_BLOCKS + b
     unsigned int* counter;
+    // Steps over <= 2 columns whose dot products the SpMV accumulates: the
+    // update of step j also writes step j+1's b partials (write_b), over
+    // b_blocks row blocks (the count step j+1's finish reads).
+    int write_b = 0;
+    int b_blocks = 0;
     DevState* st;
 };
 int device_sm_count();
 int launch_gram_dot(const GramArgs& a, cudaStream_t s);
 int launch_gram_update(const GramArgs& a, cudaStream_t s);
+// Row blocks of the update sweep of a step over <= 2 columns (its b partials).
+int gram_update2_blocks(int n);
 // |u_{j+1}| -> H(j+1, j) and s[j+1] (the last step of a basis, or a single step).
 int launch_gram_norm(const GramArgs& a, cudaStream_t s);
 
@@ -397,6 +413,11 @@ struct LiftArgs {
     double* y;
     double* partials;
     unsigned int* counter;
+    // Steps over <= 2 columns whose dot products the SpMV accumulates: the
+    // update of step j also writes step j+1's b partials (write_b), over
+    // b_blocks row blocks (the count step j+1's finish reads).
+    int write_b = 0;
+    int b_blocks = 0;
     DevState* st;
     const double* scale = nullptr;  // per-column scale of the stored basis (FP32 basis)
 };

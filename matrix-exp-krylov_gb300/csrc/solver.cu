@@ -271,17 +271,32 @@ LiftArgs lift_args(mexk_context_t ctx, bool fp32) {
 // Arnoldi step j: w = A v_j, then orthogonalise into column j+1 and H(:, j).
 // The FP64 form finishes the step (H(j+1, j), normalised column); the mixed
 // form leaves H(j+1, j) to the next step's dot sweep or to finish_basis.
-int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t s, int window = 0) {
+// A mixed-precision step j >= 1 over columns j-1 and j (every step of a
+// window of 2, step 1 of full Arnoldi) takes its dot products from the SpMV's
+// row sums and the previous update (no dot sweep of its own).
+bool fused_step(int j, int window) {
+    const int lo = window > 0 ? std::max(0, j + 1 - window) : 0;
+    return j >= 1 && j + 1 - lo <= 2;
+}
+
+// m: size of the basis being built in order (0 for a step on its own: then
+// the step does its own dot sweep, since the previous update may not have
+// written its b partials).
+int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t s, int window = 0, int m = 0) {
     const size_t ldv = static_cast<size_t>(ctx->ldv);
     int rc;
     if (fp32) {
-        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow, ctx->d_row_ptr, ctx->d_col,
-                                            ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32,
-                                            &ctx->d_state->breakdown, &ctx->d_state->status, s)))
-            return rc;
         GramArgs g = gram_args(ctx, j, reortho);
         g.lo = window > 0 ? std::max(0, j + 1 - window) : 0;
-        if ((rc = launch_gram_dot(g, s))) return rc;
+        const bool fuse = m > 0 && fused_step(j, window);
+        g.b_blocks = fuse ? gram_update2_blocks(ctx->n) : 0;
+        if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow,
+                                            ctx->d_row_ptr, ctx->d_col, ctx->d_val32, ctx->d_V32 + j * ldv,
+                                            ctx->d_w32, &ctx->d_state->breakdown, &ctx->d_state->status, s,
+                                            fuse ? &g : nullptr)))
+            return rc;
+        if (!fuse && (rc = launch_gram_dot(g, s))) return rc;
+        g.write_b = (m > 0 && j + 1 < m && fused_step(j + 1, window)) ? 1 : 0;
         return launch_gram_update(g, s);
     }
     if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow, ctx->d_row_ptr, ctx->d_col,
@@ -334,7 +349,7 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, 
     TV* V = fp32 ? reinterpret_cast<TV*>(ctx->d_V32) : reinterpret_cast<TV*>(ctx->d_V);
     int rc;
     for (int j = 0; j < m; ++j)
-        if ((rc = enqueue_step(ctx, j, reortho, fp32, s, window))) return rc;
+        if ((rc = enqueue_step(ctx, j, reortho, fp32, s, window, m))) return rc;
     if ((rc = finish_basis(ctx, m - 1, fp32, s))) return rc;
     if ((rc = enqueue_controller(ctx, m, ctrl, ctx->d_log, s))) return rc;
     const LiftArgs l = lift_args(ctx, fp32);
@@ -965,9 +980,24 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
             case MEXK_KERNEL_GRAM_DOT:
                 rc = fp32 ? launch_gram_dot(ga, s) : MEXK_ERR_UNSUPPORTED;
                 break;
-            case MEXK_KERNEL_GRAM_UPDATE:
-                rc = fp32 ? launch_gram_update(ga, s) : MEXK_ERR_UNSUPPORTED;
+            case MEXK_KERNEL_GRAM_UPDATE: {
+                GramArgs gu = ga;  // as in a solve: b partials for a fused next step
+                gu.write_b = (j + 1 < ctx->m_alloc && fused_step(j + 1, ctx->last_window)) ? 1 : 0;
+                rc = fp32 ? launch_gram_update(gu, s) : MEXK_ERR_UNSUPPORTED;
                 break;
+            }
+            case MEXK_KERNEL_SPMV_DOTS: {
+                if (!fp32 || !fused_step(j, ctx->last_window)) {
+                    rc = MEXK_ERR_UNSUPPORTED;
+                    break;
+                }
+                GramArgs gd = ga;
+                gd.b_blocks = gram_update2_blocks(ctx->n);
+                rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow,
+                                               ctx->d_row_ptr, ctx->d_col, ctx->d_val32, ctx->d_V32 + j * ldv,
+                                               ctx->d_w32, nullptr, &ctx->d_state->status, s, &gd);
+                break;
+            }
             case MEXK_KERNEL_GRAM_NORM:
                 rc = fp32 ? launch_gram_norm(ga, s) : MEXK_ERR_UNSUPPORTED;
                 break;

@@ -19,7 +19,7 @@
 // warp each, and rows longer than a tile by the whole block, in fixed
 // orders (deterministic, within rounding of the serial sum). The gathers of x are
 // served from L2 (x is one basis column, read right after it was written).
-#include "mexk_internal.cuh"
+#include "gram_step.cuh"
 
 #include <algorithm>
 #include <climits>
@@ -345,12 +345,19 @@ int build_spmv_schedule(int n, const int* row_ptr, const int* d_col, SpmvSchedul
 // block included), the products overwrite the staged values, and the row
 // sums read only the row block's own. Row blocks of one long row are not
 // staged: the block streams them directly.
-template <typename TA, typename TX, bool NARROW>
+//
+// DOTS (FP32 mixed form, a step j >= 1 over columns lo = j-1 and j): every
+// thread that writes a row sum w_r also accumulates u_{j-1,r} w_r, u_{j,r} w_r
+// and w_r^2 (FP32 per thread); each block then writes its partials (FP64
+// over the warps), and the last block to finish runs the step's finish
+// (step2_finish: b partials from the previous update). This replaces the
+// step's separate dot sweep.
+template <typename TA, typename TX, bool NARROW, bool DOTS>
 __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
     spmv_stream_kernel(int nblocks, const int4* __restrict__ tiles, const uint16_t* __restrict__ col16,
                        const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
                        const TA* __restrict__ values, const TX* __restrict__ x,
-                       TX* __restrict__ y, const int* __restrict__ skip, int* __restrict__ status) {
+                       TX* __restrict__ y, const int* __restrict__ skip, int* __restrict__ status, GramArgs ga) {
     using TP = typename AccType<TX>::type;
     using SL = TileStage<TA, NARROW>;
     constexpr int S = SL::STAGES;
@@ -367,6 +374,21 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
     const int t0 = g * per + (g < extra ? g : extra);
     const int t1 = t0 + per + (g < extra ? 1 : 0);
     auto staged = [&](int i) { return tiles[i + 1].y - tiles[i].y <= ST_TILE; };
+    float da0 = 0.f, da1 = 0.f, dw = 0.f;  // DOTS: u_{j-1}.w, u_j.w, |w|^2
+    auto dots_with = [&](float up, float uj, TP s) {
+        if constexpr (DOTS) {
+            const float sf = static_cast<float>(s);
+            da0 = fmaf(up, sf, da0);
+            da1 = fmaf(uj, sf, da1);
+            dw = fmaf(sf, sf, dw);
+        }
+    };
+    auto dots = [&](int r, TP s) {  // rows summed outside the thread's own (long rows)
+        if constexpr (DOTS) {
+            const size_t ldv = static_cast<size_t>(ga.ldv);
+            dots_with(ga.V[static_cast<size_t>(ga.lo) * ldv + r], ga.V[static_cast<size_t>(ga.j) * ldv + r], s);
+        }
+    };
     auto issue = [&](int i, uint64_t pol) {  // thread 0
         const int4 a = tiles[i], b = tiles[i + 1];
         if (b.y - a.y > ST_TILE) return;
@@ -425,7 +447,10 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
             for (int e = e0 + tid; e < e1; e += ST_THREADS)
                 s += static_cast<TP>(__ldcs(&values[e])) * static_cast<TP>(__ldg(&x[__ldcs(&col_idx[e])]));
             s = block_sum(s, red);
-            if (tid == 0) y[r0] = static_cast<TX>(s);
+            if (tid == 0) {
+                y[r0] = static_cast<TX>(s);
+                dots(r0, s);
+            }
             continue;
         }
         unsigned char* st = smem + sb * SL::BYTES;
@@ -436,6 +461,18 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
         const int nq = (e1 - base + 3) >> 2;
         const int rbase = r0 & ~3;
         if (tid == 0) s_nlong = 0;
+        // DOTS: the basis entries of the thread's own rows, requested now so
+        // that they arrive during phase 1.
+        float pre_p[ST_RPT], pre_j[ST_RPT];
+        if constexpr (DOTS) {
+            const size_t ldv = static_cast<size_t>(ga.ldv);
+#pragma unroll
+            for (int q = 0; q < ST_RPT; ++q) {
+                const int r = r0 + tid + q * ST_THREADS;
+                pre_p[q] = r < r1 ? __ldg(ga.V + static_cast<size_t>(ga.lo) * ldv + r) : 0.f;
+                pre_j[q] = r < r1 ? __ldg(ga.V + static_cast<size_t>(ga.j) * ldv + r) : 0.f;
+            }
+        }
         // Phase 1: every gather of the thread issued together.
         int4 cq[ST_QUADS];
         if (narrow) {
@@ -488,6 +525,7 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
                     TP s = 0;
                     for (int p = ra - base; p < rz - base; ++p) s += sv[p];
                     y[r] = static_cast<TX>(s);
+                    if constexpr (DOTS) dots_with(pre_p[q], pre_j[q], s);
                 }
             }
         }
@@ -499,7 +537,10 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
             TP s = 0;
             for (int p = a + lane; p < z; p += 32) s += sv[p];
             s = warp_sum(s);
-            if (lane == 0) y[r] = static_cast<TX>(s);
+            if (lane == 0) {
+                y[r] = static_cast<TX>(s);
+                dots(r, s);
+            }
         }
         // this thread's writes to the buffer before the next bulk copy into it
         fence_proxy_async_smem();
@@ -515,14 +556,32 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
             phase ^= 1u << sb;
         }
     }
+    if constexpr (DOTS) {
+        // Every block that ran (a timed-out one too, so that the arrival count
+        // stays whole) writes its partials; the last one finishes the step.
+        if (skipped) return;
+        __shared__ double s_red[8][3];
+        const float r0 = warp_sum(da0), r1 = warp_sum(da1), r2 = warp_sum(dw);
+        if (lane == 0) {
+            s_red[tid >> 5][0] = r0;
+            s_red[tid >> 5][1] = r1;
+            s_red[tid >> 5][2] = r2;
+        }
+        const int jj = ga.j;
+        step_write_partials(s_red, ga.part, blockIdx.x, [&](int q) { return q < 2 ? jj - 1 + q : GRAM_NWOFF; });
+        __shared__ int s_flag;
+        if (!grid_last_block(ga.counter, &s_flag)) return;
+        step2_finish(ga, gridDim.x, ga.b_blocks);
+    }
 }
 
-template <typename TA, typename TX, bool NARROW>
+template <typename TA, typename TX, bool NARROW, bool DOTS>
 int launch_spmv_as(int nblocks, const int4* tiles, const uint16_t* col16, const int* row_ptr, const int* col_idx,
-                   const TA* values, const TX* x, TX* y, const int* skip_flag, int* status, cudaStream_t s) {
+                   const TA* values, const TX* x, TX* y, const int* skip_flag, int* status, const GramArgs& ga,
+                   cudaStream_t s) {
     using SL = TileStage<TA, NARROW>;
     constexpr size_t smem = SL::STAGES * SL::BYTES;
-    auto kern = spmv_stream_kernel<TA, TX, NARROW>;
+    auto kern = spmv_stream_kernel<TA, TX, NARROW, DOTS>;
     static int resident = 0;  // thread blocks per SM (one device type per process)
     if (resident == 0) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -534,10 +593,11 @@ int launch_spmv_as(int nblocks, const int4* tiles, const uint16_t* col16, const 
             return MEXK_ERR_CUDA;
         }
     }
-    const long long cap = static_cast<long long>(device_sm_count()) * resident;
+    long long cap = static_cast<long long>(device_sm_count()) * resident;
+    if (DOTS && cap > GRAM_MAX_ROW_BLOCKS) cap = GRAM_MAX_ROW_BLOCKS;  // one partial slot per block
     const int grid = static_cast<int>(nblocks < cap ? nblocks : cap);
     const cudaError_t e = launch_dependent(kern, grid, ST_THREADS, smem, s, nblocks, tiles, col16, row_ptr, col_idx,
-                                           values, x, y, skip_flag, status);
+                                           values, x, y, skip_flag, status, ga);
     if (e != cudaSuccess) {
         set_cuda_error(e, "spmv_stream_kernel", __FILE__, __LINE__);
         return MEXK_ERR_CUDA;
@@ -548,23 +608,37 @@ int launch_spmv_as(int nblocks, const int4* tiles, const uint16_t* col16, const 
 template <typename TA, typename TX>
 int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bool all_narrow, const int* row_ptr,
                 const int* col_idx, const TA* values, const TX* x, TX* y, const int* skip_flag, int* status,
-                cudaStream_t s) {
+                cudaStream_t s, const GramArgs* dots) {
     if (n <= 0 || nblocks <= 0) return MEXK_OK;
     if (reinterpret_cast<uintptr_t>(col_idx) % 16 != 0 || reinterpret_cast<uintptr_t>(values) % 16 != 0 ||
         reinterpret_cast<uintptr_t>(row_ptr) % 16 != 0 || reinterpret_cast<uintptr_t>(col16) % 16 != 0) {
         set_error_text("spmv: context arrays must be 16-byte aligned");
         return MEXK_ERR_INVALID;
     }
-    return all_narrow ? launch_spmv_as<TA, TX, true>(nblocks, tiles, col16, row_ptr, col_idx, values, x, y,
-                                                      skip_flag, status, s)
-                      : launch_spmv_as<TA, TX, false>(nblocks, tiles, col16, row_ptr, col_idx, values, x, y,
-                                                       skip_flag, status, s);
+    const GramArgs none{};
+    if constexpr (sizeof(TX) == 4) {
+        if (dots) {
+            if (dots->j < 1 || dots->lo != dots->j - 1 || dots->b_blocks < 1) return MEXK_ERR_INVALID;
+            return all_narrow ? launch_spmv_as<TA, TX, true, true>(nblocks, tiles, col16, row_ptr, col_idx, values,
+                                                                    x, y, skip_flag, status, *dots, s)
+                              : launch_spmv_as<TA, TX, false, true>(nblocks, tiles, col16, row_ptr, col_idx, values,
+                                                                     x, y, skip_flag, status, *dots, s);
+        }
+    } else if (dots) {
+        return MEXK_ERR_UNSUPPORTED;
+    }
+    return all_narrow ? launch_spmv_as<TA, TX, true, false>(nblocks, tiles, col16, row_ptr, col_idx, values, x, y,
+                                                             skip_flag, status, none, s)
+                      : launch_spmv_as<TA, TX, false, false>(nblocks, tiles, col16, row_ptr, col_idx, values, x, y,
+                                                              skip_flag, status, none, s);
 }
 
 template int launch_spmv<double, double>(int, int, const int4*, const uint16_t*, bool, const int*, const int*,
-                                         const double*, const double*, double*, const int*, int*, cudaStream_t);
+                                         const double*, const double*, double*, const int*, int*, cudaStream_t,
+                                         const GramArgs*);
 template int launch_spmv<float, float>(int, int, const int4*, const uint16_t*, bool, const int*, const int*,
-                                       const float*, const float*, float*, const int*, int*, cudaStream_t);
+                                       const float*, const float*, float*, const int*, int*, cudaStream_t,
+                                       const GramArgs*);
 
 // FP32 copy of the FP64 matrix values for the mixed-precision form
 // (round to nearest).

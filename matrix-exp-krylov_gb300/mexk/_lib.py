@@ -123,7 +123,7 @@ _PROTOS = {
 }
 
 KERNELS = {"spmv": 0, "gs_dot": 1, "gs_upd_dot": 2, "gs_upd_norm": 3, "normalize": 4, "lift": 5, "controller": 6,
-           "gram_dot": 7, "gram_update": 8, "gram_norm": 9}
+           "gram_dot": 7, "gram_update": 8, "gram_norm": 9, "spmv_dots": 10}
 
 _lib = None
 
