@@ -108,6 +108,10 @@ class ClockSampler:
 # still in L2 when the kernel ends). The same stencil's traffic grows with
 # its nonzeros.
 SPMV_F32_TRAFFIC_HEAT1536 = (89.869312e6 + 3.002624e6, 11790336)
+# The same for the SpMV that also accumulates a step's dot products
+# (spmv_stream_kernel<float, float, 1, 1>): 99.40 MB read (u_{j-1} too) +
+# 3.27 MB written.
+SPMV_DOTS_F32_TRAFFIC_HEAT1536 = (99.39968e6 + 3.26912e6, 11790336)
 
 def kernel_bytes(kind, n, nnz, k, fp32, window=0):
     """Algorithmic HBM bytes of one launch (per-kernel minimum traffic); with a
@@ -382,10 +386,10 @@ def run_ours(args, rank, world, local_rank):
     dom = max(per, key=lambda k: per[k]["ms"])
     ach = per[dom]["bytes"] / (per[dom]["ms"] / 1e3) / 1e9
     traffic, tsrc = None, None
-    if dom == "spmv" and form != "fp64":
-        mb, nz = SPMV_F32_TRAFFIC_HEAT1536
+    if dom in ("spmv", "spmv_dots") and form != "fp64":
+        mb, nz = SPMV_DOTS_F32_TRAFFIC_HEAT1536 if dom == "spmv_dots" else SPMV_F32_TRAFFIC_HEAT1536
         traffic = mb * nnz / nz
-        tsrc = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of spmv_stream_kernel<float, float> on the "
+        tsrc = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the {dom} kernel on the "
                 "1536^2 heat grid (11,790,336 nonzeros), scaled by nonzeros")
     roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
             "traffic": traffic, "traffic_source": tsrc,
