@@ -166,8 +166,6 @@ struct ExpmBuf {
     double* red;  // >= k doubles
 };
 
-// exp of the k-by-k matrix in B.A (ld k); returns the buffer holding the
-// result. All threads of the block must call it.
 // 1-norm column sums of the k-by-k matrix in A (thread j < k: column j).
 __device__ __forceinline__ double col_abs_sum(int k, const double* A, int j) {
     double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
@@ -182,6 +180,8 @@ __device__ __forceinline__ double col_abs_sum(int k, const double* A, int j) {
     return (c0 + c1) + (c2 + c3);
 }
 
+// exp of the k-by-k matrix in B.A (ld k) by Pade scaling and squaring;
+// returns the buffer holding the result. All threads of the block must call it.
 __device__ double* expm_block(const ExpmBuf& B, int k, int* status) {
     __shared__ int s_deg, s_sq;
     __shared__ double s_b[14];
@@ -708,14 +708,28 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         }
     }
     if (!grid_last_block(a.counter, &s_flag)) return;
-    if (threadIdx.x == 0) {
-        int best = -1;
-        for (int g = 0; g < static_cast<int>(gridDim.x) / SEARCH_CLUSTER; ++g) {
+    static_assert(SEARCH_CAND <= 32, "one lane per candidate");
+    if (threadIdx.x < 32) {
+        // The largest passing step, the lowest index among equal steps (the
+        // serial scan's choice), one lane per candidate and a butterfly.
+        const int ncand = static_cast<int>(gridDim.x) / SEARCH_CLUSTER;
+        int g = static_cast<int>(threadIdx.x);
+        double tau = -1.0;
+        if (g < ncand) {
             const double* c = a.cand + static_cast<size_t>(g) * CAND_STRIDE;
-            if (__ldcg(&c[0]) <= tol_eff && (best < 0 || __ldcg(&c[1]) > __ldcg(&a.cand[best * CAND_STRIDE + 1])))
-                best = g;
+            if (__ldcg(&c[0]) <= tol_eff) tau = __ldcg(&c[1]);
         }
-        s_best = best;
+        if (tau < 0.0) g = 32;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ot = __shfl_xor_sync(0xffffffffu, tau, o);
+            const int og = __shfl_xor_sync(0xffffffffu, g, o);
+            if (ot > tau || (ot == tau && og < g)) {
+                tau = ot;
+                g = og;
+            }
+        }
+        if (threadIdx.x == 0) s_best = g < 32 ? g : -1;
     }
     __syncthreads();
     const double vn = st->v_norm;
