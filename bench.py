@@ -147,12 +147,12 @@ STEP_KINDS = {"fp64": ["spmv", "gs_dot", "gs_upd_dot", "gs_upd_norm", "normalize
               "mixed": ["spmv", "gram_dot", "gram_update"]}
 
 
-def step_kinds(precision, j, window=0):
-    """Kernels of Arnoldi step j as a solve runs them: in mixed precision a
-    step j >= 1 over two columns (every step of a window of 2, step 1 of full
-    Arnoldi) takes its dot products from the SpMV (spmv_dots) and needs no
-    dot sweep."""
-    if precision == "mixed":
+def step_kinds(precision, j, window=0, staged=True):
+    """Kernels of Arnoldi step j as a solve runs them: in mixed precision with
+    the staged SpMV a step j >= 1 over two columns (every step of a window of
+    2, step 1 of full Arnoldi) takes its dot products from the SpMV
+    (spmv_dots) and needs no dot sweep."""
+    if precision == "mixed" and staged:
         lo = max(0, j + 1 - window) if window else 0
         if j >= 1 and j + 1 - lo <= 2:
             return ["spmv_dots", "gram_update"]
@@ -167,6 +167,7 @@ def profile_cycle(ctx, m, n, nnz, precision, iters=2, window=0):
     as the context's last solve ran them: with its window, if any)."""
     fp32 = precision == "mixed"
     once = CYCLE_KINDS[precision]
+    staged = ctx.spmv_form(precision) == "staged"
     per = {}
 
     def add(kind, j, k):
@@ -180,7 +181,7 @@ def profile_cycle(ctx, m, n, nnz, precision, iters=2, window=0):
     for kind in once:
         add(kind, m - 1, m)
     for j in range(m):
-        for kind in step_kinds(precision, j, window):
+        for kind in step_kinds(precision, j, window, staged):
             add(kind, j, j + 1)
     return per
 
@@ -194,7 +195,8 @@ def launches_per_solve(ctx, precision, res, m, window=0):
     if len(sizes) != res["cycles"]:  # rejects reuse their cycle's basis
         sizes = [m] * res["cycles"]
     per_cycle = 4 if precision == "mixed" else 3
-    return 2 + sum(sum(len(step_kinds(precision, j, window)) for j in range(k)) + per_cycle for k in sizes)
+    staged = ctx.spmv_form(precision) == "staged"
+    return 2 + sum(sum(len(step_kinds(precision, j, window, staged)) for j in range(k)) + per_cycle for k in sizes)
 
 
 def gs_cgs2_equivalent(per, n, m, precision):
@@ -435,6 +437,7 @@ def run_ours(args, rank, world, local_rank):
             "data": "synthetic",
             "config": {"workload": WORKLOAD,
                        "form": f"{form} + {ctrl_form} controller" + (f" + window {win_form}" if win_form else ""),
+                       "spmv_form": ctx.spmv_form(form),
                        "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (CSR 251 MB, basis >= 520 MB); no flush"},
             "fp64_solves_per_s": fp64_sps, "chosen_rel_err_vs_fp64": rel_err,
@@ -692,9 +695,15 @@ def run_powerlaw(args):
                                      "spmv": res["spmv_count"], "converged": res["converged"]}
         spmv = {}
         for prec in ("mixed", "fp64"):
-            ms = min(ctx.profile_kernel("spmv", j, 5, prec) for j in (0, 10, 20))
+            chosen = ctx.spmv_form(prec)
             b = kernel_bytes("spmv", n, nnz, 1, prec == "mixed")
-            spmv[prec] = {"us": round(ms * 1e3, 1), "gbs": round(b / (ms / 1e3) / 1e9, 1)}
+            spmv[prec] = {"form": chosen}
+            for f in ("staged", "direct"):  # both forms, then the context's own choice back
+                ctx.set_spmv_form(f, prec)
+                ms = min(ctx.profile_kernel("spmv", j, 5, prec) for j in (0, 10, 20))
+                spmv[prec][f] = {"us": round(ms * 1e3, 1), "gbs": round(b / (ms / 1e3) / 1e9, 1)}
+            ctx.set_spmv_form(chosen, prec)
+            spmv[prec].update(spmv[prec][chosen])
     ok = {k: v for k, v in out.items() if k != "fp64+reference" and v["rel_err_vs_fp64"] <= 1e-6}
     best = min(ok, key=lambda k: out[k]["ms"]) if ok else "fp64+reference"
     peak, _ = measured_peaks()

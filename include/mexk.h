@@ -341,6 +341,22 @@ int mexk_batch_destroy(mexk_batch_t b);
  * the controller, of the context's last solve. */
 int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int iters, double* ms_per_launch);
 
+/* Which form of the context SpMV runs for a precision: MEXK_SPMV_STAGED
+ * (persistent blocks, matrix tiles staged into shared memory by bulk copies;
+ * the mixed steps over two columns also accumulate their dot products in it)
+ * or MEXK_SPMV_DIRECT (one block per row block, loads straight from HBM).
+ * At upload the context picks direct when some row block's columns span
+ * 65,536 or more (gathers scattered over x, where more blocks in flight keep
+ * more gathers outstanding), staged otherwise; the setter overrides that.
+ * Both forms compute the same products and row sums, so FP64 solves are
+ * bitwise equal under either; mixed solves take the two-column steps' dots
+ * from a different sum order and agree to rounding. No reference
+ * counterpart: the reference's SpMV is one cuSPARSE call (main.cu:1743). */
+#define MEXK_SPMV_STAGED 0
+#define MEXK_SPMV_DIRECT 1
+int mexk_context_get_spmv_form(mexk_context_t ctx, int precision, int* form);
+int mexk_context_set_spmv_form(mexk_context_t ctx, int precision, int form);
+
 #ifdef __cplusplus
 }
 #endif

@@ -292,10 +292,11 @@ struct GramArgs;
 // dots (FP32, a step j >= 1 over columns j-1 and j): the SpMV also
 // accumulates that step's a = U^T w and |w|^2 and its last block finishes the
 // step (the b partials come from the previous step's update, write_b).
+// direct: the unstaged form, one thread block per row block (no dots).
 template <typename TA, typename TX>
 int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bool all_narrow, const int* row_ptr,
                 const int* col_idx, const TA* values, const TX* x, TX* y, const int* skip_flag, int* status,
-                cudaStream_t s, const GramArgs* dots = nullptr);
+                cudaStream_t s, const GramArgs* dots = nullptr, bool direct = false);
 
 // ------------------------------------------------------------ Gram-Schmidt
 enum GsMode : int { GS_DOT = 0, GS_UPD_DOT = 1, GS_UPD_NORM = 2 };

@@ -78,6 +78,10 @@ struct mexk_context_s {
     int4* d_tiles = nullptr;
     uint16_t* d_col16 = nullptr;
     bool spmv_narrow = false;  // every staged SpMV row block has 16-bit columns
+    // The SpMV form per precision: direct (one block per row block) when some
+    // row block's columns span 65,536 or more, else staged.
+    bool spmv_direct64 = false;
+    bool spmv_direct32 = false;
     double* d_V = nullptr;
     float* d_V32 = nullptr;
     double* d_w = nullptr;
@@ -211,6 +215,7 @@ int ensure_mixed(mexk_context_t ctx) {
     if ((rc = reset_gram(ctx, ctx->stream))) return rc;
     if ((rc = dalloc(&ctx->d_val32, static_cast<size_t>(ctx->nnz) + 4))) return rc;
     if ((rc = launch_narrow_values(ctx->d_val, ctx->d_val32, static_cast<size_t>(ctx->nnz), ctx->stream))) return rc;
+    ctx->spmv_direct32 = !ctx->spmv_narrow;
     MEXK_CK(cudaStreamSynchronize(ctx->stream));
     return MEXK_OK;
 }
@@ -288,20 +293,23 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
     if (fp32) {
         GramArgs g = gram_args(ctx, j, reortho);
         g.lo = window > 0 ? std::max(0, j + 1 - window) : 0;
-        const bool fuse = m > 0 && fused_step(j, window);
+        // the step's dots ride on the staged SpMV only
+        const bool fusable = m > 0 && !ctx->spmv_direct32;
+        const bool fuse = fusable && fused_step(j, window);
         g.b_blocks = fuse ? gram_update2_blocks(ctx->n) : 0;
         if ((rc = launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow,
                                             ctx->d_row_ptr, ctx->d_col, ctx->d_val32, ctx->d_V32 + j * ldv,
                                             ctx->d_w32, &ctx->d_state->breakdown, &ctx->d_state->status, s,
-                                            fuse ? &g : nullptr)))
+                                            fuse ? &g : nullptr, ctx->spmv_direct32)))
             return rc;
         if (!fuse && (rc = launch_gram_dot(g, s))) return rc;
-        g.write_b = (m > 0 && j + 1 < m && fused_step(j + 1, window)) ? 1 : 0;
+        g.write_b = (fusable && j + 1 < m && fused_step(j + 1, window)) ? 1 : 0;
         return launch_gram_update(g, s);
     }
-    if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow, ctx->d_row_ptr, ctx->d_col,
-                                          ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, &ctx->d_state->breakdown,
-                                          &ctx->d_state->status, s)))
+    if ((rc = launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow,
+                                          ctx->d_row_ptr, ctx->d_col, ctx->d_val, ctx->d_V + j * ldv, ctx->d_w,
+                                          &ctx->d_state->breakdown, &ctx->d_state->status, s, nullptr,
+                                          ctx->spmv_direct64)))
         return rc;
     const GsArgs g = gs_args(ctx, j, reortho, false);
     const int grid = gs_grid_size(ctx->n, j + 1);
@@ -391,6 +399,12 @@ int get_graph(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, int wi
     ctx->graphs.push_back({m, prec, reortho, ctrl, window, exec});
     *out = exec;
     return MEXK_OK;
+}
+
+void invalidate_graphs(mexk_context_t ctx) {
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& g : ctx->graphs) cudaGraphExecDestroy(g.exec);
+    ctx->graphs.clear();
 }
 
 void init_state(DevState* st, const mexk_params_t* p, int log_cap) {
@@ -545,6 +559,7 @@ int context_csr_finish(mexk_context_t ctx, const int* row_ptr) {
     if (rc) return rc;
     ctx->nblocks = sched.nblocks;
     ctx->spmv_narrow = sched.all_narrow;
+    ctx->spmv_direct64 = !sched.all_narrow;
     const int m_alloc_max = ctx->m_alloc;
     const size_t vcount = static_cast<size_t>(ctx->ldv) * (m_alloc_max + 1);
     if ((rc = dalloc(&ctx->d_V, vcount))) return rc;
@@ -906,6 +921,36 @@ int mexk_context_set_controller(mexk_context_t ctx, const float* weights, int co
     return MEXK_OK;
 }
 
+int mexk_context_get_spmv_form(mexk_context_t ctx, int precision, int* form) {
+    if (!ctx || !ctx->uploaded || !form) return MEXK_ERR_INVALID;
+    if (precision != MEXK_PREC_FP64 && precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
+    int rc;
+    if (precision == MEXK_PREC_MIXED) {
+        MEXK_CK(cudaSetDevice(ctx->device));
+        if ((rc = ensure_mixed(ctx))) return rc;
+    }
+    const bool d = precision == MEXK_PREC_MIXED ? ctx->spmv_direct32 : ctx->spmv_direct64;
+    *form = d ? MEXK_SPMV_DIRECT : MEXK_SPMV_STAGED;
+    return MEXK_OK;
+}
+
+int mexk_context_set_spmv_form(mexk_context_t ctx, int precision, int form) {
+    if (!ctx || !ctx->uploaded) return MEXK_ERR_INVALID;
+    if (precision != MEXK_PREC_FP64 && precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
+    if (form != MEXK_SPMV_STAGED && form != MEXK_SPMV_DIRECT) return MEXK_ERR_INVALID;
+    int rc;
+    if (precision == MEXK_PREC_MIXED) {
+        MEXK_CK(cudaSetDevice(ctx->device));
+        if ((rc = ensure_mixed(ctx))) return rc;  // its tuning must not undo the choice later
+        ctx->spmv_direct32 = form == MEXK_SPMV_DIRECT;
+    } else {
+        ctx->spmv_direct64 = form == MEXK_SPMV_DIRECT;
+    }
+    // captured cycle graphs hold the other form's launches
+    invalidate_graphs(ctx);
+    return MEXK_OK;
+}
+
 int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int iters, double* ms_per_launch) {
     if (!ctx || !ctx->uploaded || !ms_per_launch || iters < 1) return MEXK_ERR_INVALID;
     if (kind < 0 || kind >= MEXK_KERNEL_KINDS || j < 0 || j >= ctx->m_alloc) return MEXK_ERR_INVALID;
@@ -957,12 +1002,14 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
         }
         switch (kind) {
             case MEXK_KERNEL_SPMV:
-                rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow, ctx->d_row_ptr, ctx->d_col,
-                                                      ctx->d_val32, ctx->d_V32 + j * ldv, ctx->d_w32, nullptr,
-                                                      &ctx->d_state->status, s)
-                          : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16, ctx->spmv_narrow, ctx->d_row_ptr,
-                                                        ctx->d_col, ctx->d_val, ctx->d_V + j * ldv, ctx->d_w, nullptr,
-                                                        &ctx->d_state->status, s);
+                rc = fp32 ? launch_spmv<float, float>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16,
+                                                      ctx->spmv_narrow, ctx->d_row_ptr, ctx->d_col, ctx->d_val32,
+                                                      ctx->d_V32 + j * ldv, ctx->d_w32, nullptr,
+                                                      &ctx->d_state->status, s, nullptr, ctx->spmv_direct32)
+                          : launch_spmv<double, double>(ctx->n, ctx->nblocks, ctx->d_tiles, ctx->d_col16,
+                                                        ctx->spmv_narrow, ctx->d_row_ptr, ctx->d_col, ctx->d_val,
+                                                        ctx->d_V + j * ldv, ctx->d_w, nullptr, &ctx->d_state->status,
+                                                        s, nullptr, ctx->spmv_direct64);
                 break;
             case MEXK_KERNEL_GS_DOT:
             case MEXK_KERNEL_GS_UPD_DOT:
@@ -987,7 +1034,7 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
                 break;
             }
             case MEXK_KERNEL_SPMV_DOTS: {
-                if (!fp32 || !fused_step(j, ctx->last_window)) {
+                if (!fp32 || !fused_step(j, ctx->last_window) || ctx->spmv_direct32) {
                     rc = MEXK_ERR_UNSUPPORTED;
                     break;
                 }

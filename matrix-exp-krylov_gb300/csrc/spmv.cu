@@ -575,6 +575,135 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
     }
 }
 
+// Global 16-byte group of 4 values, streamed (read once).
+template <typename TA>
+__device__ __forceinline__ void gquad(const TA* p, TA (&o)[4]);
+template <>
+__device__ __forceinline__ void gquad<float>(const float* p, float (&o)[4]) {
+    const float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+    o[0] = t.x;
+    o[1] = t.y;
+    o[2] = t.z;
+    o[3] = t.w;
+}
+template <>
+__device__ __forceinline__ void gquad<double>(const double* p, double (&o)[4]) {
+    const double2 t0 = __ldcs(reinterpret_cast<const double2*>(p));
+    const double2 t1 = __ldcs(reinterpret_cast<const double2*>(p) + 1);
+    o[0] = t0.x;
+    o[1] = t0.y;
+    o[2] = t1.x;
+    o[3] = t1.y;
+}
+
+// Context form without staging, one thread block per row block (the same
+// schedule): the block loads its 16-byte groups of columns and values
+// directly, gathers x for every entry of those groups (the padding columns
+// are zero, so no range tests), keeps the products in shared memory and sums
+// the rows as spmv_stream_kernel does (same products, same order). Many
+// short-lived blocks let the scheduler keep more gathers in flight than the
+// persistent staged form: for matrices whose columns scatter over all of x
+// (every product a separate gather, e.g. the power-law rows) this form is
+// faster, for banded ones the staged form is. A context runs this form when
+// some row block's columns span 65,536 or more (the staged form's 16-bit
+// column layout does not apply).
+template <typename TA, typename TX>
+__global__ void __launch_bounds__(ST_THREADS)
+    spmv_direct_kernel(int nblocks, const int4* __restrict__ tiles, const int* __restrict__ row_ptr,
+                       const int* __restrict__ col_idx, const TA* __restrict__ values, const TX* __restrict__ x,
+                       TX* __restrict__ y, const int* __restrict__ skip) {
+    using TP = typename AccType<TX>::type;
+    constexpr int QMAX = TileStage<TA, false>::QMAX;
+    __shared__ TP prod[QMAX * 4];
+    __shared__ TP red[32];
+    __shared__ int s_long[ST_TILE / (SEQ_ROW_MAX + 1) + 1];
+    __shared__ int s_nlong;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int b = blockIdx.x;
+    const int4 ta = tiles[b], tb = tiles[b + 1];
+    const int r0 = ta.x, r1 = tb.x, e0 = ta.y, e1 = tb.y;
+    // the matrix is never written by a kernel: its loads may start before the
+    // previous kernel of the stream has finished
+    int ra[ST_RPT], rz[ST_RPT];
+#pragma unroll
+    for (int q = 0; q < ST_RPT; ++q) {
+        const int r = r0 + tid + q * ST_THREADS;
+        ra[q] = r < r1 ? row_ptr[r] : 0;
+        rz[q] = r < r1 ? row_ptr[r + 1] : 0;
+    }
+    if (e1 - e0 > ST_TILE) {
+        pdl_wait();
+        if (skip != nullptr && *skip) return;
+        if (b == static_cast<int>(gridDim.x) - 1) pdl_trigger();
+        // One long row: the block splits its nonzeros, then a tree sum.
+        TP s = 0;
+        for (int e = e0 + tid; e < e1; e += ST_THREADS)
+            s += static_cast<TP>(__ldcs(&values[e])) * static_cast<TP>(__ldg(&x[__ldcs(&col_idx[e])]));
+        s = block_sum(s, red);
+        if (tid == 0) y[r0] = static_cast<TX>(s);
+        return;
+    }
+    const int base = e0 & ~3;
+    const int nq = (e1 - base + 3) >> 2;
+    int4 cq[ST_QUADS];
+    TA aq[ST_QUADS][4];
+#pragma unroll
+    for (int q = 0; q < ST_QUADS; ++q) {
+        const int gq = tid + q * ST_THREADS;
+        if (gq < nq) {
+            cq[q] = __ldcs(reinterpret_cast<const int4*>(col_idx + base) + gq);
+            gquad<TA>(values + base + 4 * gq, aq[q]);
+        } else {
+            cq[q] = make_int4(0, 0, 0, 0);
+        }
+    }
+    pdl_wait();
+    if (skip != nullptr && *skip) return;
+    if (b == static_cast<int>(gridDim.x) - 1) pdl_trigger();
+    if (tid == 0) s_nlong = 0;
+    TP xq[ST_QUADS][4];
+#pragma unroll
+    for (int q = 0; q < ST_QUADS; ++q) {
+        xq[q][0] = static_cast<TP>(__ldg(&x[cq[q].x]));
+        xq[q][1] = static_cast<TP>(__ldg(&x[cq[q].y]));
+        xq[q][2] = static_cast<TP>(__ldg(&x[cq[q].z]));
+        xq[q][3] = static_cast<TP>(__ldg(&x[cq[q].w]));
+    }
+#pragma unroll
+    for (int q = 0; q < ST_QUADS; ++q) {
+        const int gq = tid + q * ST_THREADS;
+        if (gq < nq) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) prod[4 * gq + k] = static_cast<TP>(aq[q][k]) * xq[q][k];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < ST_RPT; ++q) {
+        const int r = r0 + tid + q * ST_THREADS;
+        if (r < r1) {
+            if (rz[q] - ra[q] > SEQ_ROW_MAX) {
+                s_long[atomicAdd(&s_nlong, 1)] = r;
+            } else {
+                TP s = 0;
+                for (int p = ra[q] - base; p < rz[q] - base; ++p) s += prod[p];
+                y[r] = static_cast<TX>(s);
+            }
+        }
+    }
+    __syncthreads();
+    for (int li = tid >> 5; li < s_nlong; li += ST_THREADS / 32) {
+        const int r = s_long[li];
+        const int a = row_ptr[r] - base;
+        const int z = row_ptr[r + 1] - base;
+        TP s = 0;
+        for (int p = a + lane; p < z; p += 32) s += prod[p];
+        s = warp_sum(s);
+        if (lane == 0) y[r] = static_cast<TX>(s);
+    }
+}
+
 template <typename TA, typename TX, bool NARROW, bool DOTS>
 int launch_spmv_as(int nblocks, const int4* tiles, const uint16_t* col16, const int* row_ptr, const int* col_idx,
                    const TA* values, const TX* x, TX* y, const int* skip_flag, int* status, const GramArgs& ga,
@@ -606,9 +735,21 @@ int launch_spmv_as(int nblocks, const int4* tiles, const uint16_t* col16, const 
 }
 
 template <typename TA, typename TX>
+int launch_spmv_direct(int nblocks, const int4* tiles, const int* row_ptr, const int* col_idx, const TA* values,
+                       const TX* x, TX* y, const int* skip_flag, cudaStream_t s) {
+    const cudaError_t e = launch_dependent(spmv_direct_kernel<TA, TX>, nblocks, ST_THREADS, 0, s, nblocks, tiles,
+                                           row_ptr, col_idx, values, x, y, skip_flag);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "spmv_direct_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
+    return MEXK_OK;
+}
+
+template <typename TA, typename TX>
 int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bool all_narrow, const int* row_ptr,
                 const int* col_idx, const TA* values, const TX* x, TX* y, const int* skip_flag, int* status,
-                cudaStream_t s, const GramArgs* dots) {
+                cudaStream_t s, const GramArgs* dots, bool direct) {
     if (n <= 0 || nblocks <= 0) return MEXK_OK;
     if (reinterpret_cast<uintptr_t>(col_idx) % 16 != 0 || reinterpret_cast<uintptr_t>(values) % 16 != 0 ||
         reinterpret_cast<uintptr_t>(row_ptr) % 16 != 0 || reinterpret_cast<uintptr_t>(col16) % 16 != 0) {
@@ -616,6 +757,7 @@ int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bo
         return MEXK_ERR_INVALID;
     }
     const GramArgs none{};
+    if (direct && !dots) return launch_spmv_direct<TA, TX>(nblocks, tiles, row_ptr, col_idx, values, x, y, skip_flag, s);
     if constexpr (sizeof(TX) == 4) {
         if (dots) {
             if (dots->j < 1 || dots->lo != dots->j - 1 || dots->b_blocks < 1) return MEXK_ERR_INVALID;
@@ -635,10 +777,10 @@ int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bo
 
 template int launch_spmv<double, double>(int, int, const int4*, const uint16_t*, bool, const int*, const int*,
                                          const double*, const double*, double*, const int*, int*, cudaStream_t,
-                                         const GramArgs*);
+                                         const GramArgs*, bool);
 template int launch_spmv<float, float>(int, int, const int4*, const uint16_t*, bool, const int*, const int*,
                                        const float*, const float*, float*, const int*, int*, cudaStream_t,
-                                       const GramArgs*);
+                                       const GramArgs*, bool);
 
 // FP32 copy of the FP64 matrix values for the mixed-precision form
 // (round to nearest).

@@ -106,6 +106,8 @@ _PROTOS = {
     "mexk_context_get_basis": ([_VP, C.c_int, _DP, C.c_int], C.c_int),
     "mexk_expm_f64": ([C.c_int, _VP, C.c_int, _VP, C.c_int, _VP], C.c_int),
     "mexk_profile_kernel": ([_VP, C.c_int, C.c_int, C.c_int, C.c_int, _DP], C.c_int),
+    "mexk_context_get_spmv_form": ([_VP, C.c_int, _IP], C.c_int),
+    "mexk_context_set_spmv_form": ([_VP, C.c_int, C.c_int], C.c_int),
     "mexk_gram_schmidt_f64_noalloc": ([C.c_int, C.c_int, _VP, C.c_int, _VP, C.c_int, _VP, _VP, _VP, _VP],
                                       C.c_int),
     "mexk_context_set_controller": ([_VP, C.POINTER(C.c_float), C.c_int], C.c_int),

@@ -167,6 +167,21 @@ class Context:
               "mexk_profile_kernel")
         return ms.value
 
+    SPMV_FORMS = ("staged", "direct")
+
+    def spmv_form(self, precision="fp64") -> str:
+        """The SpMV form the context runs for a precision: "staged" (tiles
+        staged in shared memory; the default when every row block's columns
+        span less than 65,536) or "direct" (one block per row block)."""
+        f = C.c_int(0)
+        check(lib().mexk_context_get_spmv_form(self._h, PRECISIONS[precision], C.byref(f)),
+              "mexk_context_get_spmv_form")
+        return self.SPMV_FORMS[f.value]
+
+    def set_spmv_form(self, form: str, precision="fp64") -> None:
+        check(lib().mexk_context_set_spmv_form(self._h, PRECISIONS[precision], self.SPMV_FORMS.index(form)),
+              "mexk_context_set_spmv_form")
+
     def arnoldi_step(self, j: int, reorthogonalize=True, precision="fp64"):
         h = np.zeros(j + 1)
         beta = C.c_double(0.0)

@@ -421,3 +421,77 @@ def test_window_refused_for_nonsymmetric_matrix():
             ctx.expmv(v, 0.5, 30, precision="mixed", window=1)
         y, r = ctx.expmv(v, 0.5, 30, precision="mixed")  # the context stays usable
         assert r["converged"] == 1
+
+
+def _long_row_matrix(n=6000, seed=3):
+    """Rows longer than a tile (block sum), empty rows, rows at the tile
+    boundary, short random rows."""
+    from mexk import synthetic as S
+
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, 6, size=n)
+    lens[10], lens[11], lens[4000], lens[4001] = 5000, 0, 2049, 2048
+    cols = np.concatenate([np.sort(rng.choice(n, size=l, replace=False)) for l in lens])
+    rp = np.zeros(n + 1, dtype=np.int32)
+    np.cumsum(lens, out=rp[1:])
+    return S.CSR(n, rp, cols.astype(np.int32), rng.standard_normal(int(lens.sum())) * 0.05)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["powerlaw_n2048", "heat_N32", "long_rows"])
+def test_spmv_forms_give_identical_solves(name):
+    """The staged and the direct context SpMV compute the same products and
+    sum them in the same order: FP64 solves are bitwise the same whichever
+    form the context runs; mixed ones (whose two-column steps take their dots
+    from the staged SpMV) stay within 1e-6 of FP64 under both."""
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    if name == "long_rows":
+        A, v, t, m = _long_row_matrix(), None, 0.3, 20
+    elif name == "heat_N32":
+        A, v, t, m = S.laplacian_2d(96, h=1.0 / 2049), None, 1e-5, 30
+    else:
+        A, d = load_golden(name)
+        v, t, m = d["v"], float(d["t"]), int(d["m"])
+    if v is None:
+        v = np.random.default_rng(7).uniform(0, 1, A.n)
+    runs = [("mixed", "reference", 0), ("mixed", "search", 0)]
+    if name == "heat_N32":
+        runs.append(("mixed", "search", 2))
+    with Context(A, m_alloc=m) as ctx:
+        assert ctx.spmv_form("fp64") == ctx.spmv_form("mixed") == "staged"  # n < 65,536: every span narrow
+        out = {}
+        for form in ("staged", "direct"):
+            ctx.set_spmv_form(form, precision="fp64")
+            assert ctx.spmv_form("fp64") == form
+            out[form] = ctx.expmv(v, t, m, precision="fp64")
+        (y64, rs), (yd, rd) = out["staged"], out["direct"]
+        assert np.array_equal(y64, yd)
+        assert rs["attempts"] == rd["attempts"] and rs["cycles"] == rd["cycles"]
+        for prec, ctrl, w in runs:
+            for form in ("staged", "direct"):
+                ctx.set_spmv_form(form, precision=prec)
+                y, r = ctx.expmv(v, t, m, precision=prec, controller=ctrl, window=w)
+                assert r["converged"] == 1
+                assert rel(y, y64) <= 1e-6, (prec, ctrl, w, form, rel(y, y64))
+
+
+@pytest.mark.gpu
+def test_scattered_columns_choose_direct_form():
+    """A matrix whose row blocks span more than 65,536 columns runs the
+    direct SpMV form; its FP64 solve is bitwise that of the staged form."""
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    A = S.random_diag_dominant(200_000, 6, seed=4)
+    v = np.random.default_rng(4).standard_normal(A.n)
+    with Context(A, m_alloc=20) as ctx:
+        assert ctx.spmv_form("fp64") == ctx.spmv_form("mixed") == "direct"
+        y_d, r_d = ctx.expmv(v, 0.2, 20, precision="fp64")
+        ctx.set_spmv_form("staged", "fp64")
+        y_s, r_s = ctx.expmv(v, 0.2, 20, precision="fp64")
+        assert np.array_equal(y_d, y_s) and r_d["attempts"] == r_s["attempts"]
+        ctx.set_spmv_form("staged", "mixed")
+        y_m, _ = ctx.expmv(v, 0.2, 20, precision="mixed")
+        assert rel(y_m, y_d) <= 1e-6
