@@ -113,12 +113,18 @@ SPMV_F32_TRAFFIC_HEAT1536 = (89.869312e6 + 3.002624e6, 11790336)
 # 3.27 MB written.
 SPMV_DOTS_F32_TRAFFIC_HEAT1536 = (99.39968e6 + 3.26912e6, 11790336)
 
-def kernel_bytes(kind, n, nnz, k, fp32, window=0):
+def kernel_bytes(kind, n, nnz, k, fp32, window=0, form="staged"):
     """Algorithmic HBM bytes of one launch (per-kernel minimum traffic); with a
-    short-recurrence window the sweeps touch only the last `window` columns."""
+    short-recurrence window the sweeps touch only the last `window` columns.
+    The SpMV's matrix stream depends on its form: CSR (values, int32 columns,
+    row pointers) or the row-pattern form (one id byte per row)."""
     s = 4 if fp32 else 8
     if window and kind in ("gram_dot", "gram_update"):
         k = min(k, window)
+    if form == "pattern" and kind == "spmv":
+        return n + 2 * n * s  # row ids, x once, y
+    if form == "pattern" and kind == "spmv_dots":
+        return n + 3 * n * s
     if kind == "spmv":
         return nnz * (s + 4) + 4 * (n + 1) + 2 * n * s  # values+cols, row_ptr, x once, y
     if kind == "spmv_dots":  # the SpMV, then u_{j-1} read for the dots (u_j is x)
@@ -147,12 +153,12 @@ STEP_KINDS = {"fp64": ["spmv", "gs_dot", "gs_upd_dot", "gs_upd_norm", "normalize
               "mixed": ["spmv", "gram_dot", "gram_update"]}
 
 
-def step_kinds(precision, j, window=0, staged=True):
+def step_kinds(precision, j, window=0, dots_in_spmv=True):
     """Kernels of Arnoldi step j as a solve runs them: in mixed precision with
-    the staged SpMV a step j >= 1 over two columns (every step of a window of
-    2, step 1 of full Arnoldi) takes its dot products from the SpMV
-    (spmv_dots) and needs no dot sweep."""
-    if precision == "mixed" and staged:
+    the staged or the pattern SpMV a step j >= 1 over two columns (every step
+    of a window of 2, step 1 of full Arnoldi) takes its dot products from the
+    SpMV (spmv_dots) and needs no dot sweep."""
+    if precision == "mixed" and dots_in_spmv:
         lo = max(0, j + 1 - window) if window else 0
         if j >= 1 and j + 1 - lo <= 2:
             return ["spmv_dots", "gram_update"]
@@ -167,21 +173,22 @@ def profile_cycle(ctx, m, n, nnz, precision, iters=2, window=0):
     as the context's last solve ran them: with its window, if any)."""
     fp32 = precision == "mixed"
     once = CYCLE_KINDS[precision]
-    staged = ctx.spmv_form(precision) == "staged"
+    form = ctx.spmv_form(precision)
+    dots_in_spmv = form != "direct"
     per = {}
 
     def add(kind, j, k):
         ms = ctx.profile_kernel(kind, j, iters, precision)
         p = per.setdefault(kind, {"ms": 0.0, "bytes": 0.0, "launches": 0})
         p["ms"] += ms
-        p["bytes"] += kernel_bytes(kind, n, nnz, k, fp32, window)
+        p["bytes"] += kernel_bytes(kind, n, nnz, k, fp32, window, form)
         p["launches"] += 1
 
     # The controller first: it runs on the Hessenberg matrix the last solve left.
     for kind in once:
         add(kind, m - 1, m)
     for j in range(m):
-        for kind in step_kinds(precision, j, window, staged):
+        for kind in step_kinds(precision, j, window, dots_in_spmv):
             add(kind, j, j + 1)
     return per
 
@@ -195,8 +202,9 @@ def launches_per_solve(ctx, precision, res, m, window=0):
     if len(sizes) != res["cycles"]:  # rejects reuse their cycle's basis
         sizes = [m] * res["cycles"]
     per_cycle = 4 if precision == "mixed" else 3
-    staged = ctx.spmv_form(precision) == "staged"
-    return 2 + sum(sum(len(step_kinds(precision, j, window, staged)) for j in range(k)) + per_cycle for k in sizes)
+    dots_in_spmv = ctx.spmv_form(precision) != "direct"
+    return 2 + sum(sum(len(step_kinds(precision, j, window, dots_in_spmv)) for j in range(k)) + per_cycle
+                   for k in sizes)
 
 
 def gs_cgs2_equivalent(per, n, m, precision):
@@ -402,7 +410,7 @@ def run_ours(args, rank, world, local_rank):
     dom = max(per, key=lambda k: per[k]["ms"])
     ach = per[dom]["bytes"] / (per[dom]["ms"] / 1e3) / 1e9
     traffic, tsrc = None, None
-    if dom in ("spmv", "spmv_dots") and form != "fp64":
+    if dom in ("spmv", "spmv_dots") and form != "fp64" and ctx.spmv_form(form) == "staged":
         mb, nz = SPMV_DOTS_F32_TRAFFIC_HEAT1536 if dom == "spmv_dots" else SPMV_F32_TRAFFIC_HEAT1536
         traffic = mb * nnz / nz
         tsrc = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the {dom} kernel on the "
@@ -445,8 +453,12 @@ def run_ours(args, rank, world, local_rank):
                       "restarts_done": res_c["restarts_done"], "converged": res_c["converged"],
                       "fp64_attempts": res64["attempts"], "fp64_cycles": res64["cycles"]},
             "forms_checked": [{k: v for k, v in c.items() if k != "steps"} for c in checked],
-            "spmv": {"gbs": spmv_gbs, "frac": spmv_gbs / peak, "precision": form,
-                     "fp64_gbs": sp64["bytes"] / (sp64["ms"] / 1e3) / 1e9},
+            "spmv": {"gbs": spmv_gbs, "frac": spmv_gbs / peak, "precision": form, "form": ctx.spmv_form(form),
+                     "us": 1e3 * sp["ms"] / sp["launches"],
+                     "csr_bytes_gbs": kernel_bytes("spmv", n, nnz, 1, form != "fp64") * sp["launches"]
+                     / (sp["ms"] / 1e3) / 1e9,
+                     "fp64_gbs": sp64["bytes"] / (sp64["ms"] / 1e3) / 1e9,
+                     "fp64_us": 1e3 * sp64["ms"] / sp64["launches"]},
             "kernel_share": {k: round(p["ms"] / tot_ms, 4) for k, p in per.items()},
             "kernels": {f: {k: {"ms_per_cycle": round(p["ms"], 4),
                                 "gbs": round(p["bytes"] / (p["ms"] / 1e3) / 1e9, 1) if p["bytes"] else None}

@@ -331,29 +331,39 @@ int mexk_batch_destroy(mexk_batch_t b);
 #define MEXK_KERNEL_KINDS 11
 
 /* Times `iters` launches of one solver kernel for Arnoldi step j (k = j+1
- * basis columns) on the context stream with a CUDA event pair around each
- * launch, on the context's current basis and matrix (run a solve first).
- * Each launch starts from a fresh running state. *ms_per_launch = mean
- * launch duration in milliseconds. No reference counterpart (the reference
+ * basis columns) on the context stream with CUDA events, on the context's
+ * current basis and matrix (run a solve first), from a fresh running state:
+ * the controller and the lift (which change that state) get a fresh copy and
+ * an event pair each; every other kind runs one untimed launch, then the
+ * iters launches back to back between one event pair, as they follow one
+ * another in a solve. *ms_per_launch = mean launch duration in
+ * milliseconds. No reference counterpart (the reference
  * times only the whole solve, METRIC total_compute_expmv_ms at main.cu:1570).
  * A kind marked FP64 or mixed returns MEXK_ERR_UNSUPPORTED for the other
  * precision. The mixed sweeps use the ortho_window, and the controller kind
  * the controller, of the context's last solve. */
 int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int iters, double* ms_per_launch);
 
-/* Which form of the context SpMV runs for a precision: MEXK_SPMV_STAGED
- * (persistent blocks, matrix tiles staged into shared memory by bulk copies;
- * the mixed steps over two columns also accumulate their dot products in it)
- * or MEXK_SPMV_DIRECT (one block per row block, loads straight from HBM).
- * At upload the context picks direct when some row block's columns span
- * 65,536 or more (gathers scattered over x, where more blocks in flight keep
- * more gathers outstanding), staged otherwise; the setter overrides that.
- * Both forms compute the same products and row sums, so FP64 solves are
- * bitwise equal under either; mixed solves take the two-column steps' dots
- * from a different sum order and agree to rounding. No reference
- * counterpart: the reference's SpMV is one cuSPARSE call (main.cu:1743). */
+/* Which form of the context SpMV runs for a precision:
+ * MEXK_SPMV_STAGED (persistent blocks, CSR row blocks staged into shared
+ * memory by bulk copies), MEXK_SPMV_DIRECT (one block per CSR row block,
+ * loads straight from HBM) or MEXK_SPMV_PATTERN (one byte per row naming one
+ * of at most 256 distinct rows -- offsets col - row and values, at most 16
+ * entries -- held in a table: stencil matrices). The staged and the pattern
+ * form also accumulate the mixed two-column steps' dot products. At upload
+ * the context picks the pattern form when every row is one of at most 256
+ * such patterns (detected and verified on the device), else direct when
+ * some row block's columns span 65,536 or more (gathers scattered over x,
+ * where more blocks in flight keep more gathers outstanding), else staged;
+ * the setter overrides that (MEXK_ERR_UNSUPPORTED: pattern form requested
+ * for a matrix without one). All forms compute the same products and add
+ * each row's in column order, so FP64 solves are bitwise equal under any;
+ * mixed solves take the two-column steps' dots in a form-dependent order and
+ * agree to rounding. No reference counterpart: the reference's SpMV is one
+ * cuSPARSE call (main.cu:1743). */
 #define MEXK_SPMV_STAGED 0
 #define MEXK_SPMV_DIRECT 1
+#define MEXK_SPMV_PATTERN 2
 int mexk_context_get_spmv_form(mexk_context_t ctx, int precision, int* form);
 int mexk_context_set_spmv_form(mexk_context_t ctx, int precision, int form);
 

@@ -267,6 +267,33 @@ struct SpmvSchedule {
 };
 int build_spmv_schedule(int n, const int* row_ptr, const int* d_col, SpmvSchedule* out, cudaStream_t s);
 
+// Row-pattern form of the context SpMV (spmv_pattern.cu): pattern p has
+// len[p] <= PAT_LEN entries, column offsets off[p * PAT_LEN + q] (col - row,
+// ascending) and values v64 / v32 (the FP32 copy rounded to nearest); row r
+// is pattern pid[r]. keys / ids: the detection's hash table.
+constexpr int PAT_MAX = 256;
+constexpr int PAT_LEN = 16;
+constexpr int PAT_SLOTS = 1024;
+constexpr int PAT_ROW_ALIGN = 1024;  // pid is padded with zeros to a multiple of this
+struct RowPatterns {
+    unsigned long long keys[PAT_SLOTS];
+    int ids[PAT_SLOTS];
+    int count;
+    int rows[PAT_MAX];  // rows of each pattern
+    int len[PAT_MAX];
+    int off[PAT_MAX * PAT_LEN];
+    double v64[PAT_MAX * PAT_LEN];
+    float v32[PAT_MAX * PAT_LEN];
+};
+// Detects the patterns of the device CSR (d_pid: n rounded up to
+// PAT_ROW_ALIGN bytes, zero-filled by the caller); *ok when every row is one
+// of at most PAT_MAX patterns of at most PAT_LEN entries; *major = the
+// pattern with the most rows, *major_len its length, *max_len the longest
+// pattern's. Synchronises s.
+int build_row_patterns(int n, const int* d_row_ptr, const int* d_col, const double* d_val, RowPatterns* d_T,
+                       uint8_t* d_pid, int* d_flags, bool* ok, int* major, int* major_len, int* max_len,
+                       cudaStream_t s);
+
 // Upload stages shared by mexk_context_upload_csr and the .bincsr loader:
 // begin sets the sizes and allocates the context's CSR arrays (padded, zero
 // tails); the caller fills row_ptr[0..rows], col_idx and values; finish
@@ -297,6 +324,10 @@ template <typename TA, typename TX>
 int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bool all_narrow, const int* row_ptr,
                 const int* col_idx, const TA* values, const TX* x, TX* y, const int* skip_flag, int* status,
                 cudaStream_t s, const GramArgs* dots = nullptr, bool direct = false);
+// w = A x in the pattern form; dots as for launch_spmv (FP32 only).
+template <typename TX>
+int launch_spmv_pattern(int n, int major, int major_len, int max_len, const uint8_t* pid, const RowPatterns* T,
+                        const TX* x, TX* y, const int* skip_flag, cudaStream_t s, const GramArgs* dots = nullptr);
 
 // ------------------------------------------------------------ Gram-Schmidt
 enum GsMode : int { GS_DOT = 0, GS_UPD_DOT = 1, GS_UPD_NORM = 2 };

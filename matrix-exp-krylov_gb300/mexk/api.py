@@ -167,12 +167,14 @@ class Context:
               "mexk_profile_kernel")
         return ms.value
 
-    SPMV_FORMS = ("staged", "direct")
+    SPMV_FORMS = ("staged", "direct", "pattern")
 
     def spmv_form(self, precision="fp64") -> str:
-        """The SpMV form the context runs for a precision: "staged" (tiles
-        staged in shared memory; the default when every row block's columns
-        span less than 65,536) or "direct" (one block per row block)."""
+        """The SpMV form the context runs for a precision: "pattern" (one
+        byte per row naming one of <= 256 distinct rows; the default when the
+        matrix has that form), "staged" (CSR tiles staged in shared memory;
+        the default when every row block's columns span less than 65,536) or
+        "direct" (one block per CSR row block)."""
         f = C.c_int(0)
         check(lib().mexk_context_get_spmv_form(self._h, PRECISIONS[precision], C.byref(f)),
               "mexk_context_get_spmv_form")

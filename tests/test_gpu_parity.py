@@ -438,12 +438,12 @@ def _long_row_matrix(n=6000, seed=3):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["powerlaw_n2048", "heat_N32", "long_rows"])
+@pytest.mark.parametrize("name", ["powerlaw_n2048", "heat_N32", "convdiff_N8_pe100", "long_rows"])
 def test_spmv_forms_give_identical_solves(name):
-    """The staged and the direct context SpMV compute the same products and
-    sum them in the same order: FP64 solves are bitwise the same whichever
-    form the context runs; mixed ones (whose two-column steps take their dots
-    from the staged SpMV) stay within 1e-6 of FP64 under both."""
+    """Every SpMV form computes the same products and adds each row's in
+    column order: FP64 solves are bitwise the same whichever form the context
+    runs; mixed ones (whose two-column steps take their dots in a
+    form-dependent order) stay within 1e-6 of FP64 under all."""
     from mexk import synthetic as S
     from mexk.api import Context
 
@@ -456,21 +456,26 @@ def test_spmv_forms_give_identical_solves(name):
         v, t, m = d["v"], float(d["t"]), int(d["m"])
     if v is None:
         v = np.random.default_rng(7).uniform(0, 1, A.n)
+    stencil = name in ("heat_N32", "convdiff_N8_pe100")
     runs = [("mixed", "reference", 0), ("mixed", "search", 0)]
     if name == "heat_N32":
         runs.append(("mixed", "search", 2))
     with Context(A, m_alloc=m) as ctx:
-        assert ctx.spmv_form("fp64") == ctx.spmv_form("mixed") == "staged"  # n < 65,536: every span narrow
+        default = "pattern" if stencil else "staged"  # n < 65,536: every CSR span narrow
+        assert ctx.spmv_form("fp64") == ctx.spmv_form("mixed") == default
+        forms = ("staged", "direct") + (("pattern",) if stencil else ())
         out = {}
-        for form in ("staged", "direct"):
+        for form in forms:
             ctx.set_spmv_form(form, precision="fp64")
             assert ctx.spmv_form("fp64") == form
             out[form] = ctx.expmv(v, t, m, precision="fp64")
-        (y64, rs), (yd, rd) = out["staged"], out["direct"]
-        assert np.array_equal(y64, yd)
-        assert rs["attempts"] == rd["attempts"] and rs["cycles"] == rd["cycles"]
+        y64, r64 = out["staged"]
+        for form in forms[1:]:
+            y, r = out[form]
+            assert np.array_equal(y, y64), form
+            assert r["attempts"] == r64["attempts"] and r["cycles"] == r64["cycles"]
         for prec, ctrl, w in runs:
-            for form in ("staged", "direct"):
+            for form in forms:
                 ctx.set_spmv_form(form, precision=prec)
                 y, r = ctx.expmv(v, t, m, precision=prec, controller=ctrl, window=w)
                 assert r["converged"] == 1
@@ -482,12 +487,15 @@ def test_scattered_columns_choose_direct_form():
     """A matrix whose row blocks span more than 65,536 columns runs the
     direct SpMV form; its FP64 solve is bitwise that of the staged form."""
     from mexk import synthetic as S
+    from mexk._lib import MexkError
     from mexk.api import Context
 
     A = S.random_diag_dominant(200_000, 6, seed=4)
     v = np.random.default_rng(4).standard_normal(A.n)
     with Context(A, m_alloc=20) as ctx:
         assert ctx.spmv_form("fp64") == ctx.spmv_form("mixed") == "direct"
+        with pytest.raises(MexkError, match="row-pattern"):
+            ctx.set_spmv_form("pattern", "fp64")
         y_d, r_d = ctx.expmv(v, 0.2, 20, precision="fp64")
         ctx.set_spmv_form("staged", "fp64")
         y_s, r_s = ctx.expmv(v, 0.2, 20, precision="fp64")
@@ -495,3 +503,59 @@ def test_scattered_columns_choose_direct_form():
         ctx.set_spmv_form("staged", "mixed")
         y_m, _ = ctx.expmv(v, 0.2, 20, precision="mixed")
         assert rel(y_m, y_d) <= 1e-6
+
+
+def _banded(n, offsets, vals_of_row, drop=()):
+    """CSR with entries at row + offset (inside [0, n)), values from
+    vals_of_row(r) (one per offset), rows in `drop` empty."""
+    from mexk import synthetic as S
+
+    rp, ci, va = [0], [], []
+    for r in range(n):
+        if r not in drop:
+            vr = vals_of_row(r)
+            for o, a in zip(offsets, vr):
+                if 0 <= r + o < n:
+                    ci.append(r + o)
+                    va.append(a)
+        rp.append(len(ci))
+    return S.CSR(n, np.array(rp, np.int32), np.array(ci, np.int32), np.array(va, np.float64))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["empty_rows", "256_patterns", "257_patterns", "row_of_17", "row_of_16",
+                                  "ragged_tail"])
+def test_row_pattern_detection(case):
+    """The pattern form is taken exactly when every row is one of <= 256
+    patterns of <= 16 entries; when taken, FP64 solves are bitwise those of
+    the staged CSR form (empty rows, the last partial chunk of rows
+    included)."""
+    from mexk.api import Context
+
+    offs5 = (-40, -1, 0, 1, 40)
+    base = (0.3, 0.2, -1.5, 0.25, 0.1)
+    if case == "empty_rows":
+        A, want = _banded(5000, offs5, lambda r: base, drop={0, 17, 2500, 4999}), "pattern"
+    elif case == "256_patterns":  # 254 diagonal values in the interior + the first and the last row
+        A, want = _banded(3000, (-1, 0, 1), lambda r: (0.1, -1.0 - (r % 254) / 1000, 0.2)), "pattern"
+    elif case == "257_patterns":
+        A, want = _banded(3000, (-1, 0, 1), lambda r: (0.1, -1.0 - (r % 255) / 1000, 0.2)), "staged"
+    elif case == "row_of_17":
+        offs = tuple(range(-8, 9))
+        A, want = _banded(2000, offs, lambda r: [0.01] * 8 + [-1.0] + [0.01] * 8), "staged"
+    elif case == "row_of_16":
+        offs = tuple(range(-8, 8))
+        A, want = _banded(2000, offs, lambda r: [0.01] * 8 + [-1.0] + [0.01] * 7), "pattern"
+    else:  # n not a multiple of the 1024-row chunk nor of 4
+        A, want = _banded(1024 * 3 + 7, offs5, lambda r: base), "pattern"
+    v = np.random.default_rng(2).uniform(-1, 1, A.n)
+    with Context(A, m_alloc=20) as ctx:
+        assert ctx.spmv_form("fp64") == want
+        if want != "pattern":
+            return
+        y_p, r_p = ctx.expmv(v, 0.4, 20, precision="fp64")
+        ctx.set_spmv_form("staged", "fp64")
+        y_s, r_s = ctx.expmv(v, 0.4, 20, precision="fp64")
+        assert np.array_equal(y_p, y_s) and r_p["attempts"] == r_s["attempts"]
+        y_m, _ = ctx.expmv(v, 0.4, 20, precision="mixed")
+        assert rel(y_m, y_s) <= 1e-6
