@@ -112,6 +112,9 @@ SPMV_F32_TRAFFIC_HEAT1536 = (89.869312e6 + 3.002624e6, 11790336)
 # (spmv_stream_kernel<float, float, 1, 1>): 99.40 MB read (u_{j-1} too) +
 # 3.27 MB written.
 SPMV_DOTS_F32_TRAFFIC_HEAT1536 = (99.39968e6 + 3.26912e6, 11790336)
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of the row-pattern SpMV
+# with dots on the 1536^2 heat grid (2,359,296 rows): (bytes, rows).
+PAT_DOTS_F32_TRAFFIC_HEAT1536 = (21.274624e6, 2359296)
 
 def kernel_bytes(kind, n, nnz, k, fp32, window=0, form="staged"):
     """Algorithmic HBM bytes of one launch (per-kernel minimum traffic); with a
@@ -410,7 +413,12 @@ def run_ours(args, rank, world, local_rank):
     dom = max(per, key=lambda k: per[k]["ms"])
     ach = per[dom]["bytes"] / (per[dom]["ms"] / 1e3) / 1e9
     traffic, tsrc = None, None
-    if dom in ("spmv", "spmv_dots") and form != "fp64" and ctx.spmv_form(form) == "staged":
+    if dom == "spmv_dots" and form != "fp64" and ctx.spmv_form(form) == "pattern":
+        mb, rows = PAT_DOTS_F32_TRAFFIC_HEAT1536
+        traffic = mb * n / rows
+        tsrc = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the row-pattern spmv_dots kernel on the "
+                "1536^2 heat grid (2,359,296 rows), scaled by rows")
+    elif dom in ("spmv", "spmv_dots") and form != "fp64" and ctx.spmv_form(form) == "staged":
         mb, nz = SPMV_DOTS_F32_TRAFFIC_HEAT1536 if dom == "spmv_dots" else SPMV_F32_TRAFFIC_HEAT1536
         traffic = mb * nnz / nz
         tsrc = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the {dom} kernel on the "
