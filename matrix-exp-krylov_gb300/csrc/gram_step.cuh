@@ -78,6 +78,9 @@ __device__ __forceinline__ int step2_slot(int v, int kw, int lo) {
 // entry G(j-1, j), c = s s_j a, h = c - (G - I) c, H(:, j), the update
 // coefficients and the pre-scale p of the next column (one rsqrt, a few
 // products, one rsqrt).
+// PR: partials loaded per lane and round (20: one round for up to 640 row
+// blocks, where the caller's registers allow).
+template <int PR = 16>
 __device__ __forceinline__ void step2_finish(const GramArgs& g, int nrb_a, int nrb_b) {
     DevState* st = g.st;
     const int j = g.j;
@@ -91,47 +94,33 @@ __device__ __forceinline__ void step2_finish(const GramArgs& g, int nrb_a, int n
     for (int r = t; r < lo; r += blockDim.x) g.H[r + static_cast<size_t>(j) * ldh] = 0.0;  // outside the window
     const double s0 = kw == 2 ? gs->s[lo] : 0.0;
     const double ip_j = gs->ip[j];
-    step_sum_partials<16>(
+    step_sum_partials<PR>(
         g.part, 2 * kw + 1, [&](int v) { return step2_slot(v, kw, lo); },
         [&](int v) { return (v >= kw && v < 2 * kw) ? nrb_b : nrb_a; }, s_tot);
     __syncthreads();
     if (t != 0) return;
     const double bj = s_tot[2 * kw - 1];
     const double sj = (bj > 0.0 && !isinf(bj)) ? rsqrt(bj) : 0.0;
-    if (j >= 1) {
-        const double beta = sqrt(bj) * ip_j;
-        const bool bad = !(beta >= 1e-14) || isinf(beta);
-        g.H[j + static_cast<size_t>(j - 1) * ldh] = bad ? 0.0 : beta;
-        if (bad) {
-            st->breakdown = 1;
-            st->k_used = j;
-            return;
-        }
-    }
-    gs->s[j] = sj;
-    G[j + static_cast<size_t>(j) * GRAM_LD] = 1.0;
+    // H(j, j-1) and the breakdown test: the square root runs beside the
+    // chain below, which writes nothing until the test has passed
+    const double beta = j >= 1 ? sqrt(bj) * ip_j : 1.0;
+    const bool bad = !(beta >= 1e-14) || isinf(beta);
     const double sj2 = sj * sj;
     const double cj = sj2 * s_tot[kw - 1];
-    double hj = cj, part;
+    double hj = cj, hp = 0.0, g01 = 0.0, part;
     if (kw == 2) {
-        const double g01 = (s0 * s_tot[kw]) * sj;  // G(j-1, j)
-        const double cp = (s0 * s_tot[0]) * sj;    // c_{j-1}
-        G[lo + static_cast<size_t>(j) * GRAM_LD] = g01;
-        G[j + static_cast<size_t>(lo) * GRAM_LD] = g01;
-        double hp = cp;
+        g01 = (s0 * s_tot[kw]) * sj;              // G(j-1, j)
+        const double cp = (s0 * s_tot[0]) * sj;  // c_{j-1}
+        hp = cp;
         if (g.reortho) {
             hp = cp - __dmul_rn(g01, cj);
             hj = cj - __dmul_rn(g01, cp);
         }
-        g.H[lo + static_cast<size_t>(j) * ldh] = hp;
-        gs->coef[lo] = static_cast<float>(s0 * hp);
         const double gh0 = fma(g01, hj, hp), gh1 = hj + __dmul_rn(g01, hp);
         part = hp * (gh0 - 2.0 * cp) + hj * (gh1 - 2.0 * cj);
     } else {
         part = hj * (hj - 2.0 * cj);
     }
-    g.H[j + static_cast<size_t>(j) * ldh] = hj;
-    gs->coef[j] = static_cast<float>(sj * hj);
     const double w2 = sj2 * s_tot[2 * kw];
     const double u2 = w2 + part;
     double p = 1.0, ip = 1.0;
@@ -142,6 +131,22 @@ __device__ __forceinline__ void step2_finish(const GramArgs& g, int nrb_a, int n
         p = rsqrt(w2);
         ip = w2 * p;
     }
+    if (j >= 1) g.H[j + static_cast<size_t>(j - 1) * ldh] = bad ? 0.0 : beta;
+    if (j >= 1 && bad) {
+        st->breakdown = 1;
+        st->k_used = j;
+        return;
+    }
+    gs->s[j] = sj;
+    G[j + static_cast<size_t>(j) * GRAM_LD] = 1.0;
+    if (kw == 2) {
+        G[lo + static_cast<size_t>(j) * GRAM_LD] = g01;
+        G[j + static_cast<size_t>(lo) * GRAM_LD] = g01;
+        g.H[lo + static_cast<size_t>(j) * ldh] = hp;
+        gs->coef[lo] = static_cast<float>(s0 * hp);
+    }
+    g.H[j + static_cast<size_t>(j) * ldh] = hj;
+    gs->coef[j] = static_cast<float>(sj * hj);
     gs->ip[j + 1] = ip;
     gs->wsc = static_cast<float>(sj);
     gs->psc = static_cast<float>(p);

@@ -163,9 +163,9 @@ constexpr unsigned PAT_FULL = 0xffffffffu;
 // rows) has major_len entries, whose offsets and values are held in
 // registers from the start. A warp whose 128 rows are all major goes
 // straight to its gathers; any other warp takes each non-major row's
-// offsets and values from the table -- all entries of two rows of the
-// thread requested together, so a boundary costs two more round trips, not
-// one per entry. Either way a row's products are formed and added in
+// offsets and values from the table -- all entries of a row (two rows
+// without DOTS, whose registers allow it) requested together, so a boundary
+// costs a round trip per row, not one per entry. Either way a row's products are formed and added in
 // entry order from zero. With DOTS (FP32 mixed form, a step j >= 1 over
 // columns j-1 and j) each row sum also accumulates u_{j-1} w, u_j w, |w|^2
 // and the last block finishes the step, as the staged CSR form does.
@@ -200,12 +200,19 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
         mo[q] = on ? __ldg(toff + major * PAT_LEN + q) : 0;
         ma[q] = on ? __ldg(tv + major * PAT_LEN + q) : TX(0);
     }
+    int q0 = -1;  // the major pattern's entry at offset 0, if any
+#pragma unroll
+    for (int q = 0; q < LMAX; ++q)
+        if (q < major_len && mo[q] == 0) q0 = q;
     int c = blockIdx.x;
     load_ids(c, 0);
     pdl_wait();
     if (skip != nullptr && *skip) return;
     pdl_trigger();
     float da0 = 0.f, da1 = 0.f, dw = 0.f;
+    // DOTS: columns j-1 and j of the basis
+    const float* __restrict__ vlo = DOTS ? ga.V + static_cast<size_t>(ga.lo) * static_cast<size_t>(ga.ldv) : nullptr;
+    const float* __restrict__ vj = DOTS ? ga.V + static_cast<size_t>(ga.j) * static_cast<size_t>(ga.ldv) : nullptr;
     for (int k = 0; c < nchunk; c += gridDim.x, ++k) {
         const int r0 = c * PAT_CHUNK + wrow(k);
         int cur[PAT_RPT];
@@ -214,38 +221,66 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
         load_ids(c + gridDim.x, k + 1);
         float up[PAT_RPT], uj[PAT_RPT];
         if constexpr (DOTS) {
-            const size_t ldv = static_cast<size_t>(ga.ldv);
+#pragma unroll
+            for (int i = 0; i < PAT_RPT; ++i) up[i] = r0 + i * 32 < n ? __ldg(vlo + (r0 + i * 32)) : 0.f;
+        }
+        auto load_uj = [&]() {  // u_j = x at the thread's rows
+            if constexpr (DOTS) {
+#pragma unroll
+                for (int i = 0; i < PAT_RPT; ++i) uj[i] = r0 + i * 32 < n ? __ldg(vj + (r0 + i * 32)) : 0.f;
+            }
+        };
+        // rows [r0, r0 + 32 i] in range and their sums in s: store, accumulate the dots
+        auto emit = [&](const TX (&s)[PAT_RPT], bool all_in) {
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i) {
                 const int r = r0 + i * 32;
-                up[i] = r < n ? __ldg(ga.V + static_cast<size_t>(ga.lo) * ldv + r) : 0.f;
-                uj[i] = r < n ? __ldg(ga.V + static_cast<size_t>(ga.j) * ldv + r) : 0.f;
+                if (all_in || r < n) {
+                    y[r] = s[i];
+                    if constexpr (DOTS) {
+                        const float sf = static_cast<float>(s[i]);
+                        da0 = fmaf(up[i], sf, da0);
+                        da1 = fmaf(uj[i], sf, da1);
+                        dw = fmaf(sf, sf, dw);
+                    }
+                }
             }
-        }
+        };
         bool all_major = r0 + (PAT_RPT - 1) * 32 < n;
 #pragma unroll
         for (int i = 0; i < PAT_RPT; ++i) all_major = all_major && cur[i] == major;
         TX s[PAT_RPT];
         if (__all_sync(PAT_FULL, all_major)) {
             const TX* xb = x + r0;
+            if (q0 < 0) load_uj();
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i) {
                 TX acc = TX(0);
 #pragma unroll
-                for (int q = 0; q < LMAX; ++q)
-                    if (q < major_len) acc += pat_mul(ma[q], __ldg(xb + (i * 32 + mo[q])));
+                for (int q = 0; q < LMAX; ++q) {
+                    if (q < major_len) {
+                        const TX xq = __ldg(xb + (i * 32 + mo[q]));
+                        if constexpr (DOTS) {
+                            if (q == q0) uj[i] = xq;  // the diagonal entry gathers u_j at the row itself
+                        }
+                        acc += pat_mul(ma[q], xq);
+                    }
+                }
                 s[i] = acc;
             }
+            emit(s, true);
         } else {
+            load_uj();
+            constexpr int GP = DOTS ? 1 : 2;  // rows whose entries are in flight together
             int len[PAT_RPT];
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i)
                 len[i] = r0 + i * 32 < n ? (cur[i] == major ? major_len : __ldg(tlen + cur[i])) : 0;
 #pragma unroll
-            for (int i0 = 0; i0 < PAT_RPT; i0 += 2) {
-                TX av[2][LMAX], xv[2][LMAX];
+            for (int i0 = 0; i0 < PAT_RPT; i0 += GP) {
+                TX av[GP][LMAX], xv[GP][LMAX];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
+                for (int h = 0; h < GP; ++h) {
                     const int i = i0 + h;
                     const bool maj = cur[i] == major;
                     const int* to = toff + cur[i] * PAT_LEN;
@@ -259,7 +294,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
                     }
                 }
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
+                for (int h = 0; h < GP; ++h) {
                     TX acc = TX(0);
 #pragma unroll
                     for (int q = 0; q < LMAX; ++q)
@@ -267,19 +302,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
                     s[i0 + h] = acc;
                 }
             }
-        }
-#pragma unroll
-        for (int i = 0; i < PAT_RPT; ++i) {
-            const int r = r0 + i * 32;
-            if (r < n) {
-                y[r] = s[i];
-                if constexpr (DOTS) {
-                    const float sf = static_cast<float>(s[i]);
-                    da0 = fmaf(up[i], sf, da0);
-                    da1 = fmaf(uj[i], sf, da1);
-                    dw = fmaf(sf, sf, dw);
-                }
-            }
+            emit(s, false);
         }
     }
     if constexpr (DOTS) {
@@ -294,7 +317,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
         step_write_partials(s_red, ga.part, blockIdx.x, [&](int q) { return q < 2 ? jj - 1 + q : GRAM_NWOFF; });
         __shared__ int s_flag;
         if (!grid_last_block(ga.counter, &s_flag)) return;
-        step2_finish(ga, gridDim.x, ga.b_blocks);
+        step2_finish<20>(ga, gridDim.x, ga.b_blocks);  // <= 640 blocks: one round of partial loads
     }
 }
 
