@@ -333,11 +333,12 @@ int mexk_batch_destroy(mexk_batch_t b);
 /* Times `iters` launches of one solver kernel for Arnoldi step j (k = j+1
  * basis columns) on the context stream with CUDA events, on the context's
  * current basis and matrix (run a solve first), from a fresh running state:
- * the controller and the lift (which change that state) get a fresh copy and
- * an event pair each; every other kind runs one untimed launch, then the
+ * the kinds whose launch leaves its inputs unchanged (SpMV, SpMV with dots,
+ * the mixed sweeps, the FP64 pass-1 dots) run one untimed launch, then the
  * iters launches back to back between one event pair, as they follow one
- * another in a solve. *ms_per_launch = mean launch duration in
- * milliseconds. No reference counterpart (the reference
+ * another in a solve; the others (controller, lift, FP64 update passes,
+ * normalise) get a fresh copy of the state and an event pair each.
+ * *ms_per_launch = mean launch duration in milliseconds. No reference counterpart (the reference
  * times only the whole solve, METRIC total_compute_expmv_ms at main.cu:1570).
  * A kind marked FP64 or mixed returns MEXK_ERR_UNSUPPORTED for the other
  * precision. The mixed sweeps use the ortho_window, and the controller kind

@@ -19,15 +19,16 @@ namespace mexk {
 namespace {
 
 constexpr int LIFT_THREADS = 256;
+constexpr int LIFT_BLOCKS_PER_SM = 6;  // a strided multi-column read wants many warps in flight
 
-// RPT rows of y = sum_c coef_c V_c, columns loaded 8 at a time (16-byte
-// row groups). FP64 basis: one DFMA chain per row in column order (the axpy
+// RPT rows of y = sum_c coef_c V_c, columns loaded 4 at a time (16-byte
+// row groups; 40 registers, so 6 blocks of 256 threads fit an SM). FP64 basis: one DFMA chain per row in column order (the axpy
 // order). FP32 basis: FP32 products summed with compensation and widened
 // once per row, so the FP64 pipe does O(1) work per row, not O(k).
 template <typename TV, int RPT>
 __device__ __forceinline__ void lift_rows(const TV* __restrict__ V, size_t ldv, size_t r0, int k, const double* c64,
                                           const float* c32, double (&y)[RPT]) {
-    constexpr int CH = 8;
+    constexpr int CH = 4;
     using IO = RowIO<RPT, TV>;
     if constexpr (sizeof(TV) == 8) {
         double s[RPT];
@@ -74,7 +75,7 @@ __device__ __forceinline__ void lift_rows(const TV* __restrict__ V, size_t ldv, 
 }
 
 template <typename TV>
-__global__ void __launch_bounds__(LIFT_THREADS) lift_kernel(LiftArgs a) {
+__global__ void __launch_bounds__(LIFT_THREADS, LIFT_BLOCKS_PER_SM) lift_kernel(LiftArgs a) {
     constexpr int RPT = 16 / sizeof(TV);
     __shared__ double s_coef[MEXK_M_MAX + 1];
     __shared__ float s_coef32[MEXK_M_MAX + 1];
@@ -184,7 +185,11 @@ int elementwise_grid(int n) {
 }  // namespace
 
 template <typename TV>
-int launch_lift(const LiftArgs& a, int grid, cudaStream_t s) {
+int launch_lift(const LiftArgs& a, int /*grid*/, cudaStream_t s) {
+    constexpr int RPT = 16 / static_cast<int>(sizeof(TV));
+    const long long need = (static_cast<long long>(a.n) + RPT * LIFT_THREADS - 1) / (RPT * LIFT_THREADS);
+    const long long cap = static_cast<long long>(device_sm_count()) * LIFT_BLOCKS_PER_SM;
+    const int grid = static_cast<int>(need < cap ? (need < 1 ? 1 : need) : cap);
     lift_kernel<TV><<<grid, LIFT_THREADS, 0, s>>>(a);
     MEXK_CK_LAUNCH("lift_kernel");
     return MEXK_OK;

@@ -1107,12 +1107,15 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
         *ms_out = ms;
         return MEXK_OK;
     };
-    // The controller and the lift change the running state: each launch
-    // starts from a fresh copy. Every other kind leaves its inputs as they
-    // were, so it is timed as a back-to-back run of iters launches (one event
-    // pair, as the launches follow one another in a solve's graph) after one
-    // untimed launch.
-    const bool reset_each = kind == MEXK_KERNEL_CONTROLLER || kind == MEXK_KERNEL_LIFT;
+    // Kinds that leave their inputs as they were (the SpMVs, the mixed
+    // sweeps, the FP64 pass-1 dots) are timed as a back-to-back run of iters
+    // launches (one event pair, as the launches follow one another in a
+    // solve's graph) after one untimed launch. The others change the running
+    // state or update w in place (controller, lift, the FP64 update passes,
+    // normalise): each launch starts from a fresh copy of the state.
+    const bool reset_each = !(kind == MEXK_KERNEL_SPMV || kind == MEXK_KERNEL_SPMV_DOTS ||
+                              kind == MEXK_KERNEL_GRAM_DOT || kind == MEXK_KERNEL_GRAM_UPDATE ||
+                              kind == MEXK_KERNEL_GRAM_NORM || kind == MEXK_KERNEL_GS_DOT);
     if (reset_each) {
         for (int it = 0; it < iters && rc == MEXK_OK; ++it) {
             cudaError_t ce = cudaMemcpyAsync(ctx->d_state, h_run, sizeof(DevState), cudaMemcpyHostToDevice, s);
