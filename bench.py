@@ -17,6 +17,7 @@ CSR (251 MB) exceed the 129 MB L2, so no extra flush runs between steps.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -46,7 +47,11 @@ def measured_peaks():
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi samples every 20 ms (clocks, power, throttle reasons),
+    started before the timed region and waited on until its first sample;
+    summary() keeps the samples whose timestamps fall inside the region
+    marked by begin()/end() (all samples when none do)."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -54,16 +59,29 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.file = None
+        self.t_begin = self.t_end = None
 
     def __enter__(self):
         try:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.file, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return self
+        deadline = time.time() + 5.0  # the first sample, so the timed region is covered
+        while time.time() < deadline and self.proc.poll() is None:
+            if os.path.getsize(self.file.name) > 0:
+                break
+            time.sleep(0.01)
         return self
+
+    def begin(self):
+        self.t_begin = time.time()
+
+    def end(self):
+        self.t_end = time.time()
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -81,11 +99,24 @@ class ClockSampler:
         with open(self.file.name) as f:
             for line in f:
                 parts = [p.strip() for p in line.split(",")]
-                if len(parts) >= 9:
+                if len(parts) >= 10:
                     rows.append(parts)
         os.unlink(self.file.name)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+
+        def stamp(x):
+            try:
+                return datetime.datetime.strptime(x, "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                return None
+
+        inside = [r for r in rows if self.t_begin is not None and self.t_end is not None and
+                  stamp(r[0]) is not None and self.t_begin <= stamp(r[0]) <= self.t_end + 0.02]
+        in_region = len(inside)
+        if inside:
+            rows = inside
+        rows = [r[1:] for r in rows]
 
         def num(x):
             try:
@@ -98,7 +129,7 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "samples_in_timed_region": in_region}
 
 
 # ------------------------------------------------------------------ bytes model
@@ -358,6 +389,7 @@ def run_ours(args, rank, world, local_rank):
         e1 = torch.cuda.Event(enable_timing=True)
         launches = 0
         with ClockSampler(local_rank) as clk:
+            clk.begin()
             e0.record(stream)
             for _ in range(K):
                 res = ctx.expmv_device(v_d.data_ptr(), out.data_ptr(), P.t, m, precision=precision,
@@ -365,6 +397,7 @@ def run_ours(args, rank, world, local_rank):
                 launches += launches_per_solve(ctx, precision, res, m, window)
             e1.record(stream)
             torch.cuda.synchronize()
+            clk.end()
         ms = e0.elapsed_time(e1)
         if world > 1:
             t = torch.tensor([ms], device="cuda")
@@ -455,7 +488,8 @@ def run_ours(args, rank, world, local_rank):
                        "form": f"{form} + {ctrl_form} controller" + (f" + window {win_form}" if win_form else ""),
                        "spmv_form": ctx.spmv_form(form),
                        "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (CSR 251 MB, basis >= 520 MB); no flush"},
+                       "l2": ("inputs larger than L2 (basis >= 520 MB; CSR 251 MB, of which the row-pattern "
+                              "SpMV reads 4.2 MB of row ids); no flush")},
             "fp64_solves_per_s": fp64_sps, "chosen_rel_err_vs_fp64": rel_err,
             "solve": {"attempts": res_c["attempts"], "cycles": res_c["cycles"],
                       "restarts_done": res_c["restarts_done"], "converged": res_c["converged"],
@@ -536,11 +570,13 @@ def run_batch(args):
         b.run()
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
+        clk.begin()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             b.run()
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
+        clk.end()
     clocks = clk.summary()
     value = nsolves * args.steps / secs
     cycles = info["cycles"]
