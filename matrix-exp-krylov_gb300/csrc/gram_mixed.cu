@@ -456,8 +456,9 @@ __global__ void __launch_bounds__(GT, 4) gram_update2_kernel(GramArgs g) {
         r.w = fmaf(x.w, wsc, -s.w) * psc;
         return r;
     };
-    // step j+1's b: u_j . u_{j+1} and |u_{j+1}|^2 (FP32 per thread)
-    float bu = 0.f, bb = 0.f;
+    // step j+1's b: u_j . u_{j+1} and |u_{j+1}|^2; with g.sym its a_j = w_j . u_{j+1}
+    // (FP32 per thread)
+    float bu = 0.f, bb = 0.f, ba = 0.f;
     int i = blockIdx.x * GT + threadIdx.x;
     for (; i + stride < n4; i += 2 * stride) {
         const float4 x0 = __ldg(w4 + i), x1 = __ldg(w4 + i + stride);
@@ -468,6 +469,7 @@ __global__ void __launch_bounds__(GT, 4) gram_update2_kernel(GramArgs g) {
         out[i + stride] = r1;
         bu += dot4(u0, r0) + dot4(u1, r1);
         bb += dot4(r0, r0) + dot4(r1, r1);
+        ba += dot4(x0, r0) + dot4(x1, r1);
     }
     if (i < n4) {
         const float4 x0 = __ldg(w4 + i), u0 = __ldg(u4 + i);
@@ -476,16 +478,19 @@ __global__ void __launch_bounds__(GT, 4) gram_update2_kernel(GramArgs g) {
         out[i] = r0;
         bu += dot4(u0, r0);
         bb += dot4(r0, r0);
+        ba += dot4(x0, r0);
     }
     pdl_trigger();
     if (g.write_b) {
-        __shared__ double s_red[GW][2];
-        const float ru = warp_sum(bu), rb = warp_sum(bb);
+        __shared__ double s_red[GW][3];
+        const float ru = warp_sum(bu), rb = warp_sum(bb), ra = warp_sum(ba);
         if ((threadIdx.x & 31) == 0) {
             s_red[threadIdx.x >> 5][0] = ru;
             s_red[threadIdx.x >> 5][1] = rb;
+            s_red[threadIdx.x >> 5][2] = ra;
         }
-        step_write_partials(s_red, g.part, blockIdx.x, [&](int q) { return GRAM_BOFF + j + q; });
+        const bool sym = g.sym != 0;
+        step_write_partials(s_red, g.part, blockIdx.x, [&](int q) { return q < 2 ? GRAM_BOFF + j + q : (sym ? j : -1); });
     }
 }
 

@@ -94,9 +94,11 @@ __device__ __forceinline__ void step2_finish(const GramArgs& g, int nrb_a, int n
     for (int r = t; r < lo; r += blockDim.x) g.H[r + static_cast<size_t>(j) * ldh] = 0.0;  // outside the window
     const double s0 = kw == 2 ? gs->s[lo] : 0.0;
     const double ip_j = gs->ip[j];
+    // b (and, for a symmetric A, a_{j-1}) come from the previous update
+    const bool a0_from_update = g.sym && kw == 2;
     step_sum_partials<PR>(
         g.part, 2 * kw + 1, [&](int v) { return step2_slot(v, kw, lo); },
-        [&](int v) { return (v >= kw && v < 2 * kw) ? nrb_b : nrb_a; }, s_tot);
+        [&](int v) { return ((v >= kw && v < 2 * kw) || (v == 0 && a0_from_update)) ? nrb_b : nrb_a; }, s_tot);
     __syncthreads();
     if (t != 0) return;
     const double bj = s_tot[2 * kw - 1];

@@ -392,6 +392,12 @@ struct GramArgs {
     // b_blocks row blocks (the count step j+1's finish reads).
     int write_b = 0;
     int b_blocks = 0;
+    // Symmetric A (a window of 2): u_{j-1}.(A u_j) = (A u_{j-1}).u_j, so the
+    // update of step j-1, which holds w_{j-1} = A u_{j-1} and u_j, also writes
+    // step j's a_{j-1} partials (into a slot j-1 over b_blocks row blocks) and
+    // the SpMV of step j reads no u_{j-1}. sym on the update: write them; on
+    // the SpMV with dots: read them.
+    int sym = 0;
     DevState* st;
 };
 int device_sm_count();

@@ -325,6 +325,8 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
         const bool fusable = m > 0 && ctx->spmv_form32 != MEXK_SPMV_DIRECT;
         const bool fuse = fusable && fused_step(j, window);
         g.b_blocks = fuse ? gram_update2_blocks(ctx->n) : 0;
+        // window 2 (symmetric A) with the pattern SpMV: a_{j-1} from the update of step j-1
+        g.sym = (window == 2 && ctx->spmv_form32 == MEXK_SPMV_PATTERN) ? 1 : 0;
         if ((rc = context_spmv(ctx, j, true, &ctx->d_state->breakdown, s, fuse ? &g : nullptr))) return rc;
         if (!fuse && (rc = launch_gram_dot(g, s))) return rc;
         g.write_b = (fusable && j + 1 < m && fused_step(j + 1, window)) ? 1 : 0;
@@ -1063,6 +1065,7 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
             case MEXK_KERNEL_GRAM_UPDATE: {
                 GramArgs gu = ga;  // as in a solve: b partials for a fused next step
                 gu.write_b = (j + 1 < ctx->m_alloc && fused_step(j + 1, ctx->last_window)) ? 1 : 0;
+                gu.sym = (ctx->last_window == 2 && ctx->spmv_form32 == MEXK_SPMV_PATTERN) ? 1 : 0;
                 r = fp32 ? launch_gram_update(gu, s) : MEXK_ERR_UNSUPPORTED;
                 break;
             }
@@ -1073,6 +1076,7 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
                 }
                 GramArgs gd = ga;
                 gd.b_blocks = gram_update2_blocks(ctx->n);
+                gd.sym = (ctx->last_window == 2 && ctx->spmv_form32 == MEXK_SPMV_PATTERN) ? 1 : 0;
                 r = context_spmv(ctx, j, true, nullptr, s, &gd);
                 break;
             }

@@ -760,7 +760,8 @@ int launch_spmv(int n, int nblocks, const int4* tiles, const uint16_t* col16, bo
     if (direct && !dots) return launch_spmv_direct<TA, TX>(nblocks, tiles, row_ptr, col_idx, values, x, y, skip_flag, s);
     if constexpr (sizeof(TX) == 4) {
         if (dots) {
-            if (dots->j < 1 || dots->lo != dots->j - 1 || dots->b_blocks < 1) return MEXK_ERR_INVALID;
+            // the staged form takes u_{j-1}.w itself (sym is the pattern form's)
+            if (dots->j < 1 || dots->lo != dots->j - 1 || dots->b_blocks < 1 || dots->sym) return MEXK_ERR_INVALID;
             return all_narrow ? launch_spmv_as<TA, TX, true, true>(nblocks, tiles, col16, row_ptr, col_idx, values,
                                                                     x, y, skip_flag, status, *dots, s)
                               : launch_spmv_as<TA, TX, false, true>(nblocks, tiles, col16, row_ptr, col_idx, values,

@@ -167,9 +167,10 @@ constexpr unsigned PAT_FULL = 0xffffffffu;
 // without DOTS, whose registers allow it) requested together, so a boundary
 // costs a round trip per row, not one per entry. Either way a row's products are formed and added in
 // entry order from zero. With DOTS (FP32 mixed form, a step j >= 1 over
-// columns j-1 and j) each row sum also accumulates u_{j-1} w, u_j w, |w|^2
+// columns j-1 and j; DOTS 2: symmetric A, u_{j-1} w taken from the previous
+// update as w_{j-1} u_j) each row sum also accumulates u_{j-1} w, u_j w, |w|^2
 // and the last block finishes the step, as the staged CSR form does.
-template <typename TX, bool DOTS, int LMAX>
+template <typename TX, int DOTS, int LMAX>
 __global__ void __launch_bounds__(PAT_THREADS, 4)
     spmv_pattern_kernel(int n, int major, int major_len, const uint8_t* __restrict__ pid,
                         const RowPatterns* __restrict__ T, const TX* __restrict__ x, TX* __restrict__ y,
@@ -211,7 +212,8 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
     pdl_trigger();
     float da0 = 0.f, da1 = 0.f, dw = 0.f;
     // DOTS: columns j-1 and j of the basis
-    const float* __restrict__ vlo = DOTS ? ga.V + static_cast<size_t>(ga.lo) * static_cast<size_t>(ga.ldv) : nullptr;
+    const float* __restrict__ vlo =
+        DOTS == 1 ? ga.V + static_cast<size_t>(ga.lo) * static_cast<size_t>(ga.ldv) : nullptr;
     const float* __restrict__ vj = DOTS ? ga.V + static_cast<size_t>(ga.j) * static_cast<size_t>(ga.ldv) : nullptr;
     for (int k = 0; c < nchunk; c += gridDim.x, ++k) {
         const int r0 = c * PAT_CHUNK + wrow(k);
@@ -220,7 +222,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
         for (int i = 0; i < PAT_RPT; ++i) cur[i] = ids[i];
         load_ids(c + gridDim.x, k + 1);
         float up[PAT_RPT], uj[PAT_RPT];
-        if constexpr (DOTS) {
+        if constexpr (DOTS == 1) {
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i) up[i] = r0 + i * 32 < n ? __ldg(vlo + (r0 + i * 32)) : 0.f;
         }
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
                     y[r] = s[i];
                     if constexpr (DOTS) {
                         const float sf = static_cast<float>(s[i]);
-                        da0 = fmaf(up[i], sf, da0);
+                        if constexpr (DOTS == 1) da0 = fmaf(up[i], sf, da0);
                         da1 = fmaf(uj[i], sf, da1);
                         dw = fmaf(sf, sf, dw);
                     }
@@ -314,14 +316,17 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
             s_red[tid >> 5][2] = r2;
         }
         const int jj = ga.j;
-        step_write_partials(s_red, ga.part, blockIdx.x, [&](int q) { return q < 2 ? jj - 1 + q : GRAM_NWOFF; });
+        // DOTS 2 (symmetric A): a_{j-1} comes from the previous update, not from this sweep
+        step_write_partials(s_red, ga.part, blockIdx.x, [&](int q) {
+            return q == 0 ? (DOTS == 1 ? jj - 1 : -1) : q == 1 ? jj : GRAM_NWOFF;
+        });
         __shared__ int s_flag;
         if (!grid_last_block(ga.counter, &s_flag)) return;
         step2_finish<20>(ga, gridDim.x, ga.b_blocks);  // <= 640 blocks: one round of partial loads
     }
 }
 
-template <typename TX, bool DOTS, int LMAX>
+template <typename TX, int DOTS, int LMAX>
 int launch_pattern_as(int n, int major, int major_len, const uint8_t* pid, const RowPatterns* T, const TX* x,
                       TX* y, const int* skip, const GramArgs& ga, cudaStream_t s) {
     auto kern = spmv_pattern_kernel<TX, DOTS, LMAX>;
@@ -350,7 +355,7 @@ int launch_pattern_as(int n, int major, int major_len, const uint8_t* pid, const
 
 // The longest pattern picks the kernel: the stencils' 3, 5, 7 and 9 entries
 // (1-D, 2-D, 3-D, 2-D nine-point) unroll exactly.
-template <typename TX, bool DOTS>
+template <typename TX, int DOTS>
 int launch_pattern_len(int n, int major, int major_len, int max_len, const uint8_t* pid, const RowPatterns* T,
                        const TX* x, TX* y, const int* skip, const GramArgs& ga, cudaStream_t s) {
     if (max_len <= 3) return launch_pattern_as<TX, DOTS, 3>(n, major, major_len, pid, T, x, y, skip, ga, s);
@@ -408,12 +413,14 @@ int launch_spmv_pattern(int n, int major, int major_len, int max_len, const uint
     if constexpr (sizeof(TX) == 4) {
         if (dots) {
             if (dots->j < 1 || dots->lo != dots->j - 1 || dots->b_blocks < 1) return MEXK_ERR_INVALID;
-            return launch_pattern_len<TX, true>(n, major, major_len, max_len, pid, T, x, y, skip_flag, *dots, s);
+            return dots->sym
+                       ? launch_pattern_len<TX, 2>(n, major, major_len, max_len, pid, T, x, y, skip_flag, *dots, s)
+                       : launch_pattern_len<TX, 1>(n, major, major_len, max_len, pid, T, x, y, skip_flag, *dots, s);
         }
     } else if (dots) {
         return MEXK_ERR_UNSUPPORTED;
     }
-    return launch_pattern_len<TX, false>(n, major, major_len, max_len, pid, T, x, y, skip_flag, none, s);
+    return launch_pattern_len<TX, 0>(n, major, major_len, max_len, pid, T, x, y, skip_flag, none, s);
 }
 
 template int launch_spmv_pattern<double>(int, int, int, int, const uint8_t*, const RowPatterns*, const double*,
