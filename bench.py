@@ -145,7 +145,7 @@ SPMV_F32_TRAFFIC_HEAT1536 = (89.869312e6 + 3.002624e6, 11790336)
 SPMV_DOTS_F32_TRAFFIC_HEAT1536 = (99.39968e6 + 3.26912e6, 11790336)
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the row-pattern SpMV
 # with dots on the 1536^2 heat grid (2,359,296 rows): (bytes, rows).
-PAT_DOTS_F32_TRAFFIC_HEAT1536 = (21.274624e6, 2359296)
+PAT_DOTS_F32_TRAFFIC_HEAT1536 = (11.843968e6, 2359296)
 
 def kernel_bytes(kind, n, nnz, k, fp32, window=0, form="staged"):
     """Algorithmic HBM bytes of one launch (per-kernel minimum traffic); with a
@@ -157,8 +157,8 @@ def kernel_bytes(kind, n, nnz, k, fp32, window=0, form="staged"):
         k = min(k, window)
     if form == "pattern" and kind == "spmv":
         return n + 2 * n * s  # row ids, x once, y
-    if form == "pattern" and kind == "spmv_dots":
-        return n + 3 * n * s
+    if form == "pattern" and kind == "spmv_dots":  # a window of 2 takes u_{j-1}.w from the update: no u_{j-1}
+        return n + (2 if window == 2 else 3) * n * s
     if kind == "spmv":
         return nnz * (s + 4) + 4 * (n + 1) + 2 * n * s  # values+cols, row_ptr, x once, y
     if kind == "spmv_dots":  # the SpMV, then u_{j-1} read for the dots (u_j is x)
