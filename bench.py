@@ -202,6 +202,32 @@ def step_kinds(precision, j, window=0, dots_in_spmv=True):
 CYCLE_KINDS = {"fp64": ["controller", "lift"], "mixed": ["controller", "lift", "gram_norm"]}
 
 
+def size_matched_copy(nbytes, stream, iters=20):
+    """A plain device copy moving the same bytes as one launch of a kernel
+    (half read, half written; torch's copy kernel), timed back to back with
+    CUDA events: what a launch of that size reaches on this GPU, for reading
+    the roofline fraction of a kernel whose launches are short."""
+    import torch
+
+    half = max(1, int(nbytes) // 8)  # floats per buffer
+    with torch.cuda.stream(stream):  # the copies and the events on one stream
+        a = torch.empty(half, dtype=torch.float32, device="cuda")
+        b = torch.empty_like(a)
+        a.fill_(1.0)
+        for _ in range(3):
+            b.copy_(a)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(iters):
+            b.copy_(a)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    us = 1e3 * e0.elapsed_time(e1) / iters
+    moved = 8 * half
+    return {"bytes": moved, "us": round(us, 2), "gbs": round(moved / (us / 1e6) / 1e9, 1)}
+
+
 def profile_cycle(ctx, m, n, nnz, precision, iters=2, window=0):
     """CUDA-event timing of every kernel kind of one Krylov cycle (the sweeps
     as the context's last solve ran them: with its window, if any)."""
@@ -458,7 +484,8 @@ def run_ours(args, rank, world, local_rank):
                 "1536^2 heat grid (11,790,336 nonzeros), scaled by nonzeros")
     roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
             "traffic": traffic, "traffic_source": tsrc,
-            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"}
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "size_matched_copy": size_matched_copy(per[dom]["bytes"] / per[dom]["launches"], stream)}
     sp = per["spmv"]
     spmv_gbs = sp["bytes"] / (sp["ms"] / 1e3) / 1e9
     if form != "fp64":
