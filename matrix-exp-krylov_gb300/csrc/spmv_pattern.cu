@@ -30,6 +30,11 @@ namespace {
 
 constexpr int PAT_THREADS = 256;
 
+// Probes of the hash table per key: a detection that succeeds holds at most
+// PAT_MAX keys in PAT_SLOTS slots (a quarter full), so a longer probe
+// sequence means too many patterns.
+constexpr int PAT_PROBES = 64;
+
 // Flags of the detection passes.
 constexpr int PAT_LONG_ROW = 1;
 constexpr int PAT_TOO_MANY = 2;
@@ -62,6 +67,8 @@ __global__ void pattern_insert_kernel(int n, const int* __restrict__ row_ptr, co
     // whole warps run every iteration (the match below takes the full mask)
     const int nw = (n + 31) & ~31;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nw; r += stride) {
+        // a failed detection stops at once (the warp decides together)
+        if (__any_sync(0xffffffffu, *reinterpret_cast<volatile int*>(flags) != 0)) return;
         const uint64_t key = r < n ? pat_row_key(r, row_ptr, col_idx, values) : 0;
         if (r < n && key == 0) atomicOr(flags, PAT_LONG_ROW);
         const unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -69,7 +76,7 @@ __global__ void pattern_insert_kernel(int n, const int* __restrict__ row_ptr, co
         // one lane per distinct key of the warp inserts it
         unsigned slot = static_cast<unsigned>(key) & (PAT_SLOTS - 1);
         bool done = false;
-        for (int probe = 0; probe < PAT_SLOTS && !done; ++probe, slot = (slot + 1) & (PAT_SLOTS - 1)) {
+        for (int probe = 0; probe < PAT_PROBES && !done; ++probe, slot = (slot + 1) & (PAT_SLOTS - 1)) {
             unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&T->keys[slot]);
             if (k == 0) k = atomicCAS(&T->keys[slot], 0ull, static_cast<unsigned long long>(key));
             if (k == 0) {  // this lane inserted the key: take an id, write the pattern
@@ -102,11 +109,12 @@ __global__ void pattern_assign_kernel(int n, const int* __restrict__ row_ptr, co
     const int stride = gridDim.x * blockDim.x;
     const int nw = (n + 31) & ~31;  // whole warps run every iteration (the row count match)
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nw; r += stride) {
+        if (__any_sync(0xffffffffu, *reinterpret_cast<volatile int*>(flags) != 0)) return;  // failed: stop
         const uint64_t key = r < n ? pat_row_key(r, row_ptr, col_idx, values) : 0;
         int id = -1;
         if (key != 0) {  // rows without a key are flagged by the insert pass
             unsigned slot = static_cast<unsigned>(key) & (PAT_SLOTS - 1);
-            for (int probe = 0; probe < PAT_SLOTS; ++probe, slot = (slot + 1) & (PAT_SLOTS - 1)) {
+            for (int probe = 0; probe < PAT_PROBES; ++probe, slot = (slot + 1) & (PAT_SLOTS - 1)) {
                 const unsigned long long k = T->keys[slot];
                 if (k == key) {
                     id = T->ids[slot];
@@ -381,9 +389,12 @@ int build_row_patterns(int n, const int* d_row_ptr, const int* d_col, const doub
     const int grid = static_cast<int>(want < 8192 ? want : 8192);
     pattern_insert_kernel<<<grid, 256, 0, s>>>(n, d_row_ptr, d_col, d_val, d_T, d_flags);
     MEXK_CK_LAUNCH("pattern_insert_kernel");
+    int flags = -1;
+    MEXK_CK(cudaMemcpyAsync(&flags, d_flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MEXK_CK(cudaStreamSynchronize(s));
+    if (flags != 0) return MEXK_OK;  // a row longer than PAT_LEN or too many patterns
     pattern_assign_kernel<<<grid, 256, 0, s>>>(n, d_row_ptr, d_col, d_val, d_T, d_pid, d_flags);
     MEXK_CK_LAUNCH("pattern_assign_kernel");
-    int flags = -1;
     MEXK_CK(cudaMemcpyAsync(&flags, d_flags, sizeof(int), cudaMemcpyDeviceToHost, s));
     MEXK_CK(cudaStreamSynchronize(s));
     *ok = flags == 0;
