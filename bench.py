@@ -835,11 +835,12 @@ def run_batch_once(args):
         print(json.dumps(b.info()), flush=True)
 
 
-def run_solve_once(local_rank, grid=2048):
+def run_solve_once(local_rank, grid=2048, spmv_form=None):
     """One solve in the headline form (mixed precision, candidate-step
     controller, window 2: the heat matrix is symmetric) and one plain FP64
     solve of the heat equation on a grid x grid mesh, untimed: the command
-    ncu captures."""
+    ncu captures. spmv_form: run that SpMV form instead of the context's
+    choice (the row-pattern form on this matrix)."""
     import torch
 
     from mexk import synthetic as S
@@ -848,6 +849,9 @@ def run_solve_once(local_rank, grid=2048):
     torch.cuda.set_device(local_rank)
     P = make_problem() if grid == 2048 else S.config1(N=grid)
     with Context(P.A, m_alloc=P.m, device=local_rank) as ctx:
+        if spmv_form is not None:
+            for prec in ("mixed", "fp64"):
+                ctx.set_spmv_form(spmv_form, prec)
         for prec, ctrl, window in (("mixed", "search", 2), ("fp64", "reference", 0)):
             _, res = ctx.expmv(P.v, P.t, P.m, precision=prec, controller=ctrl, window=window)
             print(prec, ctrl, window, res, flush=True)
@@ -921,13 +925,15 @@ def main():
     ap.add_argument("--problems", type=int, default=256, help="batch workload: number of problems")
     ap.add_argument("--sample", type=int, default=8, help="batch workload: problems in the serial FP64 sample")
     ap.add_argument("--grid", type=int, default=2048, help="--solve-once: heat-equation grid size")
+    ap.add_argument("--spmv-form", choices=["staged", "direct", "pattern"], default=None,
+                    help="--solve-once: SpMV form to run instead of the context's choice")
     ap.add_argument("--first", type=int, default=0, help="batch --solve-once: index of the first problem")
     args = ap.parse_args()
     if args.solve_once and args.workload == "batch":
         run_batch_once(args)
         return
     if args.solve_once:
-        run_solve_once(int(os.environ.get("LOCAL_RANK", "0")), args.grid)
+        run_solve_once(int(os.environ.get("LOCAL_RANK", "0")), args.grid, args.spmv_form)
         return
     if args.workload == "batch" and args.impl == "ours":
         run_batch(args)
