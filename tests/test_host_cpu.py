@@ -41,6 +41,10 @@ def test_invalid_arguments_without_gpu():
     assert L.mexk_expm_f64(0, None, 0, None, 0, None) == _lib_err("INVALID")
     assert L.mexk_gram_schmidt_f64_noalloc(10, 0, 1, 10, 1, 1, 1, 1, 1, None) == _lib_err("INVALID")
     assert L.mexk_expmv(None, None, None, None, None) == _lib_err("INVALID")
+    form = C.c_int(-1)
+    assert L.mexk_context_get_spmv_form(None, 0, C.byref(form)) == _lib_err("INVALID")
+    assert L.mexk_context_set_spmv_form(None, 0, 2) == _lib_err("INVALID")
+    assert L.mexk_profile_kernel(None, 0, 0, 0, 1, None) == _lib_err("INVALID")
     assert L.mexk_error_string(3) == b"allocation failed"
 
 
