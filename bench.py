@@ -290,6 +290,34 @@ def cpu_cycle_seconds(A, v, t, m, cycles=1):
     return (time.perf_counter() - t0) / cycles
 
 
+def whole_solve_check(N=1024):
+    """The cycle x attempts model of the CPU baseline checked against a whole
+    solve: the oracle port (bit-identical to main_cpu.cpp) solves the heat
+    workload on an N^2 grid to convergence on one core, and the same
+    problem's first cycle is timed alone. Returns the wall times, the
+    attempts and measured / (cycle x attempts)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from mexk import synthetic as S
+
+    if not os.path.exists(O.LIB_PATH):
+        O.build(with_reference=False)
+    P = S.config1(N=N)
+    t0 = time.perf_counter()
+    _, st, steps = O.expmv(P.A, P.v, P.t, P.m)
+    whole = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.expmv(P.A, P.v, P.t, P.m, max_cycles=1)
+    cycle = time.perf_counter() - t0
+    out = {"grid": f"{N}^2", "n": P.A.n, "whole_solve_s": round(whole, 3), "cycle_s": round(cycle, 3),
+           "attempts": len(steps), "converged": st["converged"],
+           "measured_over_model": round(whole / (cycle * len(steps)), 3)}
+    if os.path.exists(HEAT_GOLDEN):
+        # the reference's own compiled main_cpu.cpp, full 2048^2 solve, one core of the x86 build machine
+        out["reference_binary_heat2048_whole_solve_s"] = round(float(np.load(HEAT_GOLDEN)["wall_seconds"]), 1)
+    return out
+
+
 def reference_attempts():
     """Basis builds per solve of the reference: one per [STEP] attempt (it
     rebuilds the basis on every reject), from its own full-size run."""
@@ -333,16 +361,20 @@ def run_reference(args, rank, world):
             walls.append(max(pool.map(_reference_worker, range(cores))))
     t_cycle = statistics.median(walls)
     value = cores / (t_cycle * attempts)
+    check = whole_solve_check()
     sample = (f"{len(walls)} x {cores} concurrent single-threaded solves (one per host core), each timed for "
               f"one Arnoldi cycle (m=30, n=4194304) of the reference's CPU algorithm (oracle port, bit-identical "
               f"to main_cpu.cpp); slowest cycle {t_cycle:.2f}s (median over rounds); a solve = {attempts} basis "
-              f"builds ({src})")
+              f"builds ({src}). Model check on one core: a whole {check['grid']} heat solve took "
+              f"{check['whole_solve_s']}s against {check['cycle_s']}s x {check['attempts']} attempts "
+              f"(measured/model {check['measured_over_model']})")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_cycle * attempts * 1e3 / cores,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "form": f"reference CPU (FP64), {cores} concurrent solves"},
-            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample,
+                             "whole_solve_check": check},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -509,9 +541,14 @@ def run_ours(args, rank, world, local_rank):
         if attempts is None:
             attempts, src = len(steps64), "this run's FP64 decision sequence"
         t_cycle = cpu_cycle_seconds(P.A, P.v, P.t, m, 1)
+        check = whole_solve_check()
         cpu = {"value": 1.0 / (t_cycle * attempts), "unit": "solves/s", "cores": 1, "kind": "port",
                "sample": (f"one Arnoldi cycle (m=30, n=4194304) of the oracle port of main_cpu.cpp on 1 core "
-                          f"took {t_cycle:.2f}s; a reference solve = {attempts} basis builds ({src})")}
+                          f"took {t_cycle:.2f}s; a reference solve = {attempts} basis builds ({src}); "
+                          f"model check: a whole {check['grid']} heat solve took {check['whole_solve_s']}s against "
+                          f"{check['cycle_s']}s x {check['attempts']} attempts (measured/model "
+                          f"{check['measured_over_model']})"),
+               "whole_solve_check": check}
 
     if rank == 0:
         line = {

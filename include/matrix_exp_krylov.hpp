@@ -145,6 +145,9 @@ struct ArnoldiRunner {
     int ortho_window = 0;
     bool net_loaded = false;
     bool verbose = true;
+    // Also print the reference's per-step "H_m column j stored" lines
+    // (store_H_column, main.cu:1944-1952) before each attempt's [STEP] line.
+    bool log_h_columns = false;
     mexk_result_t last_result{};
     std::vector<mexk_step_t> last_steps;
 

@@ -39,19 +39,45 @@ extern "C" {
 #define MEXK_CTRL_REFERENCE 0 /* the reference's accept/reject heuristic (main.cu:1476-1516) */
 #define MEXK_CTRL_SEARCH 1    /* per basis, the largest of 32 candidate steps whose
                                  residual estimate passes; reference heuristic if none.
-                                 With MEXK_PREC_MIXED the per-step tolerance is
-                                 max(tol, 2^-24 |v|): the FP32 basis precision */
+                                 With MEXK_PREC_MIXED the FP32 basis cannot resolve a
+                                 truncation error below its rounding of the current
+                                 iterate y, so a step may also pass with
+                                 err <= min(2^-24 |y|, 5e-7 |y| - E), E the sum of
+                                 the errors already accepted: the accepted errors of
+                                 a solve never add up to more than 5e-7 of the
+                                 iterate's norm (beyond what tol itself allows) */
 #define MEXK_CTRL_LEARNED 2   /* SEARCH centred on an MLP's step prediction, with the
                                  MLP also choosing the next cycle's Krylov dimension */
 
-/* Largest Krylov dimension m this build supports. */
-#define MEXK_M_MAX 64
+/* Largest Krylov dimension m: MEXK_M_MAX for the plain method (FP64 and the
+ * reference controller, the reference's ArnoldiParams default m = 100 among
+ * them); MEXK_M_MAX_MIXED for mixed precision and the candidate-step
+ * controllers, whose Gram matrix and candidate exponentials are held on chip. */
+#define MEXK_M_MAX 128
+#define MEXK_M_MAX_MIXED 64
+
+/* Time-stepping parameters: the reference's TimeSteppingParams
+ * (main.cu:1237-1250), read by compute_expmv on every solve (main.cu:1426,
+ * 1476-1516). The step is accepted when err <= tol_step (or on breakdown);
+ * an accepted step with err < 0.1 tol_step grows dt to
+ * min(dt * grow * safety, dt_max); a rejected one either raises the Krylov
+ * dimension by m_step (adapt_m, up to m_max) or shrinks dt to
+ * max(dt * shrink * safety, dt_min); max_rejects rejects in a row abort the
+ * solve and at most max_steps steps are accepted. */
+typedef struct {
+    double dt_init, dt_min, dt_max, tol_step;
+    int max_steps, max_rejects;
+    double safety, grow, shrink;
+    int adapt_m, m_max, m_step;
+} mexk_stepping_t;
 
 /* Solver parameters. Mirrors ArnoldiParams (main.cu:1221-1230) plus the
- * precision choice; the controller constants follow TimeSteppingParams
- * defaults (main.cu:1292-1305). */
+ * precision choice. stepping = NULL derives the time-stepping parameters
+ * from m, t, tol and max_restarts as the ArnoldiRunner constructor does
+ * (main.cu:1292-1305). */
 typedef struct {
-    int m;               /* Krylov dimension, 1 <= m <= MEXK_M_MAX, m < n */
+    int m;               /* Krylov dimension, 1 <= m <= MEXK_M_MAX (MEXK_M_MAX_MIXED for
+                            mixed precision or a candidate-step controller), m < n */
     double t;            /* total time */
     double tol;          /* per-step tolerance on the residual estimate */
     int max_restarts;    /* > 0: dt_init = t/max_restarts and at most that many
@@ -64,6 +90,11 @@ typedef struct {
                             only): against the last W basis vectors, the short
                             recurrence of Lanczos; the context verifies symmetry
                             (MEXK_ERR_INVALID otherwise). No reference counterpart. */
+    const mexk_stepping_t* stepping; /* NULL: the defaults above. Otherwise used as
+                            given with the reference controller; the candidate-step
+                            controllers take dt_min, dt_max, tol_step, max_steps and
+                            max_rejects from it and choose steps and m themselves.
+                            adapt_m needs m_max <= the context's m_alloc_max. */
 } mexk_params_t;
 
 /* Outcome of one solve. converged / restarts_done / last_residual are the
@@ -80,10 +111,13 @@ typedef struct {
 } mexk_result_t;
 
 /* One accept/reject attempt: the fields of the reference's [STEP] line
- * (main.cu:1471-1474). */
+ * (main.cu:1471-1474), and the Krylov dimension the attempt's basis was
+ * built for (m_current of main.cu:1435; m_used is smaller after a breakdown),
+ * which sizes the reference's "H_m column" lines (main.cu:1951). */
 typedef struct {
     double t_done, dt, err;
     int m_used, accepts, rejects;
+    int m_basis;
 } mexk_step_t;
 
 typedef struct mexk_context_s* mexk_context_t;
@@ -241,18 +275,21 @@ int mexk_controller_predict(const float* weights, const double* H, int ldh, int 
  * for callers that cannot call cudaMalloc (a host that owns all device memory
  * through its own pool, an FFI runtime that only passes buffers, a request
  * path that must not allocate). All pointers are device memory of the current
- * device: on return (in stream order) h[0..k-1] = V^T w summed over the
- * passes, *beta = |w - V h| (0 on breakdown: norm < 1e-14, NaN or Inf),
- * q[0..n-1] = (w - V h) / beta (left untouched on breakdown), and w holds the
- * orthogonalised, unnormalised vector. Limits: 1 <= k <= 64; the kernels'
- * reduction scratch is a fixed 592 KB array in the library's device memory,
- * sized for grids of up to 1024 thread blocks; larger sizes are refused with
- * MEXK_ERR_INVALID. That array is shared by all calls on a device and keeps
- * the last call's contents (each call clears what must start at zero), so
- * calls that overlap on the GPU race and must be serialised. The first call
- * on a device looks up the array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture. No counterpart in the
- * reference: it orthogonalises only inside orthogonalize_mgs with cuBLAS. */
+ * device, and `stream` (NULL = the legacy default stream) must belong to that
+ * device (MEXK_ERR_INVALID otherwise): on return (in stream order) h[0..k-1]
+ * = V^T w summed over the passes, *beta = |w - V h| (0 on breakdown: norm <
+ * 1e-14, NaN or Inf), q[0..n-1] = (w - V h) / beta (left untouched on
+ * breakdown), and w holds the orthogonalised, unnormalised vector. Limits:
+ * 1 <= k <= 64 (larger k: MEXK_ERR_INVALID); any n >= 1, the sweeps' grid
+ * being capped at 1024 thread blocks (they stride over the rows). The
+ * kernels' reduction scratch is a fixed 592 KB array in the library's device
+ * memory, shared by all calls on a device; it keeps the last call's contents
+ * (each call clears what must start at zero), so calls that overlap on the
+ * GPU race and must be serialised. Every call looks up the array's device
+ * address on the current device (cudaGetSymbolAddress); the first lookup on a
+ * device loads the library's device code, so make the first call before any
+ * stream capture. No counterpart in the reference: it orthogonalises only
+ * inside orthogonalize_mgs with cuBLAS. */
 int mexk_gram_schmidt_f64_noalloc(int n, int k, const double* V, int ldv, double* w,
                                   int reorthogonalize, double* h, double* beta, double* q,
                                   void* stream);
@@ -266,9 +303,11 @@ int mexk_gram_schmidt_f64_noalloc(int n, int k, const double* V, int ldv, double
  * main.cu:1411-1571) with its own step size. The reference solves one vector
  * per process; the batch has no reference counterpart beyond that method.
  * Problems are laid out in one row space and advanced in waves whose bases
- * fit the basis budget; one cycle of a wave is one CUDA graph launch. The
- * tolerance of a right-hand side is raised to the FP32 resolution of its
- * start vector when smaller: max(tol, 2^-24 |v|). */
+ * fit the basis budget; one cycle of a wave is one CUDA graph launch. As for
+ * MEXK_CTRL_SEARCH in mixed precision, a step of a right-hand side also
+ * passes with err <= min(2^-24 |y|, 5e-7 |y| - E) (|y| its current iterate,
+ * E its accepted errors so far): the FP32 bases do not resolve errors below
+ * their rounding of y. */
 #define MEXK_BATCH_RHS 16
 #define MEXK_BATCH_M_MAX 32
 typedef struct mexk_batch_s* mexk_batch_t;
@@ -367,6 +406,16 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
 #define MEXK_SPMV_PATTERN 2
 int mexk_context_get_spmv_form(mexk_context_t ctx, int precision, int* form);
 int mexk_context_set_spmv_form(mexk_context_t ctx, int precision, int form);
+
+/* ---- testing hooks ------------------------------------------------------ */
+/* enable != 0: from now on, thread block 0 of the staged CSR SpMV also waits
+ * (1 ms limit) on a barrier that nothing arrives at, so its bounded wait runs
+ * out: it drains its bulk copies in flight, sets the timeout status bit, and
+ * the solve returns MEXK_ERR_DEVICE while the context stays usable. enable = 0
+ * restores normal operation. For failure-path tests only: it changes no
+ * result of a solve that does not use the staged form. No reference
+ * counterpart (the reference has no bounded device waits). */
+int mexk_test_force_wait_timeout(int device, int enable);
 
 #ifdef __cplusplus
 }

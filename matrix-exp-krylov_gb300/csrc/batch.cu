@@ -307,9 +307,14 @@ void init_state(DevState* st, const mexk_batch_params_t& p, double t, bool used)
     st->dt_min = std::max(1e-12, t * 1e-6);
     const double dt_init = (p.max_restarts > 0) ? t / p.max_restarts : t;
     st->tol = p.tol;
+    st->tol_base = p.tol;
     st->max_steps = (p.max_restarts > 0) ? p.max_restarts : 1000;
     st->max_rejects = 20;
+    st->safety = 0.8;
+    st->grow = 1.5;
+    st->shrink = 0.5;
     st->m = p.m;
+    st->m_base = p.m;
     double dt = std::min(std::max(dt_init, st->dt_min), st->dt_max);
     st->done = !(0.0 < st->total_t && 0 < st->max_steps);
     dt = std::min(dt, st->total_t);
@@ -318,6 +323,7 @@ void init_state(DevState* st, const mexk_batch_params_t& p, double t, bool used)
     st->m_next = p.m;
     st->ctrl = MEXK_CTRL_REFERENCE;
     st->tol_floor_rel = 5.9604644775390625e-08;  // 2^-24
+    st->err_budget_rel = 5e-7;
     if (!used) {
         st->done = 1;
         st->converged = 1;

@@ -514,15 +514,18 @@ __global__ void __launch_bounds__(BT) lift_kernel(Layout L, int kmax, int start)
         DevState* st = L.st + p * BR + threadIdx.x;
         const double nrm = sqrt(tiles_sum(L, p, W_OFF + threadIdx.x));
         st->restart_scale = nrm > 1e-14 ? 1.0 / nrm : 1.0;
+        // FP32 bases do not resolve errors below their rounding of the iterate:
+        // a step also passes below it while the accepted errors stay within
+        // err_budget_rel of the iterate's norm.
         if (start) {
             st->v_norm = nrm;
             st->restart = 1;
-            // FP32 bases do not resolve errors below their rounding of |v|.
-            st->tol = fmax(st->tol, st->tol_floor_rel * nrm);
         } else {
             if (st->restart) st->v_norm = nrm;
             st->lift = 0;
         }
+        if (start || st->restart)
+            st->tol = fmax(st->tol_base, fmin(st->tol_floor_rel * nrm, st->err_budget_rel * nrm - st->err_acc));
     }
 }
 

@@ -111,6 +111,7 @@ __device__ inline void mlp_forward_block(const float* __restrict__ w, const floa
 
 // Network outputs -> (log2 of the step centre times |H_k|_1, next m).
 __device__ __forceinline__ int next_m_from(float o1, int m_cap) {
+    o1 = fminf(fmaxf(o1, 0.0f), 1.0f);  // also maps NaN (a broken network) to M_MIN
     const float mf = static_cast<float>(M_MIN) + o1 * static_cast<float>(M_MAX - M_MIN);
     int mq = static_cast<int>(rintf(mf / M_STEP)) * M_STEP;
     mq = mq < M_MIN ? M_MIN : (mq > M_MAX ? M_MAX : mq);

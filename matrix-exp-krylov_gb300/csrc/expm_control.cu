@@ -192,7 +192,13 @@ __device__ double* expm_block(const ExpmBuf& B, int k, int* status) {
         for (int j = 0; j < k; ++j)
             if (B.red[j] > l1) l1 = B.red[j];
         int sq = 0, deg;
-        if (l1 < 1.495585217958292e-002) deg = 3;
+        // A non-finite norm (Inf or NaN entries) keeps degree 13 without
+        // scaling: frexp's exponent is unspecified there, and the squaring
+        // loop must stay bounded; the result is then non-finite as well.
+        if (!(l1 <= 1.7976931348623157e308)) {
+            deg = 13;
+            *status |= ST_NONFINITE;
+        } else if (l1 < 1.495585217958292e-002) deg = 3;
         else if (l1 < 2.539398330063230e-001) deg = 5;
         else if (l1 < 9.504178996162932e-001) deg = 7;
         else if (l1 < 2.097847961257068e+000) deg = 9;
@@ -200,6 +206,7 @@ __device__ double* expm_block(const ExpmBuf& B, int k, int* status) {
             deg = 13;
             (void)frexp(l1 / 5.371920351148152, &sq);
             if (sq < 0) sq = 0;
+            if (sq > 1100) sq = 1100;  // beyond the double range: l1 is finite here
         }
         s_deg = deg;
         s_sq = sq;
@@ -440,22 +447,26 @@ size_t expm_smem_bytes(int k) {
     return sizeof(double) * (6 * static_cast<size_t>(k) * k + MEXK_M_MAX) + sizeof(int) * MEXK_M_MAX;
 }
 
+// Dynamic shared memory of an exponential kernel for dimensions up to m:
+// none when the matrices live in the global workspace.
+size_t expm_launch_smem(int m) { return m > EXPM_SMEM_K ? 0 : expm_smem_bytes(m); }
+
 __global__ void __launch_bounds__(EXPM_THREADS)
     expm_standalone_kernel(int k, const double* __restrict__ A, int lda, double* __restrict__ E, int lde,
-                           int* status) {
+                           int* status, double* ws) {
     extern __shared__ double smem[];
-    ExpmBuf B = carve(smem, k);
+    ExpmBuf B = carve(k > EXPM_SMEM_K ? ws : smem, k);
     for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = A[(e % k) + static_cast<size_t>(e / k) * lda];
     __syncthreads();
     double* R = expm_block(B, k, status);
     for (int e = threadIdx.x; e < k * k; e += blockDim.x) E[(e % k) + static_cast<size_t>(e / k) * lde] = R[e];
 }
 
-enum : int { DEC_REJECT = 0, DEC_ACCEPT = 1, DEC_ABORT = 2 };
+enum : int { DEC_REJECT = 0, DEC_ACCEPT = 1, DEC_ABORT = 2, DEC_REBUILD = 3 };
 
 __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a, int m) {
     extern __shared__ double smem[];
-    __shared__ int s_k, s_bd, s_dec;
+    __shared__ int s_k, s_bd, s_dec, s_mcur, s_cyc_bd, s_cyc_k;
     __shared__ double s_dt;
     // One block per state: block b drives state b (a batch), or the only one.
     DevState* st = a.st + blockIdx.x;
@@ -472,16 +483,21 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
         s_k = k;
         s_bd = bd;
         s_dt = st->dt;
+        s_mcur = m;
+        s_cyc_bd = bd;  // the basis built this cycle: m columns, or k_used up to a breakdown
+        s_cyc_k = k;
     }
     __syncthreads();
-    const int k = s_k;
-    const bool bd = s_bd != 0;
     const size_t ldh = static_cast<size_t>(a.ldh);
-    ExpmBuf B = carve(smem, k);
-    int rejects = 0;
+    // The matrices in shared memory, or (m > EXPM_SMEM_K) in the workspace.
+    double* const base = m > EXPM_SMEM_K ? a.ws : smem;
+    int rejects = st->rejects;
     double err = 0.0;
     double* R = nullptr;
     while (true) {
+        const int k = s_k;
+        const bool bd = s_bd != 0;
+        ExpmBuf B = carve(base, k);
         const double dt = s_dt;
         for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = dt * Hb[(e % k) + (e / k) * ldh];
         __syncthreads();
@@ -496,6 +512,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
                 L.m_used = k;
                 L.accepts = st->accepted;
                 L.rejects = rejects;
+                L.m_basis = s_mcur;
             }
             st->nlog += 1;
             st->attempts += 1;
@@ -507,9 +524,28 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
                 if (rejects >= st->max_rejects) {
                     dec = DEC_ABORT;
                 } else {
-                    dec = DEC_REJECT;
-                    const double dt_new = dt * 0.5 * 0.8;
-                    s_dt = dt_new > st->dt_min ? dt_new : st->dt_min;
+                    // main.cu:1507-1513: retry the same dt with a basis m_step
+                    // larger (adapt_m, up to m_max), else a shrunk dt with the
+                    // base dimension. The reference rebuilds the basis; a basis
+                    // of m' columns is the first m' of this cycle's (up to its
+                    // breakdown, where a larger one breaks down too), so only a
+                    // larger basis than this cycle built needs the next cycle.
+                    int mc = s_mcur + st->m_step;
+                    const bool grow_m = st->adapt_m && st->m_step > 0 && mc <= st->m_max;
+                    if (grow_m) {
+                        dec = (mc > m && !s_cyc_bd) ? DEC_REBUILD : DEC_REJECT;
+                    } else {
+                        dec = DEC_REJECT;
+                        const double dt_new = (dt * st->shrink) * st->safety;
+                        s_dt = dt_new > st->dt_min ? dt_new : st->dt_min;
+                        mc = st->m_base;
+                    }
+                    s_mcur = mc;
+                    if (dec == DEC_REJECT) {
+                        const bool bd2 = s_cyc_bd && s_cyc_k <= mc;
+                        s_k = bd2 ? s_cyc_k : mc;
+                        s_bd = bd2 ? 1 : 0;
+                    }
                 }
             }
             s_dec = dec;
@@ -517,25 +553,42 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
         __syncthreads();
         if (s_dec != DEC_REJECT) break;
     }
+    const int k = s_k;
+    if (s_dec == DEC_REBUILD) {
+        if (threadIdx.x == 0) {
+            st->rejects = rejects;
+            st->m_next = s_mcur;
+            st->k_used = st->m_next;
+            st->breakdown = 0;
+            st->cycles += 1;
+            st->spmv_count += k;
+            st->lift = 0;
+            st->restart = 0;
+        }
+        return;
+    }
     // Lift coefficients |v| * wH_i, zero where |wH_i| <= 1e-15 (main.cu:1993).
     const double vn = st->v_norm;
     for (int i = threadIdx.x; i <= k; i += blockDim.x) {
         const double wi = (i < k) ? R[i] : 0.0;
-        coef[i] = (fabs(wi) > 1e-15) ? vn * wi : 0.0;
+        coef[i] = (fabs(wi) > 1e-15 && isfinite(wi)) ? vn * wi : 0.0;
     }
     if (threadIdx.x == 0) {
         double dt = s_dt;
+        st->rejects = 0;
+        st->m_next = st->m_base;
         if (s_dec == DEC_ACCEPT) {
             st->t_done += dt;
             st->accepted += 1;
             st->last_residual = err;
+            st->err_acc += err;
             if (st->t_done >= st->total_t) {
                 st->converged = 1;
                 st->done = 1;
                 st->restart = 0;
             } else {
                 if (err < 0.1 * st->tol) {
-                    const double dt_new = dt * 1.5 * 0.8;
+                    const double dt_new = (dt * st->grow) * st->safety;
                     dt = dt_new < st->dt_max ? dt_new : st->dt_max;
                 }
                 if (st->accepted >= st->max_steps) {
@@ -558,7 +611,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
         st->lift = 1;
         if (!st->done) {
             st->breakdown = 0;
-            st->k_used = m;
+            st->k_used = st->m_base;
             const double rem = st->total_t - st->t_done;
             dt = dt < rem ? dt : rem;
         }
@@ -575,6 +628,7 @@ __device__ void finish_cycle(DevState* st, bool accept, double tau, double err, 
         st->t_done += tau;
         st->accepted += 1;
         st->last_residual = err;
+        st->err_acc += err;
         if (st->t_done >= st->total_t) {
             st->converged = 1;
             st->done = 1;
@@ -582,7 +636,7 @@ __device__ void finish_cycle(DevState* st, bool accept, double tau, double err, 
         } else {
             if (grow_reference) {
                 if (err < 0.1 * st->tol) {
-                    const double dt_new = dt * 1.5 * 0.8;
+                    const double dt_new = (dt * st->grow) * st->safety;
                     dt = dt_new < st->dt_max ? dt_new : st->dt_max;
                 }
             } else {
@@ -618,7 +672,7 @@ __device__ void finish_cycle(DevState* st, bool accept, double tau, double err, 
     st->dt = dt;
 }
 
-__device__ void write_log(DevState* st, mexk_step_t* log, double dt, double err, int k, int rejects) {
+__device__ void write_log(DevState* st, mexk_step_t* log, double dt, double err, int k, int rejects, int m) {
     if (log != nullptr && st->nlog < st->log_cap) {
         mexk_step_t& L = log[st->nlog];
         L.t_done = st->t_done;
@@ -627,6 +681,7 @@ __device__ void write_log(DevState* st, mexk_step_t* log, double dt, double err,
         L.m_used = k;
         L.accepts = st->accepted;
         L.rejects = rejects;
+        L.m_basis = m;
     }
     st->nlog += 1;
     st->attempts += 1;
@@ -660,7 +715,11 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
     const bool bd = s_bd != 0;
     const size_t ldh = static_cast<size_t>(a.ldh);
     const double rem = st->total_t - st->t_done;
-    const double tol_eff = fmax(st->tol, st->tol_floor_rel * st->v_norm);
+    // Mixed precision: a step may also pass below the FP32 resolution of the
+    // iterate, while the errors accepted so far stay within err_budget_rel of
+    // its norm (both zero for FP64).
+    const double relax = fmin(st->tol_floor_rel * st->v_norm, st->err_budget_rel * st->v_norm - st->err_acc);
+    const double tol_eff = fmax(st->tol, relax);
     // Learned centre and next dimension: every block evaluates the network on
     // the same inputs, so all agree on the candidate grid.
     double spacing = 0.25;
@@ -737,11 +796,11 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         const double* c = a.cand + static_cast<size_t>(s_best) * CAND_STRIDE;
         for (int i = threadIdx.x; i <= k; i += blockDim.x) {
             const double wi = (i < k) ? __ldcg(&c[2 + i]) : 0.0;
-            a.coef[i] = (fabs(wi) > 1e-15) ? vn * wi : 0.0;
+            a.coef[i] = (fabs(wi) > 1e-15 && isfinite(wi)) ? vn * wi : 0.0;
         }
         if (threadIdx.x == 0) {
             const double tau = __ldcg(&c[1]), err = __ldcg(&c[0]);
-            write_log(st, a.log, tau, err, k, 0);
+            write_log(st, a.log, tau, err, k, 0, m);
             // next centre without a network: double the step (the grid reaches 1/64 of it)
             finish_cycle(st, true, tau, err, k, s_mnext, 2.0 * tau, false);
         }
@@ -755,7 +814,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
     double* R = nullptr;
     while (true) {
         if (threadIdx.x == 0) {
-            const double dt_new = s_tau * 0.5 * 0.8;
+            const double dt_new = (s_tau * st->shrink) * st->safety;
             s_tau = dt_new > st->dt_min ? dt_new : st->dt_min;
         }
         __syncthreads();
@@ -765,7 +824,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         R = expm_taylor_block(B, k);
         if (threadIdx.x == 0) {
             err = bd ? 0.0 : fabs(a.H[k + (k - 1) * ldh] * R[k - 1]) * st->v_norm;
-            write_log(st, a.log, dt, err, k, rejects);
+            write_log(st, a.log, dt, err, k, rejects, m);
             if (err <= tol_eff || bd) {
                 s_dec = DEC_ACCEPT;
             } else {
@@ -778,7 +837,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
     }
     for (int i = threadIdx.x; i <= k; i += blockDim.x) {
         const double wi = (i < k) ? R[i] : 0.0;
-        a.coef[i] = (fabs(wi) > 1e-15) ? vn * wi : 0.0;
+        a.coef[i] = (fabs(wi) > 1e-15 && isfinite(wi)) ? vn * wi : 0.0;
     }
     if (threadIdx.x == 0) finish_cycle(st, s_dec == DEC_ACCEPT, s_tau, err, k, s_mnext, 2.0 * s_tau, false);
 }
@@ -786,6 +845,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
 }  // namespace
 
 int launch_controller_search(const SearchArgs& a, int m, cudaStream_t s) {
+    if (m > EXPM_SMEM_K) return MEXK_ERR_UNSUPPORTED;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(SEARCH_CAND * SEARCH_CLUSTER);
     cfg.blockDim = dim3(EXPM_THREADS);
@@ -806,23 +866,30 @@ int launch_controller_search(const SearchArgs& a, int m, cudaStream_t s) {
     return MEXK_OK;
 }
 
+size_t expm_ws_doubles(int k) {
+    return 6 * static_cast<size_t>(k) * k + MEXK_M_MAX + (sizeof(int) * MEXK_M_MAX + sizeof(double) - 1) / sizeof(double);
+}
+
 int expm_init_attributes() {
-    const int bytes = static_cast<int>(expm_smem_bytes(MEXK_M_MAX));
+    const int bytes = static_cast<int>(expm_smem_bytes(EXPM_SMEM_K));
     MEXK_CK(cudaFuncSetAttribute(expm_standalone_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     MEXK_CK(cudaFuncSetAttribute(controller_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     MEXK_CK(cudaFuncSetAttribute(controller_search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     return MEXK_OK;
 }
 
-int launch_expm_standalone(int k, const double* A, int lda, double* E, int lde, int* status, cudaStream_t s) {
-    const size_t smem = expm_smem_bytes(k);
-    expm_standalone_kernel<<<1, EXPM_THREADS, smem, s>>>(k, A, lda, E, lde, status);
+int launch_expm_standalone(int k, const double* A, int lda, double* E, int lde, int* status, double* ws,
+                           cudaStream_t s) {
+    if (k > EXPM_SMEM_K && ws == nullptr) return MEXK_ERR_INVALID;
+    const size_t smem = expm_launch_smem(k);
+    expm_standalone_kernel<<<1, EXPM_THREADS, smem, s>>>(k, A, lda, E, lde, status, ws);
     MEXK_CK_LAUNCH("expm_standalone_kernel");
     return MEXK_OK;
 }
 
 int launch_controller(const ControlArgs& a, int m, cudaStream_t s, int nstates) {
-    const size_t smem = expm_smem_bytes(m);
+    if (m > EXPM_SMEM_K && (a.ws == nullptr || nstates != 1)) return MEXK_ERR_INVALID;
+    const size_t smem = expm_launch_smem(m);
     controller_kernel<<<nstates, EXPM_THREADS, smem, s>>>(a, m);
     MEXK_CK_LAUNCH("controller_kernel");
     return MEXK_OK;
@@ -836,9 +903,18 @@ extern "C" int mexk_expm_f64(int k, const double* A, int lda, double* E, int lde
     int rc0 = mexk::expm_init_attributes();
     if (rc0 != MEXK_OK) return rc0;
     int* d_status = nullptr;
+    double* d_ws = nullptr;
     MEXK_CK(cudaMallocAsync(reinterpret_cast<void**>(&d_status), sizeof(int), s));
+    if (k > mexk::EXPM_SMEM_K) {
+        const cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&d_ws), sizeof(double) * mexk::expm_ws_doubles(k), s);
+        if (e != cudaSuccess) {
+            cudaFreeAsync(d_status, s);
+            mexk::set_cuda_error(e, "cudaMallocAsync", __FILE__, __LINE__);
+            return MEXK_ERR_ALLOC;
+        }
+    }
     MEXK_CK(cudaMemsetAsync(d_status, 0, sizeof(int), s));
-    int rc = mexk::launch_expm_standalone(k, A, lda, E, lde, d_status, s);
+    int rc = mexk::launch_expm_standalone(k, A, lda, E, lde, d_status, d_ws, s);
     int h_status = 0;
     if (rc == MEXK_OK) {
         cudaError_t e = cudaMemcpyAsync(&h_status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -849,6 +925,7 @@ extern "C" int mexk_expm_f64(int k, const double* A, int lda, double* E, int lde
         }
     }
     cudaFreeAsync(d_status, s);
+    if (d_ws) cudaFreeAsync(d_ws, s);
     cudaStreamSynchronize(s);
     if (rc == MEXK_OK && (h_status & mexk::ST_LU_SINGULAR)) rc = MEXK_ERR_DEVICE;
     return rc;

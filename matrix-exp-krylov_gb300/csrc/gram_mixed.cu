@@ -101,7 +101,7 @@ __device__ __noinline__ void gram_finish(const GramArgs& g, int nrb) {
     const int lo = g.lo;
     const int kw = k - lo;
     const int jw = j - lo;  // previous columns inside the window
-    __shared__ double s_tot[2 * MEXK_M_MAX + 1];  // a (kw), b (kw), |w|^2
+    __shared__ double s_tot[2 * GRAM_M + 1];  // a (kw), b (kw), |w|^2
     __shared__ double s_c[CAP], s_h[CAP], s_sc[CAP], s_y[CAP];
     __shared__ double s_G[CAP][CAP + 1];  // G(lo:k, lo:k), row-major, padded, indexed from lo
     __shared__ double s_sj, s_w2s;
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(GT, 4) gram_dot_kernel(GramArgs g) {
     // grid stage: the last block sums the row blocks and finishes the step
     __shared__ int s_flag;
     if (!grid_last_block(g.counter, &s_flag)) return;
-    gram_finish<MEXK_M_MAX>(g, nrb);
+    gram_finish<GRAM_M>(g, nrb);
 }
 
 // Sweep 1 for a step over at most two columns (the first two Arnoldi steps,
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
     pdl_wait();
     DevState* st = g.st;
     if (st->breakdown || st->done) return;
-    __shared__ float s_coef[MEXK_M_MAX + UCH];
+    __shared__ float s_coef[GRAM_M + UCH];
     __shared__ float s_sc[2];
     const int k = g.j + 1;
     const int lo = g.lo;
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
     // in L2 (default loads); a long basis is streamed (evict-first)
     const bool keep = k - lo <= 4;
     const GramState* gs = g.gs;
-    if (threadIdx.x < MEXK_M_MAX + UCH) s_coef[threadIdx.x] = threadIdx.x < k ? gs->coef[threadIdx.x] : 0.f;
+    if (threadIdx.x < GRAM_M + UCH) s_coef[threadIdx.x] = threadIdx.x < k ? gs->coef[threadIdx.x] : 0.f;
     if (threadIdx.x == 0) {
         s_sc[0] = gs->wsc;
         s_sc[1] = gs->psc;
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(GT, 4) gram_update_kernel(GramArgs g) {
         const float4 x = __ldg(w4 + i);
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int cbi = 0; cbi < MEXK_M_MAX; cbi += UCH) {
+        for (int cbi = 0; cbi < GRAM_M; cbi += UCH) {
             const int cb = lo + cbi;
             if (cb < k) {
                 float4 v[UCH];
@@ -554,7 +554,7 @@ int device_sm_count() {
 }
 
 int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
-    if (a.j < 0 || a.j >= MEXK_M_MAX) return MEXK_ERR_INVALID;
+    if (a.j < 0 || a.j >= GRAM_M) return MEXK_ERR_INVALID;
     if (a.lo < 0 || a.lo > a.j) return MEXK_ERR_INVALID;
     const int kw = a.j + 1 - a.lo;
     cudaError_t e;
@@ -580,7 +580,7 @@ int launch_gram_dot(const GramArgs& a, cudaStream_t s) {
 int gram_update2_blocks(int n) { return row_blocks((n + 1) / 2, 4); }
 
 int launch_gram_update(const GramArgs& a, cudaStream_t s) {
-    if (a.j < 0 || a.j >= MEXK_M_MAX || a.lo < 0 || a.lo > a.j) return MEXK_ERR_INVALID;
+    if (a.j < 0 || a.j >= GRAM_M || a.lo < 0 || a.lo > a.j) return MEXK_ERR_INVALID;
     const cudaError_t e = a.j + 1 - a.lo <= 2
                               ? launch_dependent(gram_update2_kernel, gram_update2_blocks(a.n), GT, 0, s, a)
                               : launch_dependent(gram_update_kernel, row_blocks(a.n, 4), GT, 0, s, a);
@@ -592,7 +592,7 @@ int launch_gram_update(const GramArgs& a, cudaStream_t s) {
 }
 
 int launch_gram_norm(const GramArgs& a, cudaStream_t s) {
-    if (a.j < 0 || a.j >= MEXK_M_MAX) return MEXK_ERR_INVALID;
+    if (a.j < 0 || a.j >= GRAM_M) return MEXK_ERR_INVALID;
     gram_norm_kernel<<<row_blocks(a.n, 4), GT, 0, s>>>(a);
     MEXK_CK_LAUNCH("gram_norm_kernel");
     return MEXK_OK;

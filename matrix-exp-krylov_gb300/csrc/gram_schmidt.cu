@@ -19,6 +19,7 @@
 // form orthogonalises its FP32 basis in gram_mixed.cu.
 #include "mexk_internal.cuh"
 
+#include <limits.h>
 #include <math.h>
 
 namespace mexk {
@@ -74,24 +75,29 @@ __device__ __forceinline__ void acc_dot(Acc<double>& a, const double (&v)[RPT], 
 // Grid stage shared by both sweep kernels: after every block wrote its
 // partials, the last block to arrive sums them in block order and writes the
 // Hessenberg entries, the next pass's coefficients, or the norm and the
-// breakdown test (main.cu:1911).
+// breakdown test (main.cu:1911). A dot sweep reduces columns c0..c0+ncols-1.
 template <int MODE>
 __device__ __forceinline__ void gs_finish(const GsArgs& a, int ncols, double* s_out, double* s_scratch, int* s_flag) {
     if (!grid_last_block(a.counter, s_flag)) return;
     reduce_partials(a.partials, gridDim.x, ncols, s_out, s_scratch);
     DevState* st = a.st;
-    const int k = a.k;
     const int j = a.j;
+    const int c = a.c0 + static_cast<int>(threadIdx.x);
     const size_t ldh = static_cast<size_t>(a.ldh);
     if (MODE == GS_DOT) {
-        if (threadIdx.x < k) {
-            a.h1[threadIdx.x] = s_out[threadIdx.x];
-            if (!a.reortho && a.H) a.H[threadIdx.x + j * ldh] = s_out[threadIdx.x];
+        if (static_cast<int>(threadIdx.x) < ncols) {
+            if (a.pass2) {
+                a.h2[c] = s_out[threadIdx.x];
+                if (a.H) a.H[c + j * ldh] = a.h1[c] + s_out[threadIdx.x];
+            } else {
+                a.h1[c] = s_out[threadIdx.x];
+                if (!a.reortho && a.H) a.H[c + j * ldh] = s_out[threadIdx.x];
+            }
         }
     } else if (MODE == GS_UPD_DOT) {
-        if (threadIdx.x < k) {
-            a.h2[threadIdx.x] = s_out[threadIdx.x];
-            if (a.H) a.H[threadIdx.x + j * ldh] = a.h1[threadIdx.x] + s_out[threadIdx.x];
+        if (static_cast<int>(threadIdx.x) < ncols) {
+            a.h2[c] = s_out[threadIdx.x];
+            if (a.H) a.H[c + j * ldh] = a.h1[c] + s_out[threadIdx.x];
         }
     } else if (threadIdx.x == 0) {
         const double beta = sqrt(s_out[0]);
@@ -109,12 +115,35 @@ __device__ __forceinline__ void gs_finish(const GsArgs& a, int ncols, double* s_
     }
 }
 
-// One row group (RPT rows starting at r0) of a sweep. Columns are read in
-// chunks of CH so that only the accumulators stay live across the loop.
+// Update part of a row group: s += sum_c h_c V[r0.., c] for columns
+// cb0 .. k-1 in order (CH at a time).
+template <int CH, typename TV, int RPT, typename TC>
+__device__ __forceinline__ void gs_upd_cols(const TV* __restrict__ V, size_t ldv, size_t r0, int cb, int k,
+                                           const TC* s_h, TC (&s)[RPT]) {
+    using IO = RowIO<RPT, TV>;
+    TV vv[CH][RPT];
+#pragma unroll
+    for (int cc = 0; cc < CH; ++cc)
+        if (cb + cc < k) IO::ld(V + (cb + cc) * ldv + r0, vv[cc]);
+#pragma unroll
+    for (int cc = 0; cc < CH; ++cc)
+        if (cb + cc < k) {
+            const TC h = s_h[cb + cc];
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) s[i] = fma(static_cast<TC>(vv[cc][i]), h, s[i]);
+        }
+}
+
+// One row group (RPT rows starting at r0) of a sweep: the update subtracts
+// sum_c h_c V[:, c] over all k columns, the dots reduce columns c0..c0+kd-1
+// (kd <= KMAX). Columns are read in chunks of CH so that only the
+// accumulators stay live across the loop; in the KEEP form (every column's
+// rows fit in registers; the launch guarantees c0 = 0 and kd = k <= KMAX)
+// each column is loaded once.
 template <int KMAX, int MODE, typename TV, int RPT>
 __device__ __forceinline__ void gs_rows(const TV* __restrict__ V, size_t ldv, TV* __restrict__ w, size_t r0,
-                                       int k, const typename Compute<TV>::type* s_h, Acc<TV> (&acc)[KMAX],
-                                       Acc<TV>& nacc) {
+                                       int k, int c0, int kd, const typename Compute<TV>::type* s_h,
+                                       Acc<TV> (&acc)[KMAX], Acc<TV>& nacc) {
     using TC = typename Compute<TV>::type;
     using IO = RowIO<RPT, TV>;
     constexpr int CH = 8;
@@ -165,21 +194,12 @@ __device__ __forceinline__ void gs_rows(const TV* __restrict__ V, size_t ldv, TV
 #pragma unroll
             for (int i = 0; i < RPT; ++i) s[i] = TC(0);
 #pragma unroll
-            for (int cb = 0; cb < KMAX; cb += CH) {
-                if (cb < k) {
-                    TV vv[CH][RPT];
-#pragma unroll
-                    for (int cc = 0; cc < CH; ++cc)
-                        if (cb + cc < k) IO::ld(V + (cb + cc) * ldv + r0, vv[cc]);
-#pragma unroll
-                    for (int cc = 0; cc < CH; ++cc)
-                        if (cb + cc < k) {
-                            const TC h = s_h[cb + cc];
-#pragma unroll
-                            for (int i = 0; i < RPT; ++i) s[i] = fma(static_cast<TC>(vv[cc][i]), h, s[i]);
-                        }
-                }
-            }
+            for (int cb = 0; cb < KMAX; cb += CH)
+                if (cb < k) gs_upd_cols<CH, TV, RPT, TC>(V, ldv, r0, cb, k, s_h, s);
+            // bases wider than the sweep's width (FP64, more than GS_DOT_COLS
+            // columns; the launch picks the full width for those)
+            if constexpr (KMAX == GS_DOT_COLS)
+                for (int cb = KMAX; cb < k; cb += CH) gs_upd_cols<CH, TV, RPT, TC>(V, ldv, r0, cb, k, s_h, s);
 #pragma unroll
             for (int i = 0; i < RPT; ++i) {
                 wr[i] = wr[i] - s[i];
@@ -188,19 +208,20 @@ __device__ __forceinline__ void gs_rows(const TV* __restrict__ V, size_t ldv, TV
             IO::st(w + r0, wv);
         }
         if (MODE != GS_UPD_NORM) {
+            const TV* Vd = V + static_cast<size_t>(c0) * ldv;
 #pragma unroll
             for (int cb = 0; cb < KMAX; cb += CH) {
-                if (cb < k) {
+                if (cb < kd) {
                     TV vv[CH][RPT];
 #pragma unroll
                     for (int cc = 0; cc < CH; ++cc)
-                        if (cb + cc < k) {
-                            if (MODE == GS_UPD_DOT) IO::ldg(V + (cb + cc) * ldv + r0, vv[cc]);
-                            else IO::ldcs(V + (cb + cc) * ldv + r0, vv[cc]);
+                        if (cb + cc < kd) {
+                            if (MODE == GS_UPD_DOT) IO::ldg(Vd + (cb + cc) * ldv + r0, vv[cc]);
+                            else IO::ldcs(Vd + (cb + cc) * ldv + r0, vv[cc]);
                         }
 #pragma unroll
                     for (int cc = 0; cc < CH; ++cc)
-                        if (cb + cc < k) {
+                        if (cb + cc < kd) {
                             TC vc[RPT];
 #pragma unroll
                             for (int i = 0; i < RPT; ++i) vc[i] = static_cast<TC>(vv[cc][i]);
@@ -230,12 +251,14 @@ __global__ void __launch_bounds__(GS_THREADS, (gs_min_blocks<KMAX, MODE>())) gs_
     __shared__ double s_red[NW][KMAX + 1];
     __shared__ double s_out[KMAX + 1];
     __shared__ double s_scratch[GS_THREADS];
-    __shared__ TC s_h[KMAX];
+    __shared__ TC s_h[MEXK_M_MAX];
     __shared__ int s_flag;
 
     DevState* st = a.st;
     if (st != nullptr && (st->breakdown || st->done)) return;
     const int k = a.k;
+    const int c0 = a.c0;
+    const int kd = a.kd > 0 ? a.kd : k;
     const int n = a.n;
     const size_t ldv = static_cast<size_t>(a.ldv);
     const TV* __restrict__ V = static_cast<const TV*>(a.V);
@@ -245,7 +268,7 @@ __global__ void __launch_bounds__(GS_THREADS, (gs_min_blocks<KMAX, MODE>())) gs_
 
     if (MODE != GS_DOT) {
         const double* hin = (MODE == GS_UPD_DOT || !a.reortho) ? a.h1 : a.h2;
-        if (threadIdx.x < KMAX) s_h[threadIdx.x] = (threadIdx.x < k) ? static_cast<TC>(hin[threadIdx.x]) : TC(0);
+        for (int c = threadIdx.x; c < k; c += GS_THREADS) s_h[c] = static_cast<TC>(hin[c]);
         __syncthreads();
     }
 
@@ -255,19 +278,20 @@ __global__ void __launch_bounds__(GS_THREADS, (gs_min_blocks<KMAX, MODE>())) gs_
     for (int c = 0; c < KMAX; ++c) acc[c].zero();
     nacc.zero();
 
+    // launch_gs refuses n > INT_MAX - GS_MAX_GRID * GS_THREADS: no counter overflows
     const int stride = gridDim.x * GS_THREADS;
     const int ngroups = n / RPT;
     for (int g = blockIdx.x * GS_THREADS + threadIdx.x; g < ngroups; g += stride)
-        gs_rows<KMAX, MODE, TV, RPT>(V, ldv, w, static_cast<size_t>(g) * RPT, k, s_h, acc, nacc);
+        gs_rows<KMAX, MODE, TV, RPT>(V, ldv, w, static_cast<size_t>(g) * RPT, k, c0, kd, s_h, acc, nacc);
     if (RPT > 1) {
         for (int r = ngroups * RPT + blockIdx.x * GS_THREADS + threadIdx.x; r < n; r += stride)
-            gs_rows<KMAX, MODE, TV, 1>(V, ldv, w, static_cast<size_t>(r), k, s_h, acc, nacc);
+            gs_rows<KMAX, MODE, TV, 1>(V, ldv, w, static_cast<size_t>(r), k, c0, kd, s_h, acc, nacc);
     }
 
     // ---- block reduction
     int ncols;
     if (MODE != GS_UPD_NORM) {
-        ncols = k;
+        ncols = kd;
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
             double part[KR];
@@ -283,7 +307,7 @@ __global__ void __launch_bounds__(GS_THREADS, (gs_min_blocks<KMAX, MODE>())) gs_
         if (lane == 0) s_red[warp][0] = v;
     }
     __syncthreads();
-    if (threadIdx.x < ncols) {
+    if (static_cast<int>(threadIdx.x) < ncols) {
         double s = 0.0;
 #pragma unroll
         for (int q = 0; q < NW; ++q) s += s_red[q][threadIdx.x];
@@ -342,12 +366,20 @@ int launch_k(const GsArgs& a, int grid, cudaStream_t s) {
     return launch_one<KMAX, MODE, TV, 1>(a, grid, s);
 }
 
+// The width is set by the columns the sweep reduces (the update-and-norm
+// sweep reduces none: its width only decides whether columns stay in registers).
 template <int MODE, typename TV>
 int launch_mode(const GsArgs& a, int grid, cudaStream_t s) {
-    if (a.k <= 8) return launch_k<8, MODE, TV>(a, grid, s);
-    if (a.k <= 16) return launch_k<16, MODE, TV>(a, grid, s);
-    if (a.k <= 32) return launch_k<32, MODE, TV>(a, grid, s);
-    if (a.k <= 64) return launch_k<64, MODE, TV>(a, grid, s);
+    const int kd = MODE == GS_UPD_NORM ? (a.k < GS_DOT_COLS ? a.k : GS_DOT_COLS) : (a.kd > 0 ? a.kd : a.k);
+    // A chunk of a wider basis (dot columns other than all k) takes a width
+    // whose row groups do not stay in registers (those assume the dot
+    // columns are the update's).
+    const bool chunk = a.c0 != 0 || kd != a.k;
+    if (chunk) return kd <= 32 ? launch_k<32, MODE, TV>(a, grid, s) : launch_k<GS_DOT_COLS, MODE, TV>(a, grid, s);
+    if (kd <= 8) return launch_k<8, MODE, TV>(a, grid, s);
+    if (kd <= 16) return launch_k<16, MODE, TV>(a, grid, s);
+    if (kd <= 32) return launch_k<32, MODE, TV>(a, grid, s);
+    if (kd <= GS_DOT_COLS) return launch_k<GS_DOT_COLS, MODE, TV>(a, grid, s);
     return MEXK_ERR_UNSUPPORTED;
 }
 
@@ -407,13 +439,56 @@ void gs_prepare() {
 
 template <typename TV>
 int launch_gs(GsMode mode, const GsArgs& a, int grid, cudaStream_t s) {
-    if (a.k < 1 || a.k > MEXK_M_MAX) return MEXK_ERR_INVALID;
+    const int kd = a.kd > 0 ? a.kd : a.k;
+    if (a.k < 1 || a.k > MEXK_M_MAX || a.c0 < 0 || a.c0 + kd > a.k) return MEXK_ERR_INVALID;
+    if (a.n < 1 || a.n > INT_MAX - GS_MAX_GRID * GS_THREADS || grid < 1 || grid > GS_MAX_GRID) {
+        set_error_text("Gram-Schmidt sweep: n or grid out of range");
+        return MEXK_ERR_INVALID;
+    }
+    if (mode != GS_UPD_NORM && kd > GS_DOT_COLS) return MEXK_ERR_UNSUPPORTED;
     switch (mode) {
         case GS_DOT: return launch_mode<GS_DOT, TV>(a, grid, s);
         case GS_UPD_DOT: return launch_mode<GS_UPD_DOT, TV>(a, grid, s);
         case GS_UPD_NORM: return launch_mode<GS_UPD_NORM, TV>(a, grid, s);
     }
     return MEXK_ERR_INVALID;
+}
+
+int launch_gs_step(const GsArgs& g0, int grid, cudaStream_t s) {
+    int rc;
+    if (g0.k <= GS_DOT_COLS) {
+        GsArgs g = g0;
+        g.c0 = 0;
+        g.kd = 0;
+        g.pass2 = 0;
+        if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
+        if (g.reortho && (rc = launch_gs<double>(GS_UPD_DOT, g, grid, s))) return rc;
+        return launch_gs<double>(GS_UPD_NORM, g, grid, s);
+    }
+    GsArgs g = g0;
+    g.pass2 = 0;
+    for (int c0 = 0; c0 < g0.k; c0 += GS_DOT_COLS) {  // pass-1 dots, one launch per column chunk
+        g.c0 = c0;
+        g.kd = g0.k - c0 < GS_DOT_COLS ? g0.k - c0 : GS_DOT_COLS;
+        if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
+    }
+    if (g0.reortho) {
+        // pass-1 update of every column fused with the first chunk's pass-2
+        // dots, then the other chunks' pass-2 dots on the updated vector
+        g.c0 = 0;
+        g.kd = GS_DOT_COLS;
+        if ((rc = launch_gs<double>(GS_UPD_DOT, g, grid, s))) return rc;
+        g.pass2 = 1;
+        for (int c0 = GS_DOT_COLS; c0 < g0.k; c0 += GS_DOT_COLS) {
+            g.c0 = c0;
+            g.kd = g0.k - c0 < GS_DOT_COLS ? g0.k - c0 : GS_DOT_COLS;
+            if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
+        }
+    }
+    g.c0 = 0;
+    g.kd = 0;
+    g.pass2 = 0;
+    return launch_gs<double>(GS_UPD_NORM, g, grid, s);
 }
 
 template <typename TV>

@@ -18,21 +18,24 @@
 // results; serialise them.
 #include "mexk_internal.cuh"
 
-#include <mutex>
 
 namespace mexk {
 namespace {
 
 // Largest grid the kernels may use with this scratch (gs_grid_size gives at
-// most 4 blocks per SM: 608 on a 152-SM GB300).
+// most 4 blocks per SM: 608 on a 152-SM GB300); larger grids are capped, the
+// sweeps stride over the rows.
 constexpr int NOALLOC_MAX_BLOCKS = 1024;
+// Largest basis this entry point orthogonalises against (one dot sweep).
+constexpr int NOALLOC_K_MAX = 64;
+static_assert(NOALLOC_K_MAX <= GS_DOT_COLS, "one dot sweep per pass");
 
 // Byte layout of the scratch array.
 constexpr size_t OFF_PARTIALS = 0;
 constexpr size_t SZ_PARTIALS = sizeof(double) * NOALLOC_MAX_BLOCKS * RED_STRIDE;
 constexpr size_t OFF_H1 = OFF_PARTIALS + SZ_PARTIALS;
-constexpr size_t OFF_H2 = OFF_H1 + sizeof(double) * (MEXK_M_MAX + 2);
-constexpr size_t OFF_STATE = (OFF_H2 + sizeof(double) * (MEXK_M_MAX + 2) + 255) / 256 * 256;
+constexpr size_t OFF_H2 = OFF_H1 + sizeof(double) * (NOALLOC_K_MAX + 2);
+constexpr size_t OFF_STATE = (OFF_H2 + sizeof(double) * (NOALLOC_K_MAX + 2) + 255) / 256 * 256;
 constexpr size_t OFF_COUNTER = (OFF_STATE + sizeof(DevState) + 255) / 256 * 256;
 constexpr size_t SCRATCH_BYTES = OFF_COUNTER + 256;
 
@@ -40,26 +43,14 @@ constexpr size_t SCRATCH_BYTES = OFF_COUNTER + 256;
 // the process exits.
 static __device__ __align__(256) unsigned char g_gs_scratch[SCRATCH_BYTES];
 
-constexpr int MAX_DEVICES = 64;
-std::mutex g_addr_mutex;
-void* g_addr[MAX_DEVICES] = {nullptr};
-
 // Device address of g_gs_scratch on the current device. Host code cannot
 // use the symbol itself: on the host it names a stand-in, not device memory.
+// Looked up on every call (no cache): after a device reset the module, and
+// with it the array, may sit at another address.
 int scratch_address(unsigned char** out) {
-    int dev = 0;
-    MEXK_CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= MAX_DEVICES) {
-        set_error_text("device ordinal beyond the no-alloc scratch table (64 devices)");
-        return MEXK_ERR_UNSUPPORTED;
-    }
-    std::lock_guard<std::mutex> lock(g_addr_mutex);
-    if (g_addr[dev] == nullptr) {
-        void* p = nullptr;
-        MEXK_CK(cudaGetSymbolAddress(&p, g_gs_scratch));
-        g_addr[dev] = p;
-    }
-    *out = static_cast<unsigned char*>(g_addr[dev]);
+    void* p = nullptr;
+    MEXK_CK(cudaGetSymbolAddress(&p, g_gs_scratch));
+    *out = static_cast<unsigned char*>(p);
     return MEXK_OK;
 }
 
@@ -74,14 +65,24 @@ extern "C" int mexk_gram_schmidt_f64_noalloc(int n, int k, const double* V, int 
         set_error_text("mexk_gram_schmidt_f64_noalloc: bad pointer or size");
         return MEXK_ERR_INVALID;
     }
-    if (k < 1 || k > MEXK_M_MAX) {
+    if (k < 1 || k > NOALLOC_K_MAX) {
         set_error_text("mexk_gram_schmidt_f64_noalloc: k must be in 1..64 (scratch holds 64 coefficients)");
         return MEXK_ERR_INVALID;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (s != nullptr) {
+        // The scratch address belongs to the current device: so must the stream.
+        int dev = 0, sdev = 0;
+        MEXK_CK(cudaGetDevice(&dev));
+        MEXK_CK(cudaStreamGetDevice(s, &sdev));
+        if (sdev != dev) {
+            set_error_text("mexk_gram_schmidt_f64_noalloc: the stream belongs to another device than the current one");
+            return MEXK_ERR_INVALID;
+        }
     }
     unsigned char* base = nullptr;
     int rc = scratch_address(&base);
     if (rc != MEXK_OK) return rc;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     int grid = gs_grid_size(n, k);
     if (grid > NOALLOC_MAX_BLOCKS) grid = NOALLOC_MAX_BLOCKS;
     DevState* st = reinterpret_cast<DevState*>(base + OFF_STATE);
@@ -103,9 +104,7 @@ extern "C" int mexk_gram_schmidt_f64_noalloc(int n, int k, const double* V, int 
     g.counter = reinterpret_cast<unsigned int*>(base + OFF_COUNTER);
     g.st = st;
     g.beta_out = beta;
-    if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
-    if (g.reortho && (rc = launch_gs<double>(GS_UPD_DOT, g, grid, s))) return rc;
-    if ((rc = launch_gs<double>(GS_UPD_NORM, g, grid, s))) return rc;
+    if ((rc = launch_gs_step(g, grid, s))) return rc;
     // q = w / beta (column j+1 = 0 of q); skipped on breakdown.
     return launch_normalize<double>(n, -1, ldv, w, q, st, nullptr, s);
 }

@@ -21,7 +21,8 @@ namespace {
 constexpr int LIFT_THREADS = 256;
 constexpr int LIFT_BLOCKS_PER_SM = 6;  // a strided multi-column read wants many warps in flight
 
-// RPT rows of y = sum_c coef_c V_c, columns loaded 4 at a time (16-byte
+// RPT rows of y = sum_c coef_c V_c over the columns with nonzero
+// coefficients, loaded 4 at a time (16-byte
 // row groups; 40 registers, so 6 blocks of 256 threads fit an SM). FP64 basis: one DFMA chain per row in column order (the axpy
 // order). FP32 basis: FP32 products summed with compensation and widened
 // once per row, so the FP64 pipe does O(1) work per row, not O(k).
@@ -38,10 +39,10 @@ __device__ __forceinline__ void lift_rows(const TV* __restrict__ V, size_t ldv, 
             TV vv[CH][RPT];
 #pragma unroll
             for (int cc = 0; cc < CH; ++cc)
-                if (cb + cc < k) IO::ldcs(V + (cb + cc) * ldv + r0, vv[cc]);
+                if (cb + cc < k && c64[cb + cc] != 0.0) IO::ldcs(V + (cb + cc) * ldv + r0, vv[cc]);
 #pragma unroll
             for (int cc = 0; cc < CH; ++cc)
-                if (cb + cc < k) {
+                if (cb + cc < k && c64[cb + cc] != 0.0) {
 #pragma unroll
                     for (int i = 0; i < RPT; ++i) s[i] = fma(c64[cb + cc], static_cast<double>(vv[cc][i]), s[i]);
                 }
@@ -56,10 +57,10 @@ __device__ __forceinline__ void lift_rows(const TV* __restrict__ V, size_t ldv, 
             TV vv[CH][RPT];
 #pragma unroll
             for (int cc = 0; cc < CH; ++cc)
-                if (cb + cc < k) IO::ldcs(V + (cb + cc) * ldv + r0, vv[cc]);
+                if (cb + cc < k && c32[cb + cc] != 0.0f) IO::ldcs(V + (cb + cc) * ldv + r0, vv[cc]);
 #pragma unroll
             for (int cc = 0; cc < CH; ++cc)
-                if (cb + cc < k) {
+                if (cb + cc < k && c32[cb + cc] != 0.0f) {
 #pragma unroll
                     for (int i = 0; i < RPT; ++i) {
                         const float yv = __fmaf_rn(c32[cb + cc], static_cast<float>(vv[cc][i]), -comp[i]);
@@ -87,7 +88,9 @@ __global__ void __launch_bounds__(LIFT_THREADS, LIFT_BLOCKS_PER_SM) lift_kernel(
     if (!st->lift) return;
     const int k = st->k_lift;
     for (int i = threadIdx.x; i < k; i += blockDim.x) {
-        const double c = a.scale ? a.coef[i] * a.scale[i] : a.coef[i];
+        // a zero coefficient drops its column, as the reference's lift skips
+        // it (main.cu:1993): 0 * Inf or NaN entries must not reach y
+        const double c = (a.coef[i] == 0.0) ? 0.0 : (a.scale ? a.coef[i] * a.scale[i] : a.coef[i]);
         s_coef[i] = c;
         s_coef32[i] = static_cast<float>(c);
     }

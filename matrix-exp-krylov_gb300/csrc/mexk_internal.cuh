@@ -66,8 +66,18 @@ struct DevState {
     double tau_prev;
     double err_prev;
     // Candidate-step control in FP32 storage does not resolve the truncation
-    // error below the basis precision: tol_eff = max(tol, tol_floor_rel*|v|).
+    // error below the basis precision: a step also passes with
+    // err <= min(tol_floor_rel*|v|, err_budget_rel*|v| - err_acc), |v| the
+    // current iterate's norm and err_acc the errors accepted so far.
     double tol_floor_rel;
+    double tol_base;  // the caller's tolerance (batch: tol is raised per segment from it)
+    double err_budget_rel;
+    double err_acc;
+    // TimeSteppingParams (main.cu:1237-1250) as the caller set them.
+    double safety, grow, shrink;
+    int adapt_m, m_max, m_step;
+    int m_base;     // ArnoldiParams::m: the Krylov dimension each step starts from
+    int rejects;    // rejects of the current step carried across basis rebuilds (adapt_m)
 };
 
 // Status bits written by kernels.
@@ -76,6 +86,7 @@ enum : int {
     ST_SMEM = 2,
     ST_BAD_K = 4,
     ST_TIMEOUT = 8,  // a bounded wait gave up (the kernel skipped its work)
+    ST_NONFINITE = 16,  // an exponential met Inf or NaN entries (non-finite input)
 };
 
 // ------------------------------------------------------------ constants
@@ -84,7 +95,9 @@ constexpr int SPMV_TILE = 2048;     // nonzeros staged per row block
 constexpr int SPMV_TILE_ROWS = 512; // rows per row block
 constexpr int SEQ_ROW_MAX = 64;     // longest row summed by one thread (reference order)
 constexpr int GS_THREADS = 256;
-constexpr int RED_STRIDE = 72;      // doubles per block partial (>= MEXK_M_MAX + 2)
+constexpr int RED_STRIDE = 72;      // doubles per block partial (>= GS_DOT_COLS + 2)
+constexpr int GS_DOT_COLS = 64;     // basis columns one FP64 dot sweep reduces (larger k: column chunks)
+constexpr int GS_MAX_GRID = 4096;   // largest grid of a Gram-Schmidt sweep (partials hold 4096 blocks)
 
 // ------------------------------------------------------------ helpers
 // Programmatic dependent launch: a kernel launched with launch_dependent()
@@ -334,7 +347,10 @@ enum GsMode : int { GS_DOT = 0, GS_UPD_DOT = 1, GS_UPD_NORM = 2 };
 
 struct GsArgs {
     int n;
-    int k;            // number of basis columns involved (j+1)
+    int k;            // number of basis columns involved (j+1): the update sweeps use all
+    int c0 = 0;       // the dot sweep reduces columns c0 .. c0+kd-1 (kd <= GS_DOT_COLS)
+    int kd = 0;       //   (kd = 0: all k columns)
+    int pass2 = 0;    // GS_DOT on a chunk of the second pass: results into h2 and H = h1 + h2
     int j;            // Arnoldi step (column of H)
     int ldv;          // basis leading dimension (elements)
     int ldh;          // H leading dimension
@@ -357,6 +373,10 @@ struct GsArgs {
 
 template <typename TV>
 int launch_gs(GsMode mode, const GsArgs& a, int grid, cudaStream_t s);
+// The FP64 CGS2 sweeps of one step (pass-1 dots, pass-1 update + pass-2
+// dots, pass-2 update + norm); with more than GS_DOT_COLS columns the dots
+// are reduced in column chunks, one launch each.
+int launch_gs_step(const GsArgs& a, int grid, cudaStream_t s);
 int gs_grid_size(int n, int k);
 void gs_prepare();
 
@@ -366,16 +386,17 @@ int launch_normalize(int n, int j, int ldv, const TV* w, TV* V, const DevState* 
 
 // ------------------------------------------------------------ Gram-corrected sweeps (FP32 basis)
 // Column c of the FP32 basis stores u_c; the basis vector is v_c = s[c] * u_c.
-constexpr int GRAM_LD = MEXK_M_MAX + 1;         // leading dimension of G
-constexpr int GRAM_SLOTS = 2 * MEXK_M_MAX + 8;  // partial slots: a [0,64), b [64,128), |w|^2 128
-constexpr int GRAM_BOFF = MEXK_M_MAX;
-constexpr int GRAM_NWOFF = 2 * MEXK_M_MAX;
+constexpr int GRAM_M = MEXK_M_MAX_MIXED;    // largest Krylov dimension of the FP32 basis
+constexpr int GRAM_LD = GRAM_M + 1;         // leading dimension of G
+constexpr int GRAM_SLOTS = 2 * GRAM_M + 8;  // partial slots: a [0,64), b [64,128), |w|^2 128
+constexpr int GRAM_BOFF = GRAM_M;
+constexpr int GRAM_NWOFF = 2 * GRAM_M;
 constexpr int GRAM_MAX_ROW_BLOCKS = 1024;
 struct GramState {
     double G[GRAM_LD * GRAM_LD];  // Gram matrix V^T V (unit diagonal), column-major
-    double s[MEXK_M_MAX + 2];     // column scales 1/|u_c|
-    double ip[MEXK_M_MAX + 2];    // 1 / (pre-scale applied when column c was written)
-    float coef[MEXK_M_MAX + 8];   // update coefficients s_c h_c of the current step
+    double s[GRAM_M + 2];     // column scales 1/|u_c|
+    double ip[GRAM_M + 2];    // 1 / (pre-scale applied when column c was written)
+    float coef[GRAM_M + 8];   // update coefficients s_c h_c of the current step
     float wsc, psc;               // update: u_{j+1} = psc * (wsc * w - sum coef_c u_c)
 };
 struct GramArgs {
@@ -412,7 +433,11 @@ int launch_gram_norm(const GramArgs& a, cudaStream_t s);
 // Raises the dynamic shared-memory limits of the expm kernels; call once
 // per device before any launch or stream capture.
 int expm_init_attributes();
-int launch_expm_standalone(int k, const double* A, int lda, double* E, int lde, int* status,
+// Largest k whose Pade matrices fit in shared memory; larger k (up to
+// MEXK_M_MAX) work in a global-memory workspace of expm_ws_doubles(k) doubles.
+constexpr int EXPM_SMEM_K = 64;
+size_t expm_ws_doubles(int k);
+int launch_expm_standalone(int k, const double* A, int lda, double* E, int lde, int* status, double* ws,
                            cudaStream_t s);
 
 struct ControlArgs {
@@ -423,13 +448,14 @@ struct ControlArgs {
     mexk_step_t* log;   // attempt log (log_cap entries)
     size_t h_stride = 0;     // batch: state b uses st + b, H + b*h_stride,
     size_t coef_stride = 0;  //        coef + b*coef_stride (no log)
+    double* ws = nullptr;    // expm_ws_doubles(m) doubles of global memory for k > EXPM_SMEM_K
 };
 // One thread block per state (nstates > 1: a batch of independent solves).
 int launch_controller(const ControlArgs& a, int m, cudaStream_t s, int nstates = 1);
 
 // Candidate-step controller: one thread block per candidate step.
 constexpr int SEARCH_CAND = 32;
-constexpr int CAND_STRIDE = MEXK_M_MAX + 2;  // err, tau, w_0..w_{k-1}
+constexpr int CAND_STRIDE = MEXK_M_MAX_MIXED + 2;  // err, tau, w_0..w_{k-1}
 struct SearchArgs {
     DevState* st;
     const double* H;

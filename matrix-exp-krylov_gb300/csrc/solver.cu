@@ -26,11 +26,13 @@
 //   state      DevState (device) mirrored into pinned host memory
 #include "mexk_internal.cuh"
 
+#include <nvtx3/nvToolsExt.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -45,6 +47,15 @@ void set_cuda_error(cudaError_t e, const char* what, const char* file, int line)
 }
 
 void set_error_text(const std::string& s) { g_err = s; }
+
+// NVTX range over a host-side phase, named as the reference's ranges
+// (NvtxRange, main.cu:38-41): a profiler shows the solve, the start vector
+// and each Krylov cycle (whose basis build, exponential, lift and restart run
+// as one graph on the device).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
 
 constexpr int PARTIAL_BLOCKS = 4096;
 constexpr int LOG_CAP = 8192;
@@ -98,6 +109,7 @@ struct mexk_context_s {
     double* d_h2 = nullptr;
     double* d_coef = nullptr;
     double* d_cand = nullptr;
+    double* d_expm_ws = nullptr;  // Pade workspace of the reference controller for m > EXPM_SMEM_K
     float* d_mlp = nullptr;
     double* d_partials = nullptr;
     GramState* d_gram = nullptr;
@@ -161,6 +173,32 @@ int check_params(mexk_context_t ctx, const mexk_params_t* p) {
         set_error_text("Krylov dimension m out of range (1..m_alloc_max)");
         return MEXK_ERR_INVALID;
     }
+    if ((p->precision == MEXK_PREC_MIXED || p->controller != MEXK_CTRL_REFERENCE) && p->m > MEXK_M_MAX_MIXED) {
+        set_error_text("mixed precision and the candidate-step controllers take m <= 64");
+        return MEXK_ERR_UNSUPPORTED;
+    }
+    if (const mexk_stepping_t* ts = p->stepping) {
+        // The reference reads these unchecked; values that would make its loop
+        // misbehave (no progress, NaN steps) are refused here.
+        if (!(ts->dt_min > 0.0) || !(ts->dt_max >= ts->dt_min) || !(ts->dt_init > 0.0) || !(ts->tol_step >= 0.0) ||
+            !(ts->safety > 0.0) || !(ts->grow > 0.0) || !(ts->shrink > 0.0) || ts->max_steps < 0 ||
+            ts->max_rejects < 1 || !std::isfinite(ts->dt_init) || !std::isfinite(ts->dt_max)) {
+            set_error_text("time-stepping parameters out of range (dt_min > 0, dt_max >= dt_min, dt_init > 0, "
+                           "safety, grow, shrink > 0, max_rejects >= 1)");
+            return MEXK_ERR_INVALID;
+        }
+        if (ts->adapt_m && ts->m_step > 0 && ts->m_max > p->m) {
+            // main.cu:1441-1444 refuses m beyond the allocation
+            if (ts->m_max > ctx->m_alloc || ts->m_max >= ctx->n) {
+                set_error_text("adapt_m: m_max exceeds the context's allocated Krylov dimension");
+                return MEXK_ERR_INVALID;
+            }
+            if (p->precision == MEXK_PREC_MIXED || p->controller != MEXK_CTRL_REFERENCE) {
+                set_error_text("adapt_m is implemented for the FP64 form with the reference controller");
+                return MEXK_ERR_UNSUPPORTED;
+            }
+        }
+    }
     // main.cu:1322-1326: m must be smaller than the number of rows.
     if (p->m >= ctx->n) {
         set_error_text("Requested Arnoldi m must be less than the number of rows");
@@ -199,7 +237,7 @@ int reset_gram(mexk_context_t ctx, cudaStream_t s) {
     if (!init) {
         memset(&h0, 0, sizeof(h0));
         for (int i = 0; i < GRAM_LD; ++i) h0.G[i + i * GRAM_LD] = 1.0;
-        for (int i = 0; i < MEXK_M_MAX + 2; ++i) h0.s[i] = h0.ip[i] = 1.0;
+        for (int i = 0; i < GRAM_M + 2; ++i) h0.s[i] = h0.ip[i] = 1.0;
         h0.wsc = h0.psc = 1.0f;
         init = true;
     }
@@ -334,10 +372,7 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
     }
     if ((rc = context_spmv(ctx, j, false, &ctx->d_state->breakdown, s))) return rc;
     const GsArgs g = gs_args(ctx, j, reortho, false);
-    const int grid = gs_grid_size(ctx->n, j + 1);
-    if ((rc = launch_gs<double>(GS_DOT, g, grid, s))) return rc;
-    if (reortho && (rc = launch_gs<double>(GS_UPD_DOT, g, grid, s))) return rc;
-    if ((rc = launch_gs<double>(GS_UPD_NORM, g, grid, s))) return rc;
+    if ((rc = launch_gs_step(g, gs_grid_size(ctx->n, j + 1), s))) return rc;
     return launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s);
 }
 
@@ -357,6 +392,7 @@ int enqueue_controller(mexk_context_t ctx, int m, int ctrl, mexk_step_t* log, cu
         c.ldh = ctx->ldh;
         c.coef = ctx->d_coef;
         c.log = log;
+        c.ws = ctx->d_expm_ws;
         return launch_controller(c, m, s);
     }
     SearchArgs c;
@@ -429,17 +465,43 @@ void invalidate_graphs(mexk_context_t ctx) {
     ctx->graphs.clear();
 }
 
+// The reference's TimeSteppingParams defaults for ArnoldiParams
+// (ArnoldiRunner constructor, main.cu:1292-1305).
+mexk_stepping_t default_stepping(const mexk_params_t* p) {
+    mexk_stepping_t ts;
+    ts.dt_max = p->t;
+    ts.dt_min = std::max(1e-12, p->t * 1e-6);
+    const double denom = (p->max_restarts > 0) ? p->max_restarts : 1;
+    ts.dt_init = p->t / denom;
+    ts.tol_step = p->tol;
+    ts.max_steps = (p->max_restarts > 0) ? p->max_restarts : 1000;
+    ts.max_rejects = 20;
+    ts.safety = 0.8;
+    ts.grow = 1.5;
+    ts.shrink = 0.5;
+    ts.adapt_m = 0;
+    ts.m_max = p->m;
+    ts.m_step = 0;
+    return ts;
+}
+
 void init_state(DevState* st, const mexk_params_t* p, int log_cap) {
     memset(st, 0, sizeof(*st));
-    // ArnoldiRunner constructor (main.cu:1292-1305).
+    const mexk_stepping_t ts = p->stepping ? *p->stepping : default_stepping(p);
     st->total_t = p->t;
-    st->dt_max = p->t;
-    st->dt_min = std::max(1e-12, p->t * 1e-6);
-    const double denom = (p->max_restarts > 0) ? p->max_restarts : 1;
-    const double dt_init = p->t / denom;
-    st->tol = p->tol;
-    st->max_steps = (p->max_restarts > 0) ? p->max_restarts : 1000;
-    st->max_rejects = 20;
+    st->dt_max = ts.dt_max;
+    st->dt_min = ts.dt_min;
+    const double dt_init = ts.dt_init;
+    st->tol = ts.tol_step;
+    st->max_steps = ts.max_steps;
+    st->max_rejects = ts.max_rejects;
+    st->safety = ts.safety;
+    st->grow = ts.grow;
+    st->shrink = ts.shrink;
+    st->adapt_m = (ts.adapt_m && ts.m_step > 0 && ts.m_max > p->m) ? 1 : 0;
+    st->m_step = ts.m_step;
+    st->m_max = ts.m_max;
+    st->m_base = p->m;
     st->m = p->m;
     // compute_expmv (main.cu:1426-1434): clamp, then the first outer iteration's min.
     double dt = std::min(std::max(dt_init, st->dt_min), st->dt_max);
@@ -450,14 +512,15 @@ void init_state(DevState* st, const mexk_params_t* p, int log_cap) {
     st->k_used = p->m;
     st->m_next = p->m;
     st->ctrl = p->controller;
-    st->tol_floor_rel = (p->controller != MEXK_CTRL_REFERENCE && p->precision == MEXK_PREC_MIXED)
-                            ? 5.9604644775390625e-08  // 2^-24, the FP32 unit roundoff
-                            : 0.0;
+    const bool relax = p->controller != MEXK_CTRL_REFERENCE && p->precision == MEXK_PREC_MIXED;
+    st->tol_floor_rel = relax ? 5.9604644775390625e-08 : 0.0;  // 2^-24, the FP32 unit roundoff
+    st->err_budget_rel = relax ? 5e-7 : 0.0;
     st->log_cap = log_cap;
 }
 
 int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, double* y_dev, cudaStream_t s,
           mexk_result_t* result) {
+    NvtxRange total_range("total_compute_expmv");
     int rc = check_params(ctx, p);
     if (rc) return rc;
     if (p->precision == MEXK_PREC_MIXED && (rc = ensure_mixed(ctx))) return rc;
@@ -471,20 +534,26 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
         MEXK_CK(cudaMemsetAsync(ctx->d_y, 0, sizeof(double) * ctx->n, s));
     } else {
         const int grid = gs_grid_size(ctx->n, 1);
-        if (p->precision == MEXK_PREC_MIXED)
-            rc = launch_init_start<float>(ctx->n, ctx->ldv, v_dev, ctx->d_V32, ctx->d_partials, ctx->d_counter,
-                                          ctx->d_state, grid, s);
-        else
-            rc = launch_init_start<double>(ctx->n, ctx->ldv, v_dev, ctx->d_V, ctx->d_partials, ctx->d_counter,
-                                           ctx->d_state, grid, s);
+        {
+            NvtxRange init_range("init_q1");
+            if (p->precision == MEXK_PREC_MIXED)
+                rc = launch_init_start<float>(ctx->n, ctx->ldv, v_dev, ctx->d_V32, ctx->d_partials, ctx->d_counter,
+                                              ctx->d_state, grid, s);
+            else
+                rc = launch_init_start<double>(ctx->n, ctx->ldv, v_dev, ctx->d_V, ctx->d_partials, ctx->d_counter,
+                                               ctx->d_state, grid, s);
+        }
         if (rc) return rc;
         if (ctx->use_graph && s != ctx->stream) MEXK_CK(cudaStreamSynchronize(s));
-        // Every cycle ends with an accepted step or an abort, so the loop is
-        // bounded by max_steps; the extra margin only guards corrupt state.
-        const int max_cycles = ctx->h_state->max_steps + 2;
+        // Every cycle ends with an accepted step or an abort, or (adapt_m)
+        // with a larger basis requested after a reject, at most max_rejects
+        // times per step; the extra margin only guards corrupt state.
+        const long long per_step = 1 + (ctx->h_state->adapt_m ? ctx->h_state->max_rejects : 0);
+        const long long max_cycles = (static_cast<long long>(ctx->h_state->max_steps) + 2) * per_step;
         const int reortho = p->reorthogonalize ? 1 : 0;
         int m_cycle = p->m;
-        for (int cyc = 0; cyc < max_cycles; ++cyc) {
+        for (long long cyc = 0; cyc < max_cycles; ++cyc) {
+            NvtxRange cycle_range("arnoldi_step_attempt");
             if (ctx->use_graph) {
                 // Graphs are captured on the context stream and launched on `s`.
                 cudaGraphExec_t exec = nullptr;
@@ -498,6 +567,10 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
             MEXK_CK(cudaMemcpyAsync(ctx->h_state, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
             MEXK_CK(cudaStreamSynchronize(s));
             if (ctx->h_state->done) break;
+            if (ctx->h_state->status & ST_TIMEOUT) {
+                set_error_text("a device wait gave up (bulk copy did not complete)");
+                return MEXK_ERR_DEVICE;
+            }
             const int mn = ctx->h_state->m_next;
             if (mn >= 1 && mn <= ctx->m_alloc && mn < ctx->n) m_cycle = mn;
         }
@@ -593,6 +666,7 @@ int context_csr_finish(mexk_context_t ctx, const int* row_ptr) {
     const size_t hcount = static_cast<size_t>(ctx->ldh) * m_alloc_max;
     if ((rc = dalloc(&ctx->d_H, hcount))) return rc;
     MEXK_CK(cudaMemset(ctx->d_H, 0, sizeof(double) * hcount));
+    if (m_alloc_max > EXPM_SMEM_K && (rc = dalloc(&ctx->d_expm_ws, expm_ws_doubles(m_alloc_max)))) return rc;
     if ((rc = dalloc(&ctx->d_h1, MEXK_M_MAX + 2))) return rc;
     if ((rc = dalloc(&ctx->d_h2, MEXK_M_MAX + 2))) return rc;
     if ((rc = dalloc(&ctx->d_coef, MEXK_M_MAX + 2))) return rc;
@@ -745,6 +819,7 @@ int mexk_context_destroy(mexk_context_t ctx) {
     dfree(ctx->d_h2);
     dfree(ctx->d_coef);
     dfree(ctx->d_cand);
+    dfree(ctx->d_expm_ws);
     dfree(ctx->d_mlp);
     dfree(ctx->d_partials);
     dfree(ctx->d_gram);
@@ -828,7 +903,7 @@ int mexk_context_get_basis(mexk_context_t ctx, int precision, double* V_host, in
     MEXK_CK(cudaMemcpy2D(f.data(), sizeof(float) * n, ctx->d_V32, sizeof(float) * ctx->ldv, sizeof(float) * n,
                          ncols, cudaMemcpyDeviceToHost));
     // Stored columns are the basis vectors up to their scales.
-    std::vector<double> sc(MEXK_M_MAX + 2);
+    std::vector<double> sc(GRAM_M + 2);
     MEXK_CK(cudaMemcpy(sc.data(), reinterpret_cast<const char*>(ctx->d_gram) + offsetof(GramState, s),
                        sizeof(double) * sc.size(), cudaMemcpyDeviceToHost));
     for (int c = 0; c < ncols; ++c)
@@ -1022,6 +1097,10 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
     run.m = j + 1;
     run.max_steps = 1 << 30;
     run.max_rejects = 20;
+    run.safety = 0.8;
+    run.grow = 1.5;
+    run.shrink = 0.5;
+    run.m_base = j + 1;
     run.k_used = j + 1;
     run.k_lift = j + 1;
     run.lift = 1;

@@ -190,14 +190,21 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 // Bounded wait for the phase of `bar` with the given parity: false after
-// about a second (the copies did not complete).
-__device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// limit_ns (default about a second: the copies did not complete).
+__device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns = 1000000000ull) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = global_ns();
     while (!mbar_try_wait(bar, parity))
-        if (global_ns() - t0 > 1000000000ull) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     return true;
 }
+
+// Testing hook (mexk_test_force_wait_timeout): when set, block 0 of the
+// staged SpMV also waits, with a 1 ms limit, on an mbarrier that nothing
+// arrives at, so its bounded wait runs out and the timeout path (drain the
+// copies in flight, ST_TIMEOUT, MEXK_ERR_DEVICE) runs without any fault.
+__device__ int g_test_dead_wait = 0;
+constexpr unsigned long long TEST_DEAD_WAIT_NS = 1000000ull;
 
 // Shape of the context SpMV: threads per block, most nonzeros and rows per
 // row block, shared-memory buffers per block, resident blocks per SM the
@@ -364,6 +371,7 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
     static_assert(sizeof(TA) == sizeof(TP), "products overwrite the staged values");
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar[S];
+    __shared__ __align__(8) uint64_t dead_bar;  // the testing hook's barrier: never arrived at
     __shared__ TP red[32];
     __shared__ int s_long[ST_TILE / (SEQ_ROW_MAX + 1) + 1];
     __shared__ int s_nlong;
@@ -415,6 +423,7 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
     if (tid == 0) {
         pol = l2_evict_first_policy();
         for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
+        mbar_init(&dead_bar, 1);
         mbar_init_fence();
         // The matrix is never written by a kernel: its first row blocks are
         // requested before waiting for the previous kernel of the stream.
@@ -431,6 +440,8 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
         const int sb = (i - t0) % S;
         bool ok = true;
         if (st_i) ok = mbar_wait(&bar[sb], (phase >> sb) & 1u);
+        if (i == t0 && g == 0 && tid == 0 && g_test_dead_wait != 0)
+            ok = mbar_wait(&dead_bar, 0u, TEST_DEAD_WAIT_NS) && ok;
         // also: every thread has finished row block i - 1
         if (__syncthreads_or(!ok)) {
             fail = true;
@@ -802,18 +813,41 @@ int launch_narrow_values(const double* src, float* dst, size_t count, cudaStream
 
 // A == A^T exactly: every entry (r, c, v) has an entry (c, r, v). One thread
 // per row scans, for each of its entries, row c for column r.
+// A == A^T exactly: every entry (r, c, v) has an entry (c, r, v). Row c is
+// searched by bisection (its columns ascending, as the loaders and stencil
+// generators give them); a row that bisection misses is scanned only when it
+// is short (<= 64 entries) -- a long unsorted row makes the check answer
+// "not symmetric" rather than cost a serial scan per entry. Threads stop once
+// any of them found an asymmetry.
 __global__ void symmetric_check_kernel(int n, const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
                                        const double* __restrict__ values, int* __restrict__ ok) {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    for (long long rr = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; rr < n;
+         rr += static_cast<long long>(gridDim.x) * blockDim.x) {
+        if (*reinterpret_cast<volatile int*>(ok) == 0) return;
+        const int r = static_cast<int>(rr);
         for (int e = row_ptr[r]; e < row_ptr[r + 1]; ++e) {
             const int c = col_idx[e];
             const double v = values[e];
+            const int f0 = row_ptr[c], f1 = row_ptr[c + 1];
+            int lo = f0, hi = f1;  // first position with col_idx >= r
+            while (lo < hi) {
+                const int mid = lo + (hi - lo) / 2;
+                if (col_idx[mid] < r) lo = mid + 1;
+                else hi = mid;
+            }
             bool found = false;
-            for (int f = row_ptr[c]; f < row_ptr[c + 1]; ++f)
-                if (col_idx[f] == r && values[f] == v) {
+            for (int f = lo; f < f1 && col_idx[f] == r; ++f)
+                if (values[f] == v) {
                     found = true;
                     break;
                 }
+            if (!found && f1 - f0 <= 64) {
+                for (int f = f0; f < f1; ++f)
+                    if (col_idx[f] == r && values[f] == v) {
+                        found = true;
+                        break;
+                    }
+            }
             if (!found) {
                 atomicAnd(ok, 0);
                 return;
@@ -879,4 +913,15 @@ extern "C" int mexk_spmv_f64(int rows, const int* row_ptr, const int* col_idx, c
 extern "C" int mexk_spmv_f32(int rows, const int* row_ptr, const int* col_idx, const float* values,
                              const float* x, float* y, void* stream) {
     return mexk::spmv_standalone<float, float>(rows, row_ptr, col_idx, values, x, y, stream);
+}
+
+extern "C" int mexk_test_force_wait_timeout(int device, int enable) {
+    int count = 0;
+    MEXK_CK(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(device));
+    const int v = enable ? 1 : 0;
+    MEXK_CK(cudaMemcpyToSymbol(mexk::g_test_dead_wait, &v, sizeof(int)));
+    MEXK_CK(cudaDeviceSynchronize());
+    return MEXK_OK;
 }

@@ -67,7 +67,7 @@ void DeviceContext::alloc_from(const CSRHost& part, int global_cols, int m_alloc
     local_nnz = static_cast<int>(part.nnz);
     std::cout << "GPU " << device_id << " allocating: local_rows=" << local_rows << ", local_nnz=" << local_nnz
               << std::endl;
-    allocated_m_max = std::max(1, std::min(m_alloc_max, MEXK_M_MAX));
+    allocated_m_max = std::max(1, m_alloc_max);
     int rc = mexk_context_upload_csr(handle, part.rows, part.nnz, part.row_ptr.data(), part.col_idx.data(),
                                      part.values.data(), allocated_m_max);
     if (rc != MEXK_OK) die("mexk_context_upload_csr", rc);
@@ -123,6 +123,14 @@ void check_runner_shape(const ArnoldiParams& params, int global_rows, int global
     }
 }
 
+// Krylov dimension the device allocation must hold (main.cu:1343).
+int alloc_dimension(const ArnoldiParams& params, const TimeSteppingParams& ts, int global_rows) {
+    int m = std::max(params.m, ts.m_max > 0 ? ts.m_max : params.m);
+    // the basis needs m < n; a larger m_max is refused when a solve asks for it
+    m = std::min(m, std::max(params.m, global_rows - 1));
+    return std::min(m, MEXK_M_MAX);
+}
+
 }  // namespace
 
 void ArnoldiRunner::init_from_context(mexk_context_t ctx, int device_id) {
@@ -132,7 +140,7 @@ void ArnoldiRunner::init_from_context(mexk_context_t ctx, int device_id) {
     dc.handle = ctx;
     dc.local_rows = global_rows;
     dc.local_nnz = static_cast<int>(global_nnz);
-    dc.allocated_m_max = std::max(params.m, ts_params.m_max > 0 ? ts_params.m_max : params.m);
+    dc.allocated_m_max = alloc_dimension(params, ts_params, global_rows);
     std::cout << "GPU " << dc.device_id << " allocating: local_rows=" << dc.local_rows
               << ", local_nnz=" << dc.local_nnz << std::endl;
 }
@@ -161,9 +169,12 @@ void ArnoldiRunner::init_all_devices(const std::vector<CSRHost>& partitions, con
     full.nnz = static_cast<long long>(full.col_idx.size());
     DeviceContext& dc = device_contexts[0];
     dc.device_id = device_ids.empty() ? 0 : device_ids[0];
+    if (partitions.size() > 1)
+        std::cerr << "[mexk] warning: " << partitions.size() << " row partitions are concatenated onto GPU "
+                  << dc.device_id << "; this build solves on one device" << std::endl;
     dc.init_handles();
     dc.create_streams();
-    const int alloc_m = std::max(params.m, ts_params.m_max > 0 ? ts_params.m_max : params.m);
+    const int alloc_m = alloc_dimension(params, ts_params, global_rows);
     dc.alloc_from(full, global_cols, alloc_m);
     dc.create_descriptors(full, global_cols, CSRHost::GhostMap(), 0, alloc_m);
 }
@@ -184,6 +195,27 @@ void ArnoldiRunner::compute_expmv(const std::vector<double>& v_host, std::vector
     p.precision = precision;
     p.controller = controller;
     p.ortho_window = ortho_window;
+    // The caller's time-stepping parameters, read on every solve as the
+    // reference's compute_expmv does (main.cu:1426, 1476-1516).
+    mexk_stepping_t ts;
+    ts.dt_init = ts_params.dt_init;
+    ts.dt_min = ts_params.dt_min;
+    ts.dt_max = ts_params.dt_max;
+    ts.tol_step = ts_params.tol_step;
+    ts.max_steps = ts_params.max_steps;
+    ts.max_rejects = ts_params.max_rejects;
+    ts.safety = ts_params.safety;
+    ts.grow = ts_params.grow;
+    ts.shrink = ts_params.shrink;
+    ts.adapt_m = ts_params.adapt_m ? 1 : 0;
+    ts.m_max = ts_params.m_max;
+    ts.m_step = ts_params.m_step;
+    p.stepping = &ts;
+    if (ts.adapt_m && ts.m_step > 0 && ts.m_max > params.m && ts.m_max > dc.allocated_m_max) {
+        // main.cu:1441-1444
+        std::cerr << "ERROR: m_current exceeds allocated_m_max on GPU 0" << std::endl;
+        std::exit(EXIT_FAILURE);
+    }
     if (controller == MEXK_CTRL_LEARNED && !net_loaded) {
         const std::vector<float> w = load_controller_net();
         const int lrc = mexk_context_set_controller(dc.handle, w.data(), static_cast<int>(w.size()));
@@ -200,9 +232,14 @@ void ArnoldiRunner::compute_expmv(const std::vector<double>& v_host, std::vector
     last_steps.resize(static_cast<size_t>(count));
     if (count > 0) mexk_get_steps(dc.handle, last_steps.data(), count, &count);
     if (verbose) {
-        for (const mexk_step_t& s : last_steps)
+        for (const mexk_step_t& s : last_steps) {
+            if (log_h_columns)
+                for (int j = 0; j < s.m_used; ++j)
+                    std::cout << "    H_m column " << j << " stored. Current H_m size: " << (s.m_basis + 1) << "x"
+                              << s.m_basis << std::endl;
             std::cout << "[STEP] t=" << s.t_done << " dt=" << s.dt << " err=" << s.err << " m_used=" << s.m_used
                       << " accepts=" << s.accepts << " rejects=" << s.rejects << std::endl;
+        }
         // An abort (20 rejects) is the only way to finish unconverged at t_done = t.
         if (!converged && last_result.t_done >= params.t && params.t > 0)
             std::cerr << "[STEP] rejected too many times, aborting" << std::endl;

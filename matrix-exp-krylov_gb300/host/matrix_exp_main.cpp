@@ -7,7 +7,8 @@
 // reference's arithmetic), --controller reference|search|learned (default
 // the reference's heuristic), --window W (mixed precision, symmetric A:
 // orthogonalise against the last W basis vectors), --quiet (no
-// [STEP]/[FLOPs] lines) and --host-load. A .bincsr input is loaded straight
+// [STEP]/[FLOPs] lines), --verbose-h (the reference's per-step
+// "H_m column j stored" lines, main.cu:1951) and --host-load. A .bincsr input is loaded straight
 // into the device context (mexk_context_load_bincsr: mapped, streamed,
 // checked on the device) with the host loader's output and messages;
 // --host-load, symmetric_upper files and non-square matrices take the host
@@ -53,6 +54,7 @@ int main(int argc, char* argv[]) {
     int controller = MEXK_CTRL_REFERENCE;
     int window = 0;
     bool quiet = false;
+    bool verbose_h = false;
     bool host_load = false;
 
     std::vector<std::string> args(argv + 1, argv + argc);
@@ -98,6 +100,10 @@ int main(int argc, char* argv[]) {
         }
         if (a == "--quiet") {
             quiet = true;
+            continue;
+        }
+        if (a == "--verbose-h") {
+            verbose_h = true;
             continue;
         }
         if (a == "--host-load") {
@@ -236,6 +242,7 @@ int main(int argc, char* argv[]) {
     runner.controller = controller;
     runner.ortho_window = window;
     runner.verbose = !quiet;
+    runner.log_h_columns = verbose_h;
     if (loaded_ctx)
         runner.init_from_context(loaded_ctx, 0);
     else

@@ -20,7 +20,8 @@ HEADER = os.path.join(ROOT, "include", "mexk.h")
 MEXK_OK = 0
 PREC_FP64 = 0
 PREC_MIXED = 1
-M_MAX = 64
+M_MAX = 128
+M_MAX_MIXED = 64
 CTRL_REFERENCE = 0
 CTRL_SEARCH = 1
 CTRL_LEARNED = 2
@@ -30,10 +31,25 @@ class MexkError(RuntimeError):
     pass
 
 
+class Stepping(C.Structure):
+    """mexk_stepping_t: the reference's TimeSteppingParams (main.cu:1237-1250)."""
+    _fields_ = [("dt_init", C.c_double), ("dt_min", C.c_double), ("dt_max", C.c_double), ("tol_step", C.c_double),
+                ("max_steps", C.c_int), ("max_rejects", C.c_int), ("safety", C.c_double), ("grow", C.c_double),
+                ("shrink", C.c_double), ("adapt_m", C.c_int), ("m_max", C.c_int), ("m_step", C.c_int)]
+
+
+def default_stepping(m, t, tol, max_restarts) -> dict:
+    """TimeSteppingParams as the reference's ArnoldiRunner constructor derives
+    them from ArnoldiParams (main.cu:1292-1305)."""
+    return dict(dt_init=t / (max_restarts if max_restarts > 0 else 1), dt_min=max(1e-12, t * 1e-6), dt_max=t,
+                tol_step=tol, max_steps=max_restarts if max_restarts > 0 else 1000, max_rejects=20, safety=0.8,
+                grow=1.5, shrink=0.5, adapt_m=0, m_max=m, m_step=0)
+
+
 class Params(C.Structure):
     _fields_ = [("m", C.c_int), ("t", C.c_double), ("tol", C.c_double), ("max_restarts", C.c_int),
                 ("reorthogonalize", C.c_int), ("precision", C.c_int), ("controller", C.c_int),
-                ("ortho_window", C.c_int)]
+                ("ortho_window", C.c_int), ("stepping", C.POINTER(Stepping))]
 
 
 class Result(C.Structure):
@@ -47,7 +63,7 @@ class Result(C.Structure):
 
 class Step(C.Structure):
     _fields_ = [("t_done", C.c_double), ("dt", C.c_double), ("err", C.c_double), ("m_used", C.c_int),
-                ("accepts", C.c_int), ("rejects", C.c_int)]
+                ("accepts", C.c_int), ("rejects", C.c_int), ("m_basis", C.c_int)]
 
 
 class BincsrInfo(C.Structure):
@@ -120,6 +136,7 @@ _PROTOS = {
     "mexk_mlp_adam_step": ([_VP, _VP, _VP, _VP, _VP, C.c_int, C.c_int, C.c_float, _VP, _VP, _VP], C.c_int),
     "mexk_controller_predict": ([_VP, _VP, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_double, _VP, _VP], C.c_int),
+    "mexk_test_force_wait_timeout": ([C.c_int, C.c_int], C.c_int),
     "mexk_bincsr_probe": ([C.c_char_p, C.POINTER(BincsrInfo)], C.c_int),
     "mexk_context_load_bincsr": ([_VP, C.c_char_p, C.c_int, C.POINTER(BincsrInfo)], C.c_int),
 }

@@ -13,7 +13,8 @@ import os
 
 import numpy as np
 
-from ._lib import PREC_FP64, PREC_MIXED, M_MAX, Params, Result, Step, check, lib
+from ._lib import (M_MAX, M_MAX_MIXED, PREC_FP64, PREC_MIXED, Params, Result, Step, Stepping, check,
+                   default_stepping, lib)
 
 PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
 
@@ -26,13 +27,27 @@ CONTROLLERS = {"reference": 0, "search": 1, "learned": 2}
 
 
 def params(m, t, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64",
-           controller="reference", window=0) -> Params:
+           controller="reference", window=0, stepping=None) -> Params:
     """window: 0 = orthogonalise against the whole basis (Arnoldi); W >= 2 =
-    against the last W vectors (mixed precision, symmetric A only)."""
+    against the last W vectors (mixed precision, symmetric A only).
+    stepping: None (TimeSteppingParams derived from m, t, tol, max_restarts as
+    the reference's constructor does) or a dict overriding some of them
+    (dt_init, dt_min, dt_max, tol_step, max_steps, max_rejects, safety, grow,
+    shrink, adapt_m, m_max, m_step)."""
     prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     ctrl = CONTROLLERS[controller] if isinstance(controller, str) else int(controller)
-    return Params(int(m), float(t), float(tol), int(max_restarts), int(bool(reorthogonalize)), prec, ctrl,
-                  int(window))
+    p = Params(int(m), float(t), float(tol), int(max_restarts), int(bool(reorthogonalize)), prec, ctrl,
+               int(window), None)
+    if stepping is not None:
+        ts = default_stepping(int(m), float(t), float(tol), int(max_restarts))
+        unknown = set(stepping) - set(ts)
+        if unknown:
+            raise ValueError(f"unknown time-stepping parameters {sorted(unknown)}")
+        ts.update(stepping)
+        ints = {f for f, ct in Stepping._fields_ if ct is C.c_int}
+        p._stepping = Stepping(**{k: int(v) if k in ints else float(v) for k, v in ts.items()})  # kept alive with p
+        p.stepping = C.pointer(p._stepping)
+    return p
 
 
 class Context:
@@ -116,23 +131,23 @@ class Context:
             self.load_controller()
 
     def expmv(self, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, precision="fp64",
-              controller="reference", window=0):
+              controller="reference", window=0, stepping=None):
         """y = exp(t A) v with host vectors. Returns (y, result dict)."""
         self._ensure_net(controller)
         v = np.ascontiguousarray(v, dtype=np.float64)
         if v.shape != (self.n,):
             raise ValueError("v must have length n")
         y = np.zeros(self.n)
-        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller, window)
+        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller, window, stepping)
         r = Result()
         check(lib().mexk_expmv(self._h, C.byref(p), _ptr(v, C.c_double), _ptr(y, C.c_double), C.byref(r)),
               "mexk_expmv")
         return y, r.as_dict()
 
     def expmv_device(self, v_ptr: int, y_ptr: int, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True,
-                     precision="fp64", stream: int = 0, controller="reference", window=0):
+                     precision="fp64", stream: int = 0, controller="reference", window=0, stepping=None):
         self._ensure_net(controller)
-        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller, window)
+        p = params(m, t, tol, max_restarts, reorthogonalize, precision, controller, window, stepping)
         r = Result()
         check(lib().mexk_expmv_device(self._h, C.byref(p), C.c_void_p(v_ptr), C.c_void_p(y_ptr),
                                       C.c_void_p(stream), C.byref(r)), "mexk_expmv_device")
@@ -199,4 +214,4 @@ def device_count() -> int:
     return c.value
 
 
-__all__ = ["Context", "params", "device_count", "PRECISIONS", "M_MAX"]
+__all__ = ["Context", "params", "device_count", "PRECISIONS", "M_MAX", "M_MAX_MIXED"]

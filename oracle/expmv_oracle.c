@@ -119,16 +119,33 @@ int oracle_expmv(int n, const int* row_ptr, const int* col_idx, const double* va
                  const double* v, double* y_out, const oracle_params* p, oracle_stats* stats,
                  oracle_step* log, int log_cap, int* log_len) {
     if (n <= 0 || !p || p->m <= 0) return -1;
-    const int m = p->m;
-    /* ArnoldiRunnerCPU constructor, main_cpu.cpp:455-474 */
-    const double dt_max = p->t;
-    const double dt_min = (1e-12 > p->t * 1e-6) ? 1e-12 : p->t * 1e-6;
-    const double denom = (p->max_restarts > 0) ? p->max_restarts : 1;
-    const double dt_init = p->t / denom;
-    const double tol_step = p->tol;
-    const int max_steps = (p->max_restarts > 0) ? p->max_restarts : 1000;
-    const int max_rejects = 20;
-    const double safety = 0.8, grow = 1.5, shrink = 0.5;
+    const int m_base = p->m;
+    /* ArnoldiRunnerCPU constructor, main_cpu.cpp:453-466, or the caller's
+     * TimeSteppingParams as compute_expmv reads them (main_cpu.cpp:608-676) */
+    oracle_stepping ts;
+    if (p->stepping) {
+        ts = *p->stepping;
+    } else {
+        ts.dt_max = p->t;
+        ts.dt_min = (1e-12 > p->t * 1e-6) ? 1e-12 : p->t * 1e-6;
+        const double denom = (p->max_restarts > 0) ? p->max_restarts : 1;
+        ts.dt_init = p->t / denom;
+        ts.tol_step = p->tol;
+        ts.max_steps = (p->max_restarts > 0) ? p->max_restarts : 1000;
+        ts.max_rejects = 20;
+        ts.safety = 0.8;
+        ts.grow = 1.5;
+        ts.shrink = 0.5;
+        ts.adapt_m = 0;
+        ts.m_max = p->m;
+        ts.m_step = 0;
+    }
+    const double dt_max = ts.dt_max, dt_min = ts.dt_min, dt_init = ts.dt_init, tol_step = ts.tol_step;
+    const int max_steps = ts.max_steps, max_rejects = ts.max_rejects;
+    const double safety = ts.safety, grow = ts.grow, shrink = ts.shrink;
+    /* storage for the largest basis adapt_m may build (the GPU runner
+     * allocates max(m, m_max), main.cu:1343) */
+    const int m = (ts.adapt_m && ts.m_max > m_base) ? ts.m_max : m_base;
 
     size_t ldh = (size_t)m + 1;
     double* V = (double*)calloc((size_t)n * (size_t)(m + 1), sizeof(double));
@@ -160,12 +177,13 @@ int oracle_expmv(int n, const int* row_ptr, const int* col_idx, const double* va
     while (t_done < total_t && accepted < max_steps && !stop) {
         dt = (dt < total_t - t_done) ? dt : (total_t - t_done);
         int rejects = 0;
+        int m_current = m_base;
         while (1) {
             if (p->max_cycles > 0 && st.cycles >= p->max_cycles) { stop = 1; break; }
             memset(H, 0, sizeof(double) * ldh * (size_t)m);
             int k_used = 0;
             int breakdown = 0;
-            for (int j = 0; j < m; ++j) {
+            for (int j = 0; j < m_current; ++j) {
                 double beta = 0.0;
                 int ok = oracle_arnoldi_step(n, row_ptr, col_idx, values, V, j, p->reorthogonalize,
                                              w, hcol, &beta);
@@ -210,8 +228,13 @@ int oracle_expmv(int n, const int* row_ptr, const int* col_idx, const double* va
                     t_done = total_t;
                     break;
                 }
-                double dt_new = dt * shrink * safety;
-                dt = dt_new > dt_min ? dt_new : dt_min;
+                if (ts.adapt_m && (m_current + ts.m_step) <= ts.m_max && ts.m_step > 0) {
+                    m_current += ts.m_step;
+                } else {
+                    double dt_new = dt * shrink * safety;
+                    dt = dt_new > dt_min ? dt_new : dt_min;
+                    m_current = m_base;
+                }
                 continue;
             }
         }

@@ -16,6 +16,14 @@
 extern "C" {
 #endif
 
+/* TimeSteppingParams (main_cpu.cpp:417-430) as a caller may set them. */
+typedef struct {
+    double dt_init, dt_min, dt_max, tol_step;
+    int max_steps, max_rejects;
+    double safety, grow, shrink;
+    int adapt_m, m_max, m_step;
+} oracle_stepping;
+
 typedef struct {
     int m;               /* Krylov dimension (ArnoldiParams::m) */
     double t;            /* total time (ArnoldiParams::t) */
@@ -25,6 +33,8 @@ typedef struct {
     int max_cycles;      /* 0: unlimited. >0: stop after this many Arnoldi
                             basis builds (bounded timing samples only) */
     int quiet;           /* 0: print the reference's [STEP] lines to stdout */
+    const oracle_stepping* stepping; /* NULL: derived from m, t, tol, max_restarts
+                            as the constructor does (main_cpu.cpp:453-466) */
 } oracle_params;
 
 typedef struct {

@@ -23,9 +23,31 @@ _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int)
 
 
+class Stepping(C.Structure):
+    """TimeSteppingParams (main_cpu.cpp:417-430)."""
+    _fields_ = [("dt_init", C.c_double), ("dt_min", C.c_double), ("dt_max", C.c_double), ("tol_step", C.c_double),
+                ("max_steps", C.c_int), ("max_rejects", C.c_int), ("safety", C.c_double), ("grow", C.c_double),
+                ("shrink", C.c_double), ("adapt_m", C.c_int), ("m_max", C.c_int), ("m_step", C.c_int)]
+
+
+def stepping_defaults(m, t, tol, max_restarts) -> dict:
+    """The constructor's derivation (main_cpu.cpp:453-466)."""
+    return dict(dt_init=t / (max_restarts if max_restarts > 0 else 1), dt_min=max(1e-12, t * 1e-6), dt_max=t,
+                tol_step=tol, max_steps=max_restarts if max_restarts > 0 else 1000, max_rejects=20, safety=0.8,
+                grow=1.5, shrink=0.5, adapt_m=0, m_max=m, m_step=0)
+
+
+def _stepping(m, t, tol, max_restarts, overrides):
+    ts = stepping_defaults(m, t, tol, max_restarts)
+    ts.update(overrides or {})
+    ints = {f for f, ct in Stepping._fields_ if ct is C.c_int}
+    return ts, Stepping(**{k: int(v) if k in ints else float(v) for k, v in ts.items()})
+
+
 class Params(C.Structure):
     _fields_ = [("m", C.c_int), ("t", C.c_double), ("tol", C.c_double), ("max_restarts", C.c_int),
-                ("reorthogonalize", C.c_int), ("max_cycles", C.c_int), ("quiet", C.c_int)]
+                ("reorthogonalize", C.c_int), ("max_cycles", C.c_int), ("quiet", C.c_int),
+                ("stepping", C.POINTER(Stepping))]
 
 
 class Stats(C.Structure):
@@ -39,12 +61,21 @@ class Step(C.Structure):
                 ("accepts", C.c_int), ("rejects", C.c_int)]
 
 
+def reference_dir() -> str:
+    """The reference source tree: $MEXK_REFERENCE_DIR, else a `reference`
+    directory beside the repository."""
+    return os.environ.get("MEXK_REFERENCE_DIR") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
+
+
 def build(with_reference: bool | None = None) -> None:
     """make -C oracle (and `ref` when the reference tree is present)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    ref_dir = os.environ.get("MEXK_REFERENCE_DIR", "/root/reference")
+    ref_dir = reference_dir()
+    have = os.path.exists(os.path.join(ref_dir, "main_cpu.cpp"))
+    if with_reference and not have:
+        raise FileNotFoundError(f"reference tree not found at {ref_dir} (set MEXK_REFERENCE_DIR)")
     if with_reference is None:
-        with_reference = os.path.exists(os.path.join(ref_dir, "main_cpu.cpp"))
+        with_reference = have
     if with_reference:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_dir}"], check=True)
 
@@ -83,6 +114,8 @@ def ref():
         R = C.CDLL(REF_PATH)
         R.ref_expmv.argtypes = [C.c_int, C.c_longlong, _IP, _IP, _DP, _DP, _DP, C.c_int, C.c_double,
                                 C.c_double, C.c_int, C.c_int, _IP, _IP, _DP]
+        R.ref_expmv_ts.argtypes = [C.c_int, C.c_longlong, _IP, _IP, _DP, _DP, _DP, C.c_int, C.c_double,
+                                   C.c_double, C.c_int, C.c_int, _DP, _IP, _IP, _IP, _DP]
         R.ref_load.argtypes = [C.c_char_p, C.c_int, _IP, _IP, C.POINTER(C.c_longlong)]
         R.ref_load.restype = C.c_void_p
         R.ref_copy_csr.argtypes = [C.c_void_p, _IP, _IP, _DP]
@@ -102,12 +135,16 @@ def _csr(A):
     return rp, ci, va
 
 
-def expmv(A, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, max_cycles=0, log_cap=4096):
-    """Oracle y = exp(tA)v; returns (y, stats dict, list of step tuples)."""
+def expmv(A, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, max_cycles=0, log_cap=4096, stepping=None):
+    """Oracle y = exp(tA)v; returns (y, stats dict, list of step tuples).
+    stepping: a dict of TimeSteppingParams overrides (None: the defaults)."""
     rp, ci, va = _csr(A)
     v = np.ascontiguousarray(v, dtype=np.float64)
     y = np.zeros(A.n)
-    p = Params(m, t, tol, max_restarts, int(reorthogonalize), max_cycles, 1)
+    p = Params(m, t, tol, max_restarts, int(reorthogonalize), max_cycles, 1, None)
+    if stepping is not None:
+        _, ts = _stepping(m, t, tol, max_restarts, stepping)
+        p.stepping = C.pointer(ts)
     st = Stats()
     log = (Step * log_cap)()
     nlog = C.c_int(0)
@@ -171,9 +208,10 @@ def lift(V, k, wH, v_norm):
     return y
 
 
-def reference_expmv(A, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, capture=True):
+def reference_expmv(A, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, capture=True, stepping=None):
     """The reference's own ArnoldiRunnerCPU (built from main_cpu.cpp). Returns
-    (y, stats dict, [STEP] lines)."""
+    (y, stats dict, [STEP] lines). stepping: TimeSteppingParams overrides set
+    on the runner before compute_expmv."""
     rp, ci, va = _csr(A)
     v = np.ascontiguousarray(v, dtype=np.float64)
     y = np.zeros(A.n)
@@ -187,9 +225,20 @@ def reference_expmv(A, v, t, m, tol=1e-6, max_restarts=0, reorthogonalize=True, 
         if capture:
             os.dup2(tmp.fileno(), 1)
         try:
-            ref().ref_expmv(A.n, A.nnz, _p(rp, C.c_int), _p(ci, C.c_int), _p(va, C.c_double),
-                            _p(v, C.c_double), _p(y, C.c_double), m, t, tol, max_restarts,
-                            int(reorthogonalize), C.byref(rd), C.byref(cv), C.byref(res))
+            if stepping is None:
+                ref().ref_expmv(A.n, A.nnz, _p(rp, C.c_int), _p(ci, C.c_int), _p(va, C.c_double),
+                                _p(v, C.c_double), _p(y, C.c_double), m, t, tol, max_restarts,
+                                int(reorthogonalize), C.byref(rd), C.byref(cv), C.byref(res))
+            else:
+                ts, _ = _stepping(m, t, tol, max_restarts, stepping)
+                tsd = np.array([ts[k] for k in ("dt_init", "dt_min", "dt_max", "tol_step", "safety", "grow",
+                                                "shrink")], dtype=np.float64)
+                tsi = np.array([ts[k] for k in ("max_steps", "max_rejects", "adapt_m", "m_max", "m_step")],
+                               dtype=np.int32)
+                ref().ref_expmv_ts(A.n, A.nnz, _p(rp, C.c_int), _p(ci, C.c_int), _p(va, C.c_double),
+                                   _p(v, C.c_double), _p(y, C.c_double), m, t, tol, max_restarts,
+                                   int(reorthogonalize), _p(tsd, C.c_double), _p(tsi, C.c_int), C.byref(rd),
+                                   C.byref(cv), C.byref(res))
         finally:
             if capture:
                 os.dup2(saved, 1)

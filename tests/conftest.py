@@ -45,17 +45,39 @@ def rebuild_matrix(name, desc):
         n = 90
         return S.CSR(n, np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32),
                      np.tile([-1.0, -2.0, -3.0], n // 3))
-    if desc == "laplacian_2d(32)":
-        return S.laplacian_2d(32)
-    if desc == "convection_diffusion_3d(8, 100)":
-        return S.convection_diffusion_3d(8, 100.0)
+    if desc.startswith("laplacian_2d("):
+        return S.laplacian_2d(int(desc[len("laplacian_2d("):-1]))
+    if desc.startswith("convection_diffusion_3d("):
+        N, pe = desc[len("convection_diffusion_3d("):-1].split(",")
+        return S.convection_diffusion_3d(int(N), float(pe))
+    if desc == "config0(n=2000, seed=0)":
+        return S.config0().A
+    if desc == "skew300":
+        B = S.random_diag_dominant(300, 3, seed=21).to_dense()
+        np.fill_diagonal(B, 0.0)
+        Ad = B - B.T
+        rows, cols = np.nonzero(Ad)
+        rp = np.zeros(301, dtype=np.int32)
+        np.cumsum(np.bincount(rows, minlength=300), out=rp[1:])
+        return S.CSR(300, rp, cols.astype(np.int32), Ad[rows, cols], "skew300")
+    if desc.startswith("diag_linspace("):
+        n, lo, hi = desc[len("diag_linspace("):-1].split(",")
+        n = int(n)
+        return S.CSR(n, np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32),
+                     np.linspace(float(lo), float(hi), n))
     raise KeyError(desc)
+
+
+def fixture_stepping(d):
+    """The TimeSteppingParams a fixture was made with (None: the defaults)."""
+    ts = {k[3:]: d[k].item() for k in d if k.startswith("ts_")}
+    return ts or None
 
 
 # Small fixtures with stored inputs; the full-size heat2048 record only holds
 # a decision sequence and a fingerprint of y.
 GOLDEN_NAMES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                      if not os.path.basename(p).startswith("heat2048"))
+                      if not os.path.basename(p).endswith("_reference.npz"))
 
 
 def format_step(s):

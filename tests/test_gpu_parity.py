@@ -3,19 +3,31 @@ reference's golden fixtures. Needs a GB300 and the built libmexk.so.
 
 Tolerances: the FP64 path must agree with the reference's FP64 output to a
 relative 2-norm error of 1e-12 and take the same accept/reject decisions;
-the mixed-precision path must stay within 1e-6 of FP64.
+every other form (mixed precision, the candidate-step controllers, the
+short-recurrence window) must stay within a relative 2-norm error of 1e-6
+of the reference's output.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_NAMES, load_golden
+from conftest import GOLDEN_NAMES, fixture_stepping, load_golden
 
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
 MIXED_TOL = 1e-6
+
+# Fixtures whose reference solve converged: the reference's y is within
+# 1e-8 (relative) of dense expm on every one of them, so a form that must
+# agree with it to 1e-6 is held to its own accuracy.
+CONVERGED = ["cfg0_random_n2000", "heat_N32", "powerlaw_n2048", "convdiff_N8_pe100", "diag_n1000_kat",
+             "rejects_skew_n300_t20_m8", "breakdown_j2_diag3", "breakdown_j0_2I", "decay_diag_n600",
+             "decay_convdiff16_pe100", "decay_convdiff16_pe1000", "decay_heat_N64"]
+# Symmetric ones (the short-recurrence window applies).
+SYMMETRIC = ["heat_N32", "decay_heat_N64", "decay_diag_n600", "breakdown_j2_diag3", "breakdown_j0_2I",
+             "diag_n1000_kat"]
 
 
 def rel(a, b):
@@ -190,8 +202,11 @@ def test_expmv_fp64_matches_reference(name):
 
     A, d = load_golden(name)
     m = int(d["m"])
-    with Context(A, m_alloc=m) as ctx:
-        y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), max_restarts=int(d["max_restarts"]))
+    ts = fixture_stepping(d)
+    m_alloc = max(m, int(ts["m_max"])) if ts else m
+    with Context(A, m_alloc=m_alloc) as ctx:
+        y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), max_restarts=int(d["max_restarts"]),
+                           stepping=ts)
         steps = ctx.steps()
     assert rel(y, d["y"]) <= FP64_TOL, rel(y, d["y"])
     assert res["restarts_done"] == int(d["restarts_done"])
@@ -202,14 +217,17 @@ def test_expmv_fp64_matches_reference(name):
         # m_used / accepts / rejects exact; t, dt and err to printed precision
         assert f"m_used={s[3]}" == r[4] and f"accepts={s[4]}" == r[5] and f"rejects={s[5]}" == r[6]
         assert f"dt={s[1]:g}" == r[2]
-        # err near the rounding floor differs in its last digits; the
-        # decisions (checked above) are what must match.
+        # The estimate h_{k+1,k} |e_k^T exp(dt H) e1| |v| is a product of the
+        # basis's smallest quantities: CGS2 on the device and the reference's
+        # MGS2 round its late columns differently, so on strongly decaying
+        # spectra it agrees to a few percent only; the decisions (checked
+        # above) and y are what must match.
         ref_err = float(r[3].split("=")[1])
-        assert abs(s[2] - ref_err) <= 1e-5 * abs(ref_err) + 1e-3 * float(d["tol"])
+        floor = 1e-3 * float(d["tol"]) + 1e-12 * np.linalg.norm(d["v"])
+        assert abs(s[2] - ref_err) <= 0.1 * abs(ref_err) + floor
 
 
-@pytest.mark.parametrize("name", ["cfg0_random_n2000", "heat_N32", "powerlaw_n2048", "convdiff_N8_pe100",
-                                  "diag_n1000_kat", "rejects_skew_n300_t20_m8"])
+@pytest.mark.parametrize("name", CONVERGED)
 def test_expmv_mixed_within_tolerance(name):
     from mexk.api import Context
 
@@ -263,7 +281,7 @@ def test_invalid_arguments_rejected():
         with pytest.raises(MexkError):
             ctx.expmv(np.ones(50), 1.0, 0)
     with pytest.raises(MexkError):
-        Context(S.random_diag_dominant(20, 3, seed=2), m_alloc=65)
+        Context(S.random_diag_dominant(20, 3, seed=2), m_alloc=129)
 
 
 # ------------------------------------------------------------------ full size
@@ -341,13 +359,46 @@ def test_heat2048_fp64_matches_reference_run():
     assert rel(y32, y) <= MIXED_TOL, rel(y32, y)
 
 
+def test_powerlaw_fp64_matches_reference_run():
+    """Config 2 at full size (n = 8,388,608, 121M nonzeros, m = 40) against
+    the reference's own run: the same accept/reject sequence and y to 1e-12
+    (norm, sum and entries at seeded positions); the mixed forms within 1e-6
+    of that FP64 result."""
+    import os
+
+    from conftest import GOLDEN
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    d = np.load(os.path.join(GOLDEN, "powerlaw_reference.npz"))
+    P = S.config2()
+    assert P.A.nnz == int(d["nnz"])
+    with Context(P.A, m_alloc=P.m) as ctx:
+        y, res = ctx.expmv(P.v, P.t, P.m)
+        steps = ctx.steps()
+        others = {f: ctx.expmv(P.v, P.t, P.m, precision="mixed", controller=f)[0] for f in ("reference", "search")}
+    ref_steps = [ln.split() for ln in d["step_lines"]]
+    assert len(steps) == len(ref_steps)
+    for s_, r in zip(steps, ref_steps):
+        assert f"m_used={s_[3]}" == r[4] and f"accepts={s_[4]}" == r[5] and f"rejects={s_[5]}" == r[6]
+        assert f"dt={s_[1]:g}" == r[2] and f"t={s_[0]:g}" == r[1]
+    assert res["restarts_done"] == int(d["restarts_done"]) and res["converged"] == int(d["converged"])
+    assert abs(np.linalg.norm(y) - float(d["y_norm"])) <= 1e-12 * float(d["y_norm"])
+    assert abs(y.sum() - float(d["y_sum"])) <= 1e-12 * np.abs(y).sum()
+    pos = d["positions"]
+    assert rel(y[pos], d["y_at"]) <= FP64_TOL and rel(y[:16], d["y_head"]) <= FP64_TOL
+    for f, y32 in others.items():
+        assert rel(y32, y) <= MIXED_TOL, (f, rel(y32, y))
+
+
 # ------------------------------------------------------------------ step controllers
-@pytest.mark.parametrize("name", ["cfg0_random_n2000", "heat_N32", "powerlaw_n2048", "convdiff_N8_pe100",
-                                  "diag_n1000_kat", "rejects_skew_n300_t20_m8", "breakdown_j2_diag3"])
+@pytest.mark.parametrize("name", CONVERGED)
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_search_controller_accuracy(name, precision):
-    """Candidate-step control: every accepted step passes the same residual
-    test, so the result stays within the tolerance of the reference's."""
+    """Candidate-step control: every accepted step passes the residual test
+    (mixed precision: within the FP32 resolution of the iterate while the
+    accepted errors stay within 5e-7 of its norm), so the result stays within
+    1e-6 (relative) of the reference's."""
     from mexk.api import Context
 
     A, d = load_golden(name)
@@ -356,9 +407,60 @@ def test_search_controller_accuracy(name, precision):
         y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), max_restarts=int(d["max_restarts"]),
                            precision=precision, controller="search")
     assert res["converged"] == 1
-    diff = np.linalg.norm(y - d["y"])
-    bound = max(MIXED_TOL * np.linalg.norm(d["y"]), (res["restarts_done"] + int(d["restarts_done"])) * float(d["tol"]))
-    assert diff <= bound, (diff, bound)
+    assert rel(y, d["y"]) <= MIXED_TOL, rel(y, d["y"])
+
+
+@pytest.mark.parametrize("name", SYMMETRIC)
+@pytest.mark.parametrize("controller", ["search", "learned"])
+def test_headline_form_vs_reference_fixtures(name, controller):
+    """The benchmark's chosen form -- mixed precision, candidate-step
+    control, the short-recurrence window of 2 -- against the reference's own
+    output on symmetric problems, decaying ones included."""
+    from mexk.api import Context
+
+    A, d = load_golden(name)
+    m = int(d["m"])
+    with Context(A, m_alloc=m) as ctx:
+        y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), precision="mixed", controller=controller,
+                           window=2)
+    assert res["converged"] == 1
+    assert rel(y, d["y"]) <= MIXED_TOL, rel(y, d["y"])
+
+
+def test_underflowing_config4_time():
+    """Convection-diffusion at Pe = 1000 and t = 1, the config-4 time: the
+    exact solution underflows to zero; every form returns |y| within the
+    absolute tolerance, as the reference does (y = 0)."""
+    from mexk.api import Context
+
+    A, d = load_golden("convdiff16_pe1000_t1")
+    with Context(A, m_alloc=30) as ctx:
+        for prec, ctrl, w in (("fp64", "reference", 0), ("mixed", "search", 0), ("mixed", "learned", 0)):
+            y, res = ctx.expmv(d["v"], 1.0, 30, tol=float(d["tol"]), precision=prec, controller=ctrl, window=w)
+            assert res["converged"] == 1
+            assert np.linalg.norm(y) <= res["restarts_done"] * float(d["tol"]), (prec, ctrl, np.linalg.norm(y))
+
+
+def test_relaxed_tolerance_budget_holds():
+    """Mixed precision with candidate-step control accepts steps above tol
+    only while the accepted errors add up to at most 5e-7 of the iterate's
+    norm: on the skew problem (|y| = |v| = 17, 60+ reference steps at
+    tol 1e-6) the sum of accepted errors stays within tol per step plus
+    5e-7 |y|."""
+    from mexk.api import Context
+
+    A, d = load_golden("rejects_skew_n300_t20_m8")
+    tol = 1e-9
+    with Context(A, m_alloc=8) as ctx:
+        y, res = ctx.expmv(d["v"], 20.0, 8, tol=tol, precision="mixed", controller="search")
+        steps = ctx.steps()
+    # an attempt was accepted when the next one counts one more accept (the last one: the solve converged)
+    acc = [steps[i] for i in range(len(steps)) if i + 1 == len(steps) or steps[i + 1][4] == steps[i][4] + 1]
+    assert len(acc) == res["restarts_done"]
+    errs = sum(s[2] for s in acc)
+    ny = np.linalg.norm(d["v"])
+    assert errs <= len(acc) * tol + 5e-7 * ny * 1.0001, (errs, len(acc))
+    assert rel(y, d["y"]) <= MIXED_TOL
 
 
 def test_search_controller_takes_fewer_cycles():
@@ -559,3 +661,59 @@ def test_row_pattern_detection(case):
         assert np.array_equal(y_p, y_s) and r_p["attempts"] == r_s["attempts"]
         y_m, _ = ctx.expmv(v, 0.4, 20, precision="mixed")
         assert rel(y_m, y_s) <= 1e-6
+
+
+# ------------------------------------------------------------------ the C++ drop-in API
+def _runner_check(tmp_path):
+    """Compiles tests/cpp/runner_check.cpp against the public header and the
+    built host library (g++ is on both the build and the GPU machines)."""
+    import os
+    import subprocess
+
+    from conftest import ROOT
+    from mexk._lib import BUILD
+
+    exe = tmp_path / "runner_check"
+    src = os.path.join(ROOT, "tests", "cpp", "runner_check.cpp")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-o", str(exe), src,
+                    "-L", BUILD, f"-Wl,-rpath,{BUILD}", "-lmexk_host", "-lmexk"], check=True)
+    return str(exe)
+
+
+@pytest.mark.parametrize("name", ["m100_defaults_cfg0", "stepping_skew_n300", "adapt_m_skew_n300",
+                                  "stepping_cap_cfg0", "heat_N32"])
+def test_cpp_runner_matches_reference(tmp_path, name):
+    """A C++ program using ArnoldiParams (m = 100: the reference's default)
+    and an edited runner.ts_params prints the reference's [STEP] lines
+    verbatim and returns its y to 1e-12."""
+    import subprocess
+
+    from mexk.bincsr import write_bincsr
+
+    exe = _runner_check(tmp_path)
+    A, d = load_golden(name)
+    write_bincsr(tmp_path / "a.bincsr", A.row_ptr, A.col_idx, A.values)
+    np.ascontiguousarray(d["v"], dtype=np.float64).tofile(tmp_path / "v.bin")
+    args = [exe, str(tmp_path / "a.bincsr"), str(tmp_path / "v.bin"), str(tmp_path / "y.bin"), str(int(d["m"])),
+            repr(float(d["t"])), repr(float(d["tol"])), str(int(d["max_restarts"]))]
+    ts = fixture_stepping(d)
+    if ts:
+        args += [repr(float(ts[k])) for k in ("dt_init", "dt_min", "dt_max", "tol_step")]
+        args += [str(int(ts[k])) for k in ("max_steps", "max_rejects")]
+        args += [repr(float(ts[k])) for k in ("safety", "grow", "shrink")]
+        args += [str(int(ts[k])) for k in ("adapt_m", "m_max", "m_step")]
+    p = subprocess.run(args, capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr
+    lines = [ln.split() for ln in p.stdout.splitlines() if ln.startswith("[STEP]")]
+    ref_lines = [ln.split() for ln in d["step_lines"]]
+    assert len(lines) == len(ref_lines)
+    for s, r in zip(lines, ref_lines):
+        # t, dt, m_used, accepts, rejects verbatim; err to its printed digits
+        # (its last ones differ where the estimate sits at the rounding floor)
+        assert s[:3] + s[4:] == r[:3] + r[4:], (s, r)
+        e, re_ = float(s[3].split("=")[1]), float(r[3].split("=")[1])
+        floor = 1e-3 * float(d["tol"]) + 1e-12 * np.linalg.norm(d["v"])
+        assert abs(e - re_) <= 0.1 * abs(re_) + floor, (s, r)
+    y = np.fromfile(tmp_path / "y.bin", dtype=np.float64)
+    assert rel(y, d["y"]) <= FP64_TOL, rel(y, d["y"])
+    assert f"RESULT restarts_done={int(d['restarts_done'])} converged={int(d['converged'])}" in p.stdout

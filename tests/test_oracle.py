@@ -5,14 +5,14 @@ import numpy as np
 import pytest
 import scipy.linalg as sl
 
-from conftest import GOLDEN_NAMES, format_step, load_golden
+from conftest import GOLDEN_NAMES, fixture_stepping, format_step, load_golden
 
 
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
 def test_oracle_matches_reference_fixture(oracle_mod, name):
     A, d = load_golden(name)
     y, st, steps = oracle_mod.expmv(A, d["v"], float(d["t"]), int(d["m"]), tol=float(d["tol"]),
-                                    max_restarts=int(d["max_restarts"]))
+                                    max_restarts=int(d["max_restarts"]), stepping=fixture_stepping(d))
     # Same arithmetic as the reference build: bit-identical output.
     assert np.array_equal(y, d["y"]), np.abs(y - d["y"]).max()
     assert st["restarts_done"] == int(d["restarts_done"])
@@ -33,13 +33,32 @@ def test_diagonal_known_answer(oracle_mod):
 
 
 @pytest.mark.parametrize("name", ["cfg0_random_n2000", "powerlaw_n2048", "heat_N32", "convdiff_N8_pe100",
-                                  "rejects_skew_n300_t20_m8"])
+                                  "rejects_skew_n300_t20_m8", "m100_defaults_cfg0", "stepping_skew_n300",
+                                  "adapt_m_skew_n300", "decay_diag_n600", "decay_convdiff16_pe100",
+                                  "decay_convdiff16_pe1000", "decay_heat_N64"])
 def test_oracle_vs_dense_expm(oracle_mod, name):
     A, d = load_golden(name)
-    exact = sl.expm(float(d["t"]) * A.to_dense()) @ d["v"]
+    exact = dense_expmv(A, d)
     err = np.linalg.norm(d["y"] - exact) / np.linalg.norm(exact)
-    # The controller bounds the per-step residual estimate by tol (absolute).
+    # The controller bounds the per-step residual estimate by tol (absolute);
+    # the decaying fixtures use tol 1e-8, far below their |y|.
     assert err < 1e-6, err
+
+
+def dense_expmv(A, d):
+    if A.n == int(np.count_nonzero(np.diff(A.row_ptr))) and np.array_equal(A.col_idx, np.arange(A.n)):
+        return np.exp(float(d["t"]) * A.values) * d["v"]  # diagonal
+    return sl.expm(float(d["t"]) * A.to_dense()) @ d["v"]
+
+
+def test_underflowing_fixture_is_zero(oracle_mod):
+    """Convection-diffusion at Pe = 1000 and t = 1 (the config-4 time): every
+    mode decays below the double range, and the reference returns y = 0 to
+    within its absolute tolerance."""
+    A, d = load_golden("convdiff16_pe1000_t1")
+    assert np.linalg.norm(d["y"]) <= float(d["tol"])
+    y, st, _ = oracle_mod.expmv(A, d["v"], 1.0, 30, tol=float(d["tol"]))
+    assert np.array_equal(y, d["y"]) and st["converged"] == 1
 
 
 @pytest.mark.parametrize("scale", [1e-3, 0.05, 0.3, 1.0, 3.0, 30.0, 300.0])
@@ -106,6 +125,32 @@ def test_oracle_bitwise_vs_reference_build(oracle_mod, seed):
     mr = int(rng.integers(-1, 4))
     y1, st1, steps = oracle_mod.expmv(A, v, t, m, max_restarts=mr)
     y2, st2, lines = oracle_mod.reference_expmv(A, v, t, m, max_restarts=mr)
+    assert np.array_equal(y1, y2)
+    assert st1["restarts_done"] == st2["restarts_done"] and st1["converged"] == st2["converged"]
+    assert [format_step(s) for s in steps] == lines
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_oracle_stepping_bitwise_vs_reference_build(oracle_mod, seed):
+    """Caller-set TimeSteppingParams, adapt_m included: the restatement and
+    the reference's own program (ts_params set on its runner) agree bit for bit."""
+    if not oracle_mod.have_reference():
+        pytest.skip("reference build not present in this container")
+    from mexk import synthetic as S
+
+    rng = np.random.default_rng(2000 + seed)
+    n = int(rng.integers(60, 300))
+    A = S.random_diag_dominant(n, int(rng.integers(2, 8)), seed=seed + 50)
+    v = rng.standard_normal(n)
+    t = float(rng.uniform(0.5, 6.0))
+    m = int(rng.integers(3, 12))
+    ts = dict(dt_init=float(rng.uniform(0.05, 2.0)), dt_min=1e-5, dt_max=float(rng.uniform(0.5, 4.0)),
+              tol_step=float(10 ** rng.uniform(-10, -5)), safety=float(rng.uniform(0.6, 0.95)),
+              grow=float(rng.uniform(1.1, 3.0)), shrink=float(rng.uniform(0.2, 0.7)),
+              max_rejects=int(rng.integers(3, 25)), max_steps=int(rng.integers(2, 400)),
+              adapt_m=int(seed % 2), m_step=int(rng.integers(1, 5)), m_max=m + int(rng.integers(0, 12)))
+    y1, st1, steps = oracle_mod.expmv(A, v, t, m, tol=ts["tol_step"], stepping=ts)
+    y2, st2, lines = oracle_mod.reference_expmv(A, v, t, m, tol=ts["tol_step"], stepping=ts)
     assert np.array_equal(y1, y2)
     assert st1["restarts_done"] == st2["restarts_done"] and st1["converged"] == st2["converged"]
     assert [format_step(s) for s in steps] == lines
