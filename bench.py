@@ -159,6 +159,11 @@ def kernel_bytes(kind, n, nnz, k, fp32, window=0, form="staged"):
         return n + 2 * n * s  # row ids, x once, y
     if form == "pattern" and kind == "spmv_dots":  # a window of 2 takes u_{j-1}.w from the update: no u_{j-1}
         return n + (2 if window == 2 else 3) * n * s
+    if kind == "lanczos_cycle":
+        # steps 1..k-1 of a window-2 basis in one launch: the row ids once, and
+        # per step u_j (gathered once), u_{j-1} read and u_{j+1} written; w stays
+        # on chip
+        return n + (k - 1) * 3 * n * s
     if kind == "spmv":
         return nnz * (s + 4) + 4 * (n + 1) + 2 * n * s  # values+cols, row_ptr, x once, y
     if kind == "spmv_dots":  # the SpMV, then u_{j-1} read for the dots (u_j is x)
@@ -187,11 +192,14 @@ STEP_KINDS = {"fp64": ["spmv", "gs_dot", "gs_upd_dot", "gs_upd_norm", "normalize
               "mixed": ["spmv", "gram_dot", "gram_update"]}
 
 
-def step_kinds(precision, j, window=0, dots_in_spmv=True):
+def step_kinds(precision, j, window=0, dots_in_spmv=True, fused=False):
     """Kernels of Arnoldi step j as a solve runs them: in mixed precision with
     the staged or the pattern SpMV a step j >= 1 over two columns (every step
     of a window of 2, step 1 of full Arnoldi) takes its dot products from the
-    SpMV (spmv_dots) and needs no dot sweep."""
+    SpMV (spmv_dots) and needs no dot sweep; with the fused Lanczos form
+    (window 2) steps 1..m-1 are one launch, counted at step 1."""
+    if fused and precision == "mixed" and window == 2 and j >= 1:
+        return ["lanczos_cycle"] if j == 1 else []
     if precision == "mixed" and dots_in_spmv:
         lo = max(0, j + 1 - window) if window else 0
         if j >= 1 and j + 1 - lo <= 2:
@@ -228,16 +236,24 @@ def size_matched_copy(nbytes, stream, iters=20):
     return {"bytes": moved, "us": round(us, 2), "gbs": round(moved / (us / 1e6) / 1e9, 1)}
 
 
+def lanczos_fused(ctx, precision, window):
+    return precision == "mixed" and window == 2 and ctx.lanczos_form() == "fused"
+
+
 def profile_cycle(ctx, m, n, nnz, precision, iters=2, window=0):
     """CUDA-event timing of every kernel kind of one Krylov cycle (the sweeps
-    as the context's last solve ran them: with its window, if any)."""
+    as the context's last solve ran them: with its window, if any; a fused
+    Lanczos basis as its one launch for steps 1..m-1)."""
     fp32 = precision == "mixed"
     once = CYCLE_KINDS[precision]
     form = ctx.spmv_form(precision)
     dots_in_spmv = form != "direct"
+    fused = lanczos_fused(ctx, precision, window)
     per = {}
 
     def add(kind, j, k):
+        if kind == "lanczos_cycle":  # steps 1..m-1: basis size m
+            j, k = m - 1, m
         ms = ctx.profile_kernel(kind, j, iters, precision)
         p = per.setdefault(kind, {"ms": 0.0, "bytes": 0.0, "launches": 0})
         p["ms"] += ms
@@ -248,7 +264,7 @@ def profile_cycle(ctx, m, n, nnz, precision, iters=2, window=0):
     for kind in once:
         add(kind, m - 1, m)
     for j in range(m):
-        for kind in step_kinds(precision, j, window, dots_in_spmv):
+        for kind in step_kinds(precision, j, window, dots_in_spmv, fused):
             add(kind, j, j + 1)
     return per
 
@@ -263,7 +279,8 @@ def launches_per_solve(ctx, precision, res, m, window=0):
         sizes = [m] * res["cycles"]
     per_cycle = 4 if precision == "mixed" else 3
     dots_in_spmv = ctx.spmv_form(precision) != "direct"
-    return 2 + sum(sum(len(step_kinds(precision, j, window, dots_in_spmv)) for j in range(k)) + per_cycle
+    fused = lanczos_fused(ctx, precision, window)
+    return 2 + sum(sum(len(step_kinds(precision, j, window, dots_in_spmv, fused)) for j in range(k)) + per_cycle
                    for k in sizes)
 
 
@@ -664,20 +681,35 @@ def run_batch(args):
                       "gbs": round(batch_kernel_bytes(kind, rows, nnz, j + 1) / (ms / 1e3) / 1e9, 1)}
     b.close()
 
-    # serial plain FP64 on a size-stratified sample: accuracy and time per solve
+    # serial plain FP64 on a size-stratified subset (every RHS of args.sample
+    # problems): measured solve by solve, and the same subset as one batch
     order = np.argsort([P.A.n for P in probs])
     sample = sorted(set(int(order[int(i)]) for i in np.linspace(0, nprob - 1, min(args.sample, nprob)).round()))
-    pts, worst = [], 0.0
+    pts, worst, serial_s = [], 0.0, 0.0
     for i in sample:
         P = probs[i]
         with Context(P.A, m_alloc=30) as ctx:
             ctx.expmv(P.v[0], P.t, 30, precision="fp64")  # graph capture
-            for r in (0, P.v.shape[0] - 1):
+            for r in range(P.v.shape[0]):
                 ts = time.perf_counter()
                 y64, _ = ctx.expmv(P.v[r], P.t, 30, precision="fp64")
-                pts.append((P.A.n, time.perf_counter() - ts))
+                dt = time.perf_counter() - ts
+                serial_s += dt
+                pts.append((P.A.n, dt))
                 err = np.linalg.norm(ys[i][0][r] - y64) / max(np.linalg.norm(y64), 1e-300)
                 worst = max(worst, err)
+    sub_solves = len(pts)
+    with Batch(m=30, tol=1e-6, autotune=True) as bs:
+        for i in sample:
+            bs.add(probs[i].A, probs[i].v, probs[i].t)
+        bs.upload()
+        bs.run()  # autotune and graph capture
+        torch.cuda.synchronize()
+        ts = time.perf_counter()
+        for _ in range(3):
+            bs.run()
+        torch.cuda.synchronize()
+        batch_sub_s = (time.perf_counter() - ts) / 3
     nn = np.array([p[0] for p in pts], float)
     tt = np.array([p[1] for p in pts], float)
     slope, icept = np.polyfit(nn, tt, 1)
@@ -697,9 +729,16 @@ def run_batch(args):
                                 "spmm_unroll": info["spmm_unroll"], "tune_ms": round(info["tune_ms"], 1)},
                    "cycles_per_step": cycles, "generator": "torch Philox on the GPU, seeds 100+i",
                    "l2": "inputs far larger than L2 (bases > 100 GB); no flush"},
-        "serial_fp64": {"solves_per_s_estimated": serial_sps, "speedup": value / serial_sps,
-                        "sample": f"{len(pts)} plain-FP64 solves (2 RHS of {len(sample)} size-stratified problems), "
-                                  f"time per solve fitted as a + b*n and summed over all {nsolves} solves"},
+        "serial_fp64": {"measured_subset": {"problems": len(sample), "solves": sub_solves,
+                                            "serial_s": round(serial_s, 3), "batch_s": round(batch_sub_s, 4),
+                                            "serial_solves_per_s": sub_solves / serial_s,
+                                            "batch_solves_per_s": sub_solves / batch_sub_s,
+                                            "speedup": serial_s / batch_sub_s},
+                        "extrapolated_all": {"solves_per_s": serial_sps, "speedup": value / serial_sps,
+                                             "how": f"time per serial solve fitted as a + b*n on the subset and "
+                                                    f"summed over all {nsolves} solves"},
+                        "sample": f"every RHS of {len(sample)} size-stratified problems ({sub_solves} plain-FP64 "
+                                  f"solves, each timed), and the same problems as one batch"},
         "max_rel_err_vs_fp64_sample": worst,
         "setup": {"generate_s": round(t_gen, 2), "upload_s": round(t_up, 2)},
         "kernels_first_wave": kern,
@@ -960,7 +999,8 @@ def main():
     ap.add_argument("--workload", default="heat2048",
                     choices=["heat2048", "batch", "convdiff", "powerlaw", "load"])
     ap.add_argument("--problems", type=int, default=256, help="batch workload: number of problems")
-    ap.add_argument("--sample", type=int, default=8, help="batch workload: problems in the serial FP64 sample")
+    ap.add_argument("--sample", type=int, default=16,
+                    help="batch workload: problems (all their RHS) in the measured serial FP64 subset")
     ap.add_argument("--grid", type=int, default=2048, help="--solve-once: heat-equation grid size")
     ap.add_argument("--spmv-form", choices=["staged", "direct", "pattern"], default=None,
                     help="--solve-once: SpMV form to run instead of the context's choice")

@@ -367,7 +367,8 @@ int mexk_batch_destroy(mexk_batch_t b);
 #define MEXK_KERNEL_GRAM_UPDATE 8 /* mixed: streaming update into the next column */
 #define MEXK_KERNEL_GRAM_NORM 9   /* mixed: norm of the last column (once per basis) */
 #define MEXK_KERNEL_SPMV_DOTS 10  /* mixed, steps j >= 1 over two columns: SpMV + the step's dots and finish */
-#define MEXK_KERNEL_KINDS 11
+#define MEXK_KERNEL_LANCZOS_CYCLE 11 /* mixed, window 2, fused form: steps 1..j of a basis in one launch */
+#define MEXK_KERNEL_KINDS 12
 
 /* Times `iters` launches of one solver kernel for Arnoldi step j (k = j+1
  * basis columns) on the context stream with CUDA events, on the context's
@@ -407,14 +408,32 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
 int mexk_context_get_spmv_form(mexk_context_t ctx, int precision, int* form);
 int mexk_context_set_spmv_form(mexk_context_t ctx, int precision, int form);
 
+/* How a short-recurrence basis (ortho_window = 2, mixed precision, a
+ * symmetric matrix in the row-pattern SpMV form) runs its steps 1..m-1:
+ * MEXK_LANCZOS_FUSED as one cooperative launch in which one thread block
+ * per SM keeps its rows' ids and A u_j on chip and the blocks meet at two
+ * bounded grid barriers per step; MEXK_LANCZOS_STEPWISE (the default) as two
+ * launches per step (the SpMV with the step's dot products, the update).
+ * The fused form applies when every block's rows fit its shared memory
+ * (about 7 million rows on a 152-SM GB300); get reports the form a solve
+ * would run. Both compute the same row sums and updates and sum the dot
+ * products in different orders: solves agree to rounding. No reference
+ * counterpart. */
+#define MEXK_LANCZOS_STEPWISE 0
+#define MEXK_LANCZOS_FUSED 1
+int mexk_context_get_lanczos_form(mexk_context_t ctx, int* form);
+int mexk_context_set_lanczos_form(mexk_context_t ctx, int form);
+
 /* ---- testing hooks ------------------------------------------------------ */
 /* enable != 0: from now on, thread block 0 of the staged CSR SpMV also waits
  * (1 ms limit) on a barrier that nothing arrives at, so its bounded wait runs
- * out: it drains its bulk copies in flight, sets the timeout status bit, and
- * the solve returns MEXK_ERR_DEVICE while the context stays usable. enable = 0
+ * out: it drains its bulk copies in flight and sets the timeout status bit;
+ * and thread block 0 of the fused Lanczos cycle leaves before its first grid
+ * barrier, so the other blocks' bounded waits (1 s) run out. Either way the
+ * solve returns MEXK_ERR_DEVICE and the context stays usable. enable = 0
  * restores normal operation. For failure-path tests only: it changes no
- * result of a solve that does not use the staged form. No reference
- * counterpart (the reference has no bounded device waits). */
+ * result of a solve that uses neither form. No reference counterpart (the
+ * reference has no bounded device waits). */
 int mexk_test_force_wait_timeout(int device, int enable);
 
 #ifdef __cplusplus

@@ -70,26 +70,108 @@ __device__ __forceinline__ int step2_slot(int v, int kw, int lo) {
     return v < kw ? lo + v : (v < 2 * kw ? GRAM_BOFF + lo + (v - kw) : GRAM_NWOFF);
 }
 
+// The scalar chain of a step over at most two columns (kw = 1 or 2; lo =
+// j + 1 - kw) from its sums tot = {a (kw), b (kw), |w|^2}: s_j = 1/|u_j|,
+// H(j, j-1) = |u_j| / p_j with the breakdown test of main.cu:1911, the Gram
+// entry G(j-1, j), c = s s_j a, h = c - (G - I) c, the update coefficients
+// and the pre-scale p of the next column (one rsqrt, a few products, one
+// rsqrt). s0 = s_{lo} (kw = 2), ip_j = 1 / (pre-scale of column j).
+struct Step2Out {
+    double sj, beta, hp, hj, g01, p, ip;
+    bool bad;
+};
+__device__ __forceinline__ Step2Out step2_chain(const double* tot, int kw, int j, int reortho, double s0,
+                                                double ip_j) {
+    Step2Out o;
+    const double bj = tot[2 * kw - 1];
+    const double sj = (bj > 0.0 && !isinf(bj)) ? rsqrt(bj) : 0.0;
+    // H(j, j-1) and the breakdown test: the square root runs beside the
+    // chain below, whose results are used only once the test has passed
+    const double beta = j >= 1 ? sqrt(bj) * ip_j : 1.0;
+    o.bad = !(beta >= 1e-14) || isinf(beta);
+    const double sj2 = sj * sj;
+    const double cj = sj2 * tot[kw - 1];
+    double hj = cj, hp = 0.0, g01 = 0.0, part;
+    if (kw == 2) {
+        g01 = (s0 * tot[kw]) * sj;              // G(j-1, j)
+        const double cp = (s0 * tot[0]) * sj;  // c_{j-1}
+        hp = cp;
+        if (reortho) {
+            hp = cp - __dmul_rn(g01, cj);
+            hj = cj - __dmul_rn(g01, cp);
+        }
+        const double gh0 = fma(g01, hj, hp), gh1 = hj + __dmul_rn(g01, hp);
+        part = hp * (gh0 - 2.0 * cp) + hj * (gh1 - 2.0 * cj);
+    } else {
+        part = hj * (hj - 2.0 * cj);
+    }
+    const double w2 = sj2 * tot[2 * kw];
+    const double u2 = w2 + part;
+    double p = 1.0, ip = 1.0;
+    if (u2 > 1e-8 * w2 && !isinf(u2)) {
+        p = rsqrt(u2);
+        ip = u2 * p;
+    } else if (w2 > 0.0 && !isinf(w2)) {
+        p = rsqrt(w2);
+        ip = w2 * p;
+    }
+    o.sj = sj;
+    o.beta = beta;
+    o.hp = hp;
+    o.hj = hj;
+    o.g01 = g01;
+    o.p = p;
+    o.ip = ip;
+    return o;
+}
+
+// Writes a step's results (step2_chain) into H, the Gram state and the
+// solver state: H(j, j-1) (0 on breakdown, which also sets the breakdown
+// flag and writes nothing else), s_j, G(j, j) and G(j-1, j), H(lo:j, j),
+// the update coefficients, the next column's inverse pre-scale and the
+// update scales. One thread.
+__device__ __forceinline__ void step2_store(const GramArgs& g, int kw, const Step2Out& o, double s0) {
+    const int j = g.j;
+    const int lo = j + 1 - kw;
+    GramState* gs = g.gs;
+    double* G = gs->G;
+    const size_t ldh = static_cast<size_t>(g.ldh);
+    if (j >= 1) g.H[j + static_cast<size_t>(j - 1) * ldh] = o.bad ? 0.0 : o.beta;
+    if (j >= 1 && o.bad) {
+        g.st->breakdown = 1;
+        g.st->k_used = j;
+        return;
+    }
+    gs->s[j] = o.sj;
+    G[j + static_cast<size_t>(j) * GRAM_LD] = 1.0;
+    if (kw == 2) {
+        G[lo + static_cast<size_t>(j) * GRAM_LD] = o.g01;
+        G[j + static_cast<size_t>(lo) * GRAM_LD] = o.g01;
+        g.H[lo + static_cast<size_t>(j) * ldh] = o.hp;
+        gs->coef[lo] = static_cast<float>(s0 * o.hp);
+    }
+    g.H[j + static_cast<size_t>(j) * ldh] = o.hj;
+    gs->coef[j] = static_cast<float>(o.sj * o.hj);
+    gs->ip[j + 1] = o.ip;
+    gs->wsc = static_cast<float>(o.sj);
+    gs->psc = static_cast<float>(o.p);
+}
+
 // The finish of a step over at most two columns, in the last block of the
 // sweep that wrote the a and |w|^2 partials (over nrb_a row blocks; the b
 // partials over nrb_b row blocks, possibly written by the previous step's
-// update). After the sums one thread runs the whole chain: s_j = 1/|u_j|,
-// H(j, j-1) = |u_j| / p_j with the breakdown test of main.cu:1911, the Gram
-// entry G(j-1, j), c = s s_j a, h = c - (G - I) c, H(:, j), the update
-// coefficients and the pre-scale p of the next column (one rsqrt, a few
-// products, one rsqrt).
+// update): the partial sums, then one thread runs step2_chain and
+// step2_store.
 // PR: partials loaded per lane and round (20: one round for up to 640 row
 // blocks, where the caller's registers allow).
 template <int PR = 16>
 __device__ __forceinline__ void step2_finish(const GramArgs& g, int nrb_a, int nrb_b) {
-    DevState* st = g.st;
     const int j = g.j;
     const int lo = g.lo;
     const int kw = j + 1 - lo;
     __shared__ double s_tot[5];  // a (kw), b (kw), |w|^2
     const int t = threadIdx.x;
     GramState* gs = g.gs;
-    double* G = gs->G;
     const size_t ldh = static_cast<size_t>(g.ldh);
     for (int r = t; r < lo; r += blockDim.x) g.H[r + static_cast<size_t>(j) * ldh] = 0.0;  // outside the window
     const double s0 = kw == 2 ? gs->s[lo] : 0.0;
@@ -101,57 +183,8 @@ __device__ __forceinline__ void step2_finish(const GramArgs& g, int nrb_a, int n
         [&](int v) { return ((v >= kw && v < 2 * kw) || (v == 0 && a0_from_update)) ? nrb_b : nrb_a; }, s_tot);
     __syncthreads();
     if (t != 0) return;
-    const double bj = s_tot[2 * kw - 1];
-    const double sj = (bj > 0.0 && !isinf(bj)) ? rsqrt(bj) : 0.0;
-    // H(j, j-1) and the breakdown test: the square root runs beside the
-    // chain below, which writes nothing until the test has passed
-    const double beta = j >= 1 ? sqrt(bj) * ip_j : 1.0;
-    const bool bad = !(beta >= 1e-14) || isinf(beta);
-    const double sj2 = sj * sj;
-    const double cj = sj2 * s_tot[kw - 1];
-    double hj = cj, hp = 0.0, g01 = 0.0, part;
-    if (kw == 2) {
-        g01 = (s0 * s_tot[kw]) * sj;              // G(j-1, j)
-        const double cp = (s0 * s_tot[0]) * sj;  // c_{j-1}
-        hp = cp;
-        if (g.reortho) {
-            hp = cp - __dmul_rn(g01, cj);
-            hj = cj - __dmul_rn(g01, cp);
-        }
-        const double gh0 = fma(g01, hj, hp), gh1 = hj + __dmul_rn(g01, hp);
-        part = hp * (gh0 - 2.0 * cp) + hj * (gh1 - 2.0 * cj);
-    } else {
-        part = hj * (hj - 2.0 * cj);
-    }
-    const double w2 = sj2 * s_tot[2 * kw];
-    const double u2 = w2 + part;
-    double p = 1.0, ip = 1.0;
-    if (u2 > 1e-8 * w2 && !isinf(u2)) {
-        p = rsqrt(u2);
-        ip = u2 * p;
-    } else if (w2 > 0.0 && !isinf(w2)) {
-        p = rsqrt(w2);
-        ip = w2 * p;
-    }
-    if (j >= 1) g.H[j + static_cast<size_t>(j - 1) * ldh] = bad ? 0.0 : beta;
-    if (j >= 1 && bad) {
-        st->breakdown = 1;
-        st->k_used = j;
-        return;
-    }
-    gs->s[j] = sj;
-    G[j + static_cast<size_t>(j) * GRAM_LD] = 1.0;
-    if (kw == 2) {
-        G[lo + static_cast<size_t>(j) * GRAM_LD] = g01;
-        G[j + static_cast<size_t>(lo) * GRAM_LD] = g01;
-        g.H[lo + static_cast<size_t>(j) * ldh] = hp;
-        gs->coef[lo] = static_cast<float>(s0 * hp);
-    }
-    g.H[j + static_cast<size_t>(j) * ldh] = hj;
-    gs->coef[j] = static_cast<float>(sj * hj);
-    gs->ip[j + 1] = ip;
-    gs->wsc = static_cast<float>(sj);
-    gs->psc = static_cast<float>(p);
+    const Step2Out o = step2_chain(s_tot, kw, j, g.reortho, s0, ip_j);
+    step2_store(g, kw, o, s0);
 }
 
 }  // namespace

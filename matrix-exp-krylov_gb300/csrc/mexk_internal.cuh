@@ -388,7 +388,9 @@ int launch_normalize(int n, int j, int ldv, const TV* w, TV* V, const DevState* 
 // Column c of the FP32 basis stores u_c; the basis vector is v_c = s[c] * u_c.
 constexpr int GRAM_M = MEXK_M_MAX_MIXED;    // largest Krylov dimension of the FP32 basis
 constexpr int GRAM_LD = GRAM_M + 1;         // leading dimension of G
-constexpr int GRAM_SLOTS = 2 * GRAM_M + 8;  // partial slots: a [0,64), b [64,128), |w|^2 128
+// partial slots: a [0,64), b [64,128), |w|^2 128; the fused Lanczos cycle's
+// banks from 136 (lanczos_cycle.cu)
+constexpr int GRAM_SLOTS = 2 * GRAM_M + 8 + 10;
 constexpr int GRAM_BOFF = GRAM_M;
 constexpr int GRAM_NWOFF = 2 * GRAM_M;
 constexpr int GRAM_MAX_ROW_BLOCKS = 1024;
@@ -428,6 +430,33 @@ int launch_gram_update(const GramArgs& a, cudaStream_t s);
 int gram_update2_blocks(int n);
 // |u_{j+1}| -> H(j+1, j) and s[j+1] (the last step of a basis, or a single step).
 int launch_gram_norm(const GramArgs& a, cudaStream_t s);
+
+// Steps j0..m-1 of a Lanczos basis (window 2, symmetric A in the row-pattern
+// form, FP32 basis) in one cooperative launch (lanczos_cycle.cu): per step
+// the SpMV with its dot products, a grid barrier, the step's finish in every
+// block, the update, a grid barrier. Step j0's b and a_{j0-1} partials come
+// from the update of step j0-1 (over b_blocks row blocks). bar: three words
+// (arrival count, abort flag, generation), zero before the first launch;
+// the barriers leave them as they found them unless a wait gave up. Returns MEXK_ERR_UNSUPPORTED when the
+// matrix's row blocks do not fit the kernel's shared memory.
+struct LanczosArgs {
+    int n, j0, m, ldv, ldh, reortho;
+    int major, major_len, max_len, npat;
+    const uint8_t* pid;
+    const RowPatterns* T;
+    float* V;
+    double* H;
+    GramState* gs;
+    DevState* st;
+    double* part;
+    int b_blocks;
+    unsigned* bar;
+};
+bool lanczos_cycle_fits(int n);
+int lanczos_cycle_prepare();
+int launch_lanczos_cycle(const LanczosArgs& a, cudaStream_t s);
+// mexk_test_force_wait_timeout's part for the fused cycle (current device).
+int lanczos_cycle_test_hook(int enable);
 
 // ------------------------------------------------------------ expm / control
 // Raises the dynamic shared-memory limits of the expm kernels; call once

@@ -115,6 +115,8 @@ struct mexk_context_s {
     GramState* d_gram = nullptr;
     double* d_gram_part = nullptr;
     unsigned int* d_counter = nullptr;
+    unsigned int* d_bar = nullptr;  // the fused Lanczos cycle's grid-barrier words
+    bool lanczos_fused = false;     // window-2 pattern-form bases in one cooperative launch
     DevState* d_state = nullptr;
     DevState* h_state = nullptr;
     mexk_step_t* d_log = nullptr;
@@ -408,14 +410,51 @@ int enqueue_controller(mexk_context_t ctx, int m, int ctrl, mexk_step_t* log, cu
     return launch_controller_search(c, m, s);
 }
 
+// Whether a basis of m columns runs steps 1..m-1 as one cooperative launch
+// (window 2 on a symmetric matrix in the row-pattern form, FP32 basis).
+bool use_lanczos_cycle(mexk_context_t ctx, int m, bool fp32, int window) {
+    return fp32 && window == 2 && m >= 2 && ctx->lanczos_fused && ctx->spmv_form32 == MEXK_SPMV_PATTERN &&
+           lanczos_cycle_fits(ctx->n);
+}
+
+int enqueue_lanczos_cycle(mexk_context_t ctx, int m, int reortho, cudaStream_t s) {
+    LanczosArgs a;
+    a.n = ctx->n;
+    a.j0 = 1;
+    a.m = m;
+    a.ldv = ctx->ldv;
+    a.ldh = ctx->ldh;
+    a.reortho = reortho ? 1 : 0;
+    a.major = ctx->pat_major;
+    a.major_len = ctx->pat_major_len;
+    a.max_len = ctx->pat_max_len;
+    a.npat = 0;
+    a.pid = ctx->d_pid;
+    a.T = ctx->d_pat;
+    a.V = ctx->d_V32;
+    a.H = ctx->d_H;
+    a.gs = ctx->d_gram;
+    a.st = ctx->d_state;
+    a.part = ctx->d_gram_part;
+    a.b_blocks = gram_update2_blocks(ctx->n);
+    a.bar = ctx->d_bar;
+    return launch_lanczos_cycle(a, s);
+}
+
 // One Krylov cycle: the unit that is captured into a graph.
 template <typename TV>
 int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, cudaStream_t s) {
     const bool fp32 = sizeof(TV) == 4;
     TV* V = fp32 ? reinterpret_cast<TV*>(ctx->d_V32) : reinterpret_cast<TV*>(ctx->d_V);
     int rc;
-    for (int j = 0; j < m; ++j)
-        if ((rc = enqueue_step(ctx, j, reortho, fp32, s, window, m))) return rc;
+    if (use_lanczos_cycle(ctx, m, fp32, window)) {
+        // step 0 as two kernels (its update writes step 1's b and a_0 partials), then the rest in one launch
+        if ((rc = enqueue_step(ctx, 0, reortho, fp32, s, window, m))) return rc;
+        if ((rc = enqueue_lanczos_cycle(ctx, m, reortho, s))) return rc;
+    } else {
+        for (int j = 0; j < m; ++j)
+            if ((rc = enqueue_step(ctx, j, reortho, fp32, s, window, m))) return rc;
+    }
     if ((rc = finish_basis(ctx, m - 1, fp32, s))) return rc;
     if ((rc = enqueue_controller(ctx, m, ctrl, ctx->d_log, s))) return rc;
     const LiftArgs l = lift_args(ctx, fp32);
@@ -529,6 +568,7 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
     ctx->last_controller = p->controller;
     init_state(ctx->h_state, p, LOG_CAP);
     MEXK_CK(cudaMemcpyAsync(ctx->d_state, ctx->h_state, sizeof(DevState), cudaMemcpyHostToDevice, s));
+    MEXK_CK(cudaMemsetAsync(ctx->d_bar, 0, sizeof(unsigned int) * 4, s));
     if (ctx->h_state->done) {
         // The reference never lifts when no step runs: y stays zero (main_cpu.cpp:467).
         MEXK_CK(cudaMemsetAsync(ctx->d_y, 0, sizeof(double) * ctx->n, s));
@@ -674,6 +714,8 @@ int context_csr_finish(mexk_context_t ctx, const int* row_ptr) {
     if ((rc = dalloc(&ctx->d_partials, static_cast<size_t>(PARTIAL_BLOCKS) * RED_STRIDE))) return rc;
     if ((rc = dalloc(&ctx->d_counter, 4))) return rc;
     MEXK_CK(cudaMemset(ctx->d_counter, 0, sizeof(unsigned int) * 4));
+    if ((rc = dalloc(&ctx->d_bar, 4))) return rc;
+    MEXK_CK(cudaMemset(ctx->d_bar, 0, sizeof(unsigned int) * 4));
     if ((rc = dalloc(&ctx->d_state, 1))) return rc;
     if ((rc = dalloc(&ctx->d_log, LOG_CAP))) return rc;
     cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&ctx->h_state), sizeof(DevState));
@@ -755,6 +797,8 @@ int mexk_context_create(int device, mexk_context_t* out) {
         return MEXK_ERR_CUDA;
     }
     int rc = expm_init_attributes();
+    // without its shared memory the fused Lanczos form stays off (lanczos_cycle_fits says no)
+    if (rc == MEXK_OK && lanczos_cycle_prepare() != MEXK_OK) (void)cudaGetLastError();
     gs_prepare();
     if (rc) {
         cudaStreamDestroy(c->stream);
@@ -825,6 +869,7 @@ int mexk_context_destroy(mexk_context_t ctx) {
     dfree(ctx->d_gram);
     dfree(ctx->d_gram_part);
     dfree(ctx->d_counter);
+    dfree(ctx->d_bar);
     dfree(ctx->d_state);
     dfree(ctx->d_log);
     if (ctx->h_state) cudaFreeHost(ctx->h_state);
@@ -1074,6 +1119,25 @@ int mexk_context_set_spmv_form(mexk_context_t ctx, int precision, int form) {
     return MEXK_OK;
 }
 
+int mexk_context_get_lanczos_form(mexk_context_t ctx, int* form) {
+    if (!ctx || !ctx->uploaded || !form) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    int rc;
+    if ((rc = ensure_mixed(ctx))) return rc;  // the mixed SpMV form is set there
+    const bool applies = ctx->d_pat != nullptr && lanczos_cycle_fits(ctx->n) && ctx->spmv_form32 == MEXK_SPMV_PATTERN;
+    *form = (ctx->lanczos_fused && applies) ? MEXK_LANCZOS_FUSED : MEXK_LANCZOS_STEPWISE;
+    return MEXK_OK;
+}
+
+int mexk_context_set_lanczos_form(mexk_context_t ctx, int form) {
+    if (!ctx || !ctx->uploaded) return MEXK_ERR_INVALID;
+    if (form != MEXK_LANCZOS_STEPWISE && form != MEXK_LANCZOS_FUSED) return MEXK_ERR_INVALID;
+    MEXK_CK(cudaSetDevice(ctx->device));
+    ctx->lanczos_fused = form == MEXK_LANCZOS_FUSED;
+    invalidate_graphs(ctx);  // captured cycles hold the other form's launches
+    return MEXK_OK;
+}
+
 int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int iters, double* ms_per_launch) {
     if (!ctx || !ctx->uploaded || !ms_per_launch || iters < 1) return MEXK_ERR_INVALID;
     if (kind < 0 || kind >= MEXK_KERNEL_KINDS || j < 0 || j >= ctx->m_alloc) return MEXK_ERR_INVALID;
@@ -1162,6 +1226,13 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
             case MEXK_KERNEL_GRAM_NORM:
                 r = fp32 ? launch_gram_norm(ga, s) : MEXK_ERR_UNSUPPORTED;
                 break;
+            case MEXK_KERNEL_LANCZOS_CYCLE:
+                // steps 1..j from the context's basis columns 0 and 1 (their
+                // inputs stay untouched: launches repeat the same work)
+                r = (fp32 && j >= 1 && use_lanczos_cycle(ctx, j + 1, true, ctx->last_window))
+                        ? enqueue_lanczos_cycle(ctx, j + 1, 1, s)
+                        : MEXK_ERR_UNSUPPORTED;
+                break;
             case MEXK_KERNEL_LIFT: {
                 const LiftArgs l = lift_args(ctx, fp32);
                 r = fp32 ? launch_lift<float>(l, gs_grid_size(ctx->n, 1), s)
@@ -1198,7 +1269,8 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
     // normalise): each launch starts from a fresh copy of the state.
     const bool reset_each = !(kind == MEXK_KERNEL_SPMV || kind == MEXK_KERNEL_SPMV_DOTS ||
                               kind == MEXK_KERNEL_GRAM_DOT || kind == MEXK_KERNEL_GRAM_UPDATE ||
-                              kind == MEXK_KERNEL_GRAM_NORM || kind == MEXK_KERNEL_GS_DOT);
+                              kind == MEXK_KERNEL_GRAM_NORM || kind == MEXK_KERNEL_GS_DOT ||
+                              kind == MEXK_KERNEL_LANCZOS_CYCLE);
     if (reset_each) {
         for (int it = 0; it < iters && rc == MEXK_OK; ++it) {
             cudaError_t ce = cudaMemcpyAsync(ctx->d_state, h_run, sizeof(DevState), cudaMemcpyHostToDevice, s);

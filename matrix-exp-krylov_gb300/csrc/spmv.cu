@@ -922,6 +922,8 @@ extern "C" int mexk_test_force_wait_timeout(int device, int enable) {
     MEXK_CK(cudaSetDevice(device));
     const int v = enable ? 1 : 0;
     MEXK_CK(cudaMemcpyToSymbol(mexk::g_test_dead_wait, &v, sizeof(int)));
+    const int rc = mexk::lanczos_cycle_test_hook(enable);
+    if (rc != MEXK_OK) return rc;
     MEXK_CK(cudaDeviceSynchronize());
     return MEXK_OK;
 }

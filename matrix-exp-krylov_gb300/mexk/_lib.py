@@ -137,12 +137,14 @@ _PROTOS = {
     "mexk_controller_predict": ([_VP, _VP, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_double, _VP, _VP], C.c_int),
     "mexk_test_force_wait_timeout": ([C.c_int, C.c_int], C.c_int),
+    "mexk_context_get_lanczos_form": ([_VP, _IP], C.c_int),
+    "mexk_context_set_lanczos_form": ([_VP, C.c_int], C.c_int),
     "mexk_bincsr_probe": ([C.c_char_p, C.POINTER(BincsrInfo)], C.c_int),
     "mexk_context_load_bincsr": ([_VP, C.c_char_p, C.c_int, C.POINTER(BincsrInfo)], C.c_int),
 }
 
 KERNELS = {"spmv": 0, "gs_dot": 1, "gs_upd_dot": 2, "gs_upd_norm": 3, "normalize": 4, "lift": 5, "controller": 6,
-           "gram_dot": 7, "gram_update": 8, "gram_norm": 9, "spmv_dots": 10}
+           "gram_dot": 7, "gram_update": 8, "gram_norm": 9, "spmv_dots": 10, "lanczos_cycle": 11}
 
 _lib = None
 

@@ -199,6 +199,19 @@ class Context:
         check(lib().mexk_context_set_spmv_form(self._h, PRECISIONS[precision], self.SPMV_FORMS.index(form)),
               "mexk_context_set_spmv_form")
 
+    LANCZOS_FORMS = ("stepwise", "fused")
+
+    def lanczos_form(self) -> str:
+        """How window-2 bases run their steps: "fused" (one cooperative
+        launch per basis, the default where it applies) or "stepwise"."""
+        f = C.c_int(0)
+        check(lib().mexk_context_get_lanczos_form(self._h, C.byref(f)), "mexk_context_get_lanczos_form")
+        return self.LANCZOS_FORMS[f.value]
+
+    def set_lanczos_form(self, form: str) -> None:
+        check(lib().mexk_context_set_lanczos_form(self._h, self.LANCZOS_FORMS.index(form)),
+              "mexk_context_set_lanczos_form")
+
     def arnoldi_step(self, j: int, reorthogonalize=True, precision="fp64"):
         h = np.zeros(j + 1)
         beta = C.c_double(0.0)

@@ -40,6 +40,31 @@ def test_bounded_wait_timeout_reports_and_context_survives(oracle_mod):
     assert rel(y, y_ref) <= 1e-12
 
 
+def test_fused_cycle_barrier_timeout_reports_and_context_survives():
+    """Block 0 of the fused Lanczos cycle leaves before its first grid
+    barrier: the other blocks' bounded waits run out (about a second), every
+    block leaves, the solve stops with MEXK_ERR_DEVICE (timeout), and the
+    context then solves normally with the barrier words reset."""
+    from mexk import synthetic as S
+    from mexk._lib import MexkError, check, lib
+    from mexk.api import Context
+
+    A = S.laplacian_2d(300, h=1.0 / 2049)
+    v = np.random.default_rng(3).uniform(0, 1, A.n)
+    with Context(A, m_alloc=30) as ctx:
+        ctx.set_lanczos_form("fused")
+        assert ctx.lanczos_form() == "fused"
+        y_ok, _ = ctx.expmv(v, 1e-5, 30, precision="mixed", controller="search", window=2)
+        check(lib().mexk_test_force_wait_timeout(0, 1))
+        try:
+            with pytest.raises(MexkError, match="device wait gave up"):
+                ctx.expmv(v, 1e-5, 30, precision="mixed", controller="search", window=2)
+        finally:
+            check(lib().mexk_test_force_wait_timeout(0, 0))
+        y, res = ctx.expmv(v, 1e-5, 30, precision="mixed", controller="search", window=2)
+    assert res["status"] == 0 and np.array_equal(y, y_ok)
+
+
 @pytest.mark.parametrize("where", ["nan_in_v", "inf_in_v", "nan_in_A", "inf_in_A"])
 @pytest.mark.parametrize("form", [("fp64", "reference"), ("mixed", "reference"), ("mixed", "search")])
 def test_non_finite_input_takes_the_breakdown_path(oracle_mod, where, form):

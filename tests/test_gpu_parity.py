@@ -328,6 +328,30 @@ def test_cli_diagonal_known_answer(tmp_path):
     assert rel(y, exact) < 1e-13
 
 
+def test_cli_verbose_h_lines():
+    """--verbose-h prints the reference's store_H_column line for every
+    column of every attempt's basis (main.cu:1951), before its [STEP] line."""
+    import os
+    import subprocess
+
+    from mexk._lib import BUILD
+
+    p = subprocess.run([os.path.join(BUILD, "matrix_exp"), "1000", "--verbose-h"], capture_output=True, text=True,
+                       timeout=300)
+    assert p.returncode == 0, p.stderr
+    lines = p.stdout.splitlines()
+    steps = [i for i, ln in enumerate(lines) if ln.startswith("[STEP]")]
+    assert steps
+    prev = -1
+    for i in steps:
+        m_used = int(lines[i].split("m_used=")[1].split()[0])
+        hl = [ln for ln in lines[prev + 1:i] if ln.startswith("    H_m column")]
+        assert len(hl) == m_used
+        assert hl[0] == "    H_m column 0 stored. Current H_m size: 31x30"
+        assert hl[-1].startswith(f"    H_m column {m_used - 1} stored.")
+        prev = i
+
+
 def test_heat2048_fp64_matches_reference_run():
     """Full-size workload (n = 4,194,304) against the reference's own run:
     the same accept/reject sequence and y to 1e-12 (norm, sum and entries at
@@ -412,15 +436,18 @@ def test_search_controller_accuracy(name, precision):
 
 @pytest.mark.parametrize("name", SYMMETRIC)
 @pytest.mark.parametrize("controller", ["search", "learned"])
-def test_headline_form_vs_reference_fixtures(name, controller):
+@pytest.mark.parametrize("lanczos", ["stepwise", "fused"])
+def test_headline_form_vs_reference_fixtures(name, controller, lanczos):
     """The benchmark's chosen form -- mixed precision, candidate-step
-    control, the short-recurrence window of 2 -- against the reference's own
-    output on symmetric problems, decaying ones included."""
+    control, the short-recurrence window of 2, its steps as two launches
+    each or as one cooperative launch per basis -- against the reference's
+    own output on symmetric problems, decaying ones included."""
     from mexk.api import Context
 
     A, d = load_golden(name)
     m = int(d["m"])
     with Context(A, m_alloc=m) as ctx:
+        ctx.set_lanczos_form(lanczos)
         y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), precision="mixed", controller=controller,
                            window=2)
     assert res["converged"] == 1
@@ -717,3 +744,32 @@ def test_cpp_runner_matches_reference(tmp_path, name):
     y = np.fromfile(tmp_path / "y.bin", dtype=np.float64)
     assert rel(y, d["y"]) <= FP64_TOL, rel(y, d["y"])
     assert f"RESULT restarts_done={int(d['restarts_done'])} converged={int(d['converged'])}" in p.stdout
+
+
+# ------------------------------------------------------------------ fused Lanczos cycle
+@pytest.mark.parametrize("N", [32, 97, 160, 700])
+@pytest.mark.parametrize("controller", ["reference", "search"])
+def test_lanczos_fused_form_matches_stepwise(N, controller):
+    """Window-2 bases in one cooperative launch against the two-kernel
+    steps: the same row sums and updates, dot products summed in another
+    order -- both within 1e-6 of FP64, and of each other (grids whose row
+    count is not a multiple of the blocks' row groups included)."""
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    A = S.laplacian_2d(N, h=1.0 / 2049)
+    v = np.random.default_rng(N).uniform(0, 1, A.n)
+    t = 2e-5
+    with Context(A, m_alloc=30) as ctx:
+        assert ctx.lanczos_form() == "stepwise"  # the default
+        ctx.set_lanczos_form("fused")
+        y64, _ = ctx.expmv(v, t, 30, precision="fp64")
+        yf, rf = ctx.expmv(v, t, 30, precision="mixed", controller=controller, window=2)
+        ctx.set_lanczos_form("stepwise")
+        assert ctx.lanczos_form() == "stepwise"
+        ys, rs = ctx.expmv(v, t, 30, precision="mixed", controller=controller, window=2)
+        ctx.set_lanczos_form("fused")
+        yf2, _ = ctx.expmv(v, t, 30, precision="mixed", controller=controller, window=2)
+    assert rf["converged"] == rs["converged"] == 1
+    assert rel(yf, y64) <= MIXED_TOL and rel(ys, y64) <= MIXED_TOL, (rel(yf, y64), rel(ys, y64))
+    assert np.array_equal(yf, yf2)  # deterministic: the same sums in the same order every launch

@@ -34,3 +34,12 @@ def test_every_kind_times(precision):
                 for kind in ("spmv_dots", "gram_update"):
                     ms = ctx.profile_kernel(kind, j, 3, "mixed")
                     assert 0.0 < ms < 50.0, (kind, j, ms)
+            # the fused form of the window-2 steps: one launch for steps 1..j
+            ctx.set_lanczos_form("fused")
+            assert ctx.lanczos_form() == "fused"
+            ctx.expmv(v, 1e-5, 30, precision="mixed", controller="search", window=2)
+            t29 = ctx.profile_kernel("lanczos_cycle", 29, 3, "mixed")
+            t5 = ctx.profile_kernel("lanczos_cycle", 5, 3, "mixed")
+            assert 0.0 < t5 < t29 < 50.0, (t5, t29)
+            # a step writes one FP32 vector at least: far below 20 TB/s
+            assert 28 * n * 4 / (t29 * 1e-3) < 20e12
