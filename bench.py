@@ -814,6 +814,11 @@ def run_convdiff(args):
                                        "speedup": plain["ms"] / learned["ms"],
                                        "spmv": learned["spmv"], "plain_spmv": plain["spmv"],
                                        "spmv_ratio": plain["spmv"] / max(learned["spmv"], 1)},
+        # the same candidate search without the network (the method the network centres)
+        "learned_vs_search": {"search_solves_per_s": nprob / (tot["mixed+search"]["ms"] / 1e3),
+                              "speedup": tot["mixed+search"]["ms"] / learned["ms"],
+                              "spmv": learned["spmv"], "search_spmv": tot["mixed+search"]["spmv"],
+                              "spmv_ratio": tot["mixed+search"]["spmv"] / max(learned["spmv"], 1)},
         "totals": {k: {"ms": round(v["ms"], 2), "spmv": v["spmv"], "cycles": v["cycles"]} for k, v in tot.items()},
         "per_pe": per_pe,
     }

@@ -250,6 +250,13 @@ int mexk_krylov_result(mexk_context_t ctx, double* y_host);
  * controller is the fixed heuristic of main.cu:1476-1516). */
 int mexk_context_set_controller(mexk_context_t ctx, const float* weights, int count);
 
+/* Loads a second network, used by MEXK_CTRL_LEARNED for solves with a
+ * short-recurrence window (ortho_window > 0, symmetric A), whose cycles cost
+ * about linearly in m where full Gram-Schmidt cycles cost quadratically:
+ * the two are trained on different cycle prices. Without it those solves use
+ * the mexk_context_set_controller network. Same layout and count. */
+int mexk_context_set_window_controller(mexk_context_t ctx, const float* weights, int count);
+
 /* Network on N raw feature rows X[N][8] -> raw outputs Y[N][2] (device). */
 int mexk_mlp_forward(const float* weights, const float* X, int N, float* Y, void* stream);
 /* Gradient of the mean squared error of the normalised outputs over the

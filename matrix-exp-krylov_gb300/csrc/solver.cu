@@ -111,6 +111,7 @@ struct mexk_context_s {
     double* d_cand = nullptr;
     double* d_expm_ws = nullptr;  // Pade workspace of the reference controller for m > EXPM_SMEM_K
     float* d_mlp = nullptr;
+    float* d_mlp_win = nullptr;  // the network for solves with a window (may be null)
     double* d_partials = nullptr;
     GramState* d_gram = nullptr;
     double* d_gram_part = nullptr;
@@ -386,7 +387,7 @@ int finish_basis(mexk_context_t ctx, int j, bool fp32, cudaStream_t s) {
 // The cycle's step controller over the k x k Hessenberg (k = m, or the
 // breakdown size): the reference's (Pade exponential per attempt) or the
 // candidate-step search (with the learned centre for MEXK_CTRL_LEARNED).
-int enqueue_controller(mexk_context_t ctx, int m, int ctrl, mexk_step_t* log, cudaStream_t s) {
+int enqueue_controller(mexk_context_t ctx, int m, int ctrl, mexk_step_t* log, cudaStream_t s, int window = 0) {
     if (ctrl == MEXK_CTRL_REFERENCE) {
         ControlArgs c;
         c.st = ctx->d_state;
@@ -405,7 +406,7 @@ int enqueue_controller(mexk_context_t ctx, int m, int ctrl, mexk_step_t* log, cu
     c.log = log;
     c.cand = ctx->d_cand;
     c.counter = ctx->d_counter + 1;
-    c.mlp = ctrl == MEXK_CTRL_LEARNED ? ctx->d_mlp : nullptr;
+    c.mlp = ctrl != MEXK_CTRL_LEARNED ? nullptr : (window > 0 && ctx->d_mlp_win) ? ctx->d_mlp_win : ctx->d_mlp;
     c.m_cap = ctx->m_alloc < ctx->n - 1 ? ctx->m_alloc : ctx->n - 1;
     return launch_controller_search(c, m, s);
 }
@@ -456,7 +457,7 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, 
             if ((rc = enqueue_step(ctx, j, reortho, fp32, s, window, m))) return rc;
     }
     if ((rc = finish_basis(ctx, m - 1, fp32, s))) return rc;
-    if ((rc = enqueue_controller(ctx, m, ctrl, ctx->d_log, s))) return rc;
+    if ((rc = enqueue_controller(ctx, m, ctrl, ctx->d_log, s, window))) return rc;
     const LiftArgs l = lift_args(ctx, fp32);
     if ((rc = launch_lift<TV>(l, gs_grid_size(ctx->n, 1), s))) return rc;
     return launch_restart<TV>(ctx->n, ctx->ldv, ctx->d_y, V, ctx->d_state, s);
@@ -865,6 +866,7 @@ int mexk_context_destroy(mexk_context_t ctx) {
     dfree(ctx->d_cand);
     dfree(ctx->d_expm_ws);
     dfree(ctx->d_mlp);
+    dfree(ctx->d_mlp_win);
     dfree(ctx->d_partials);
     dfree(ctx->d_gram);
     dfree(ctx->d_gram_part);
@@ -1086,6 +1088,21 @@ int mexk_context_set_controller(mexk_context_t ctx, const float* weights, int co
     return MEXK_OK;
 }
 
+int mexk_context_set_window_controller(mexk_context_t ctx, const float* weights, int count) {
+    if (!ctx || !weights || count != 4886) {
+        set_error_text("controller network must have 4886 parameters");
+        return MEXK_ERR_INVALID;
+    }
+    MEXK_CK(cudaSetDevice(ctx->device));
+    if (!ctx->d_mlp_win) {
+        int rc;
+        if ((rc = dalloc(&ctx->d_mlp_win, static_cast<size_t>(count)))) return rc;
+        invalidate_graphs(ctx);  // captured window cycles hold the other network's address
+    }
+    MEXK_CK(cudaMemcpy(ctx->d_mlp_win, weights, sizeof(float) * count, cudaMemcpyHostToDevice));
+    return MEXK_OK;
+}
+
 int mexk_context_get_spmv_form(mexk_context_t ctx, int precision, int* form) {
     if (!ctx || !ctx->uploaded || !form) return MEXK_ERR_INVALID;
     if (precision != MEXK_PREC_FP64 && precision != MEXK_PREC_MIXED) return MEXK_ERR_INVALID;
@@ -1240,7 +1257,7 @@ int mexk_profile_kernel(mexk_context_t ctx, int kind, int precision, int j, int 
                 break;
             }
             case MEXK_KERNEL_CONTROLLER:
-                r = enqueue_controller(ctx, j + 1, ctx->last_controller, nullptr, s);
+                r = enqueue_controller(ctx, j + 1, ctx->last_controller, nullptr, s, ctx->last_window);
                 break;
         }
         return r;

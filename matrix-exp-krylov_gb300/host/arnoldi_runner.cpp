@@ -20,22 +20,26 @@
 
 namespace {
 
-// The trained controller network: $MEXK_CONTROLLER_NET, else the file the
-// package ships next to the build directory (../mexk/controller_net.f32).
-std::vector<float> load_controller_net() {
+// A trained controller network: $<env>, else the file the package ships
+// next to the build directory (../mexk/<file>). An empty vector when the
+// file is optional and absent; a missing required file exits as the
+// reference does on a bad input.
+std::vector<float> load_controller_net(const char* env_name = "MEXK_CONTROLLER_NET",
+                                       const char* file = "controller_net.f32", bool required = true) {
     std::string path;
-    if (const char* env = std::getenv("MEXK_CONTROLLER_NET"); env && env[0]) {
+    if (const char* env = std::getenv(env_name); env && env[0]) {
         path = env;
     } else {
         Dl_info info;
         if (dladdr(reinterpret_cast<void*>(&load_controller_net), &info) && info.dli_fname) {
             std::string lib(info.dli_fname);
-            path = lib.substr(0, lib.find_last_of('/')) + "/../mexk/controller_net.f32";
+            path = lib.substr(0, lib.find_last_of('/')) + "/../mexk/" + file;
         }
     }
     std::ifstream f(path, std::ios::binary);
     std::vector<float> w(MEXK_NET_TOTAL);
     if (!f || !f.read(reinterpret_cast<char*>(w.data()), sizeof(float) * w.size())) {
+        if (!required) return {};
         std::cerr << "Error: could not read the controller network from " << path << std::endl;
         std::exit(EXIT_FAILURE);
     }
@@ -218,8 +222,15 @@ void ArnoldiRunner::compute_expmv(const std::vector<double>& v_host, std::vector
     }
     if (controller == MEXK_CTRL_LEARNED && !net_loaded) {
         const std::vector<float> w = load_controller_net();
-        const int lrc = mexk_context_set_controller(dc.handle, w.data(), static_cast<int>(w.size()));
+        int lrc = mexk_context_set_controller(dc.handle, w.data(), static_cast<int>(w.size()));
         if (lrc != MEXK_OK) die("mexk_context_set_controller", lrc);
+        // the network priced for window-2 cycles, when shipped
+        const std::vector<float> ww =
+            load_controller_net("MEXK_CONTROLLER_NET_WINDOW", "controller_net_window.f32", false);
+        if (!ww.empty()) {
+            lrc = mexk_context_set_window_controller(dc.handle, ww.data(), static_cast<int>(ww.size()));
+            if (lrc != MEXK_OK) die("mexk_context_set_window_controller", lrc);
+        }
         net_loaded = true;
     }
     int rc = mexk_expmv(dc.handle, &p, v_host.data(), y_host.data(), &last_result);

@@ -127,6 +127,7 @@ _PROTOS = {
     "mexk_gram_schmidt_f64_noalloc": ([C.c_int, C.c_int, _VP, C.c_int, _VP, C.c_int, _VP, _VP, _VP, _VP],
                                       C.c_int),
     "mexk_context_set_controller": ([_VP, C.POINTER(C.c_float), C.c_int], C.c_int),
+    "mexk_context_set_window_controller": ([_VP, C.POINTER(C.c_float), C.c_int], C.c_int),
     "mexk_krylov_start": ([_VP, C.c_int, _DP, _DP], C.c_int),
     "mexk_krylov_build": ([_VP, C.c_int, C.c_int, C.c_int, _DP, _IP], C.c_int),
     "mexk_krylov_advance": ([_VP, C.c_int, C.c_int, _DP, _DP], C.c_int),

@@ -116,14 +116,20 @@ class Context:
         except Exception:
             pass
 
-    def load_controller(self, path=None):
-        """Loads the learned controller's network (default: the trained file
-        shipped with the package)."""
+    def load_controller(self, path=None, window_path=None):
+        """Loads the learned controller's networks (default: the trained files
+        shipped with the package): the one for full Gram-Schmidt cycles and,
+        when its file exists, the one for solves with a window of 2."""
         from . import controller as K
 
         w = np.ascontiguousarray(K.load(path or K.WEIGHTS), dtype=np.float32)
         check(lib().mexk_context_set_controller(self._h, w.ctypes.data_as(C.POINTER(C.c_float)), w.size),
               "mexk_context_set_controller")
+        wp = window_path or (K.WINDOW_WEIGHTS if path is None else None)
+        if wp and os.path.exists(wp):
+            ww = np.ascontiguousarray(K.load(wp), dtype=np.float32)
+            check(lib().mexk_context_set_window_controller(self._h, ww.ctypes.data_as(C.POINTER(C.c_float)),
+                                                           ww.size), "mexk_context_set_window_controller")
         self._net_loaded = True
 
     def _ensure_net(self, controller):

@@ -6,9 +6,10 @@ builds the Arnoldi basis (mexk_krylov_build); the host then evaluates the
 residual estimate |H(k,k-1) [exp(tau H_k) e1]_{k-1}| |v| on a 1/8-octave
 grid of steps tau and keeps the largest passing step tau_max(m). Every grid
 point is one (tau, m, cost, error) tuple. The state's best dimension m* maximises
-tau_max(m) / cost(m) under the byte-count cost model below; the trajectory
+tau_max(m) / cost(m) under the measured cycle-cost model below; the trajectory
 advances with (m*, tau_max(m*)) so the states seen are those the learned
-policy visits.
+policy visits. Two networks: one priced for full Gram-Schmidt cycles, one for
+the window-2 short recurrence of a symmetric A (cycles linear in m).
 
 Network (8 -> 64 -> 64 -> 2, GELU, FP32; mexk_mlp_* kernels):
   inputs  the basis features of csrc/controller_net.cuh (same formulas here)
@@ -34,9 +35,12 @@ NET_PARAMS = 4866
 NET_TOTAL = 4886
 M_SET = (10, 20, 30, 40, 50, 60)
 FP32_FLOOR = 2.0 ** -24
+ERR_BUDGET_REL = 5e-7  # accepted errors, relative to |y|, the relaxed tolerance may spend
 HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS = os.path.join(HERE, "controller_net.f32")
 META = os.path.join(HERE, "controller_net.json")
+# the network for solves with a window of 2 (symmetric A), trained on that cycle's cost
+WINDOW_WEIGHTS = os.path.join(HERE, "controller_net_window.f32")
 
 
 # ------------------------------------------------------------------ features
@@ -65,31 +69,26 @@ def features(H, k, rem, tol, vnorm, tau_prev, err_prev):
 
 
 # ------------------------------------------------------------------ cost model
-# Cycles are priced at the workloads' scale: the sweep problems are small,
-# but the trained policy runs on matrices of millions of rows, where bytes
-# dominate the fixed per-launch costs. The network sees no problem size, so
-# the labels must come from one consistent price.
-TARGET_ROWS = 4_194_304
+# Cycles are priced by their measured time on GB300 (mixed precision, the
+# candidate-step search, one cycle per graph launch), fitted as
+# F + C m + D m^2 milliseconds. The network sees no problem size, so the
+# labels come from one consistent price per kind of cycle:
+#   "arnoldi"  full Gram-Schmidt (any A): the 128^3 convection-diffusion
+#              workload, 2,097,152 rows; m = 10..60 -> 0.54, 1.27, 2.28,
+#              3.56, 5.18, 7.00 ms per cycle (the sweeps grow with k);
+#   "window2"  the short recurrence of a symmetric A (ortho_window = 2):
+#              heat 2048^2, 4,194,304 rows; m = 10..60 -> 0.38, 0.65, 0.93,
+#              1.23, 1.59, 1.94 ms per cycle (every step reads four vectors).
+CYCLE_COST_MS = {
+    "arnoldi": (0.0924, 0.030694, 0.0014114),
+    "window2": (0.14639, 0.022511, 0.00012409),
+}
 
 
-def cycle_cost(m, n, nnz, precision="mixed", target_rows=TARGET_ROWS, step_fixed_s=2.0e-5,
-               cycle_fixed_s=2.5e-4, gbs=5.5e12):
-    """Seconds per Krylov cycle of dimension m for a matrix with this
-    nonzeros-per-row ratio at `target_rows` rows (None: its own n):
-    algorithmic bytes at `gbs`, plus a fixed cost per Arnoldi step (launches,
-    the dot sweep's grid reduction) and per cycle (controller, lift, sync).
-    Mixed: SpMV, a (k+1)-vector dot sweep and a (k+2)-vector update per step,
-    one norm per cycle; FP64: SpMV, three CGS2 sweeps and a normalisation."""
-    s = 4 if precision == "mixed" else 8
-    rows = target_rows if target_rows else n
-    nz = nnz / max(n, 1) * rows
-    spmv = m * (nz * (s + 4) + 4 * (rows + 1) + 2 * rows * s)
-    if precision == "mixed":
-        gs = s * rows * (sum(2 * k + 3 for k in range(1, m + 1)) + 1)
-    else:
-        gs = s * rows * sum(3 * k + 7 for k in range(1, m + 1))
-    lift = (m * s + 8) * rows
-    return (spmv + gs + lift) / gbs + m * step_fixed_s + cycle_fixed_s
+def cycle_cost(m, kind="arnoldi"):
+    """Seconds per Krylov cycle of dimension m under the measured model."""
+    F, C_, D = CYCLE_COST_MS[kind]
+    return (F + C_ * m + D * m * m) * 1e-3
 
 
 # ------------------------------------------------------------------ step search
@@ -134,23 +133,28 @@ def largest_tau(H, k, beta, tol, rem, start, breakdown=False):
 
 
 # ------------------------------------------------------------------ data
-def sweep_problem(ctx, A, v, t, precision="mixed", tol=1e-6, max_states=60, m_set=M_SET, log=None):
+def sweep_problem(ctx, A, v, t, precision="mixed", tol=1e-6, max_states=60, m_set=M_SET, log=None,
+                  kind="arnoldi"):
     """Walk one solve with per-state sweeps over m. Returns (X, T, tuples)."""
     L = lib()
     prec = PREC_MIXED if precision == "mixed" else PREC_FP64
     floor = FP32_FLOOR if precision == "mixed" else 0.0
+    budget = ERR_BUDGET_REL if precision == "mixed" else 0.0
     v = np.ascontiguousarray(v, dtype=np.float64)
     beta = C.c_double(0.0)
     check(L.mexk_krylov_start(ctx.handle, prec, v.ctypes.data_as(C.POINTER(C.c_double)), C.byref(beta)))
     beta = beta.value
     t_done, tau_prev, err_prev = 0.0, 0.0, 0.0
+    err_acc = 0.0  # the errors accepted so far (the relaxed tolerance's budget)
     X, T, tuples = [], [], []
     mmax = min(max(m_set), ctx.m_alloc, A.n - 1)
     for _ in range(max_states):
         rem = t - t_done
         if rem <= 0 or beta <= 1e-300:
             break
-        tol_eff = max(tol, floor * beta)
+        # the device's rule for a mixed-precision solve under the candidate
+        # search: max(tol, min(2^-24 |y|, 5e-7 |y| - accepted errors))
+        tol_eff = max(tol, min(floor * beta, budget * beta - err_acc))
         per_m = []
         for m in m_set:
             if m > mmax:
@@ -163,7 +167,7 @@ def sweep_problem(ctx, A, v, t, precision="mixed", tol=1e-6, max_states=60, m_se
             f, n1 = features(H, k, rem, tol_eff, beta, tau_prev, err_prev)
             start = tau_prev * 2 if tau_prev > 0 else rem
             tau, w, err, tp = largest_tau(H, k, beta, tol_eff, rem, start, breakdown=k < m)
-            cost = cycle_cost(m, A.n, A.nnz, precision)
+            cost = cycle_cost(m, kind)
             tuples.extend((tt, m, cost, ee) for tt, ee in tp)
             if tau is None:
                 continue
@@ -185,6 +189,7 @@ def sweep_problem(ctx, A, v, t, precision="mixed", tol=1e-6, max_states=60, m_se
         check(L.mexk_krylov_advance(ctx.handle, prec, k, coef.ctypes.data_as(C.POINTER(C.c_double)), C.byref(nb)))
         beta = nb.value
         t_done += tau
+        err_acc += err
         tau_prev, err_prev = tau, err
         if log:
             log(f"  t={t_done:.3e} m*={m_star} tau={tau:.3e} beta={beta:.3e}")
@@ -218,14 +223,28 @@ def skew_problem(n, degree, seed, shift=0.1):
 CONVDIFF_T = {1.0: 2e-3, 10.0: 2e-3, 100.0: 1e-3, 1000.0: 1e-4}
 
 
-def training_problems(scale="small"):
-    """Seeded problems for the sweeps: 3D convection-diffusion at the four
-    Peclet numbers of the learned-controller workload (coarser grids, times
-    from CONVDIFF_T), 2D heat at the heat2048 stiffness, and oscillatory
-    skew-symmetric-plus-shift matrices."""
+def training_problems(scale="small", kind="arnoldi"):
+    """Seeded problems for the sweeps. "arnoldi": 3D convection-diffusion at
+    the four Peclet numbers of the learned-controller workload (coarser
+    grids, times from CONVDIFF_T), 2D heat at the heat2048 stiffness, and
+    oscillatory skew-symmetric-plus-shift matrices. "window2" (symmetric A
+    only): 2D heat over grids and horizons around the heat2048 workload's
+    stiffness and 3D diffusion (the convection-diffusion operator at Pe = 0)."""
     from . import synthetic as S
 
     probs = []
+    if kind == "window2":
+        for N in (64, 96, 128, 192, 256, 384, 512, 768):
+            A = S.laplacian_2d(N, h=1.0 / 2049)
+            v = np.random.default_rng(N).uniform(0, 1, A.n)
+            for f in (1, 3):
+                probs.append((f"heat{N}_{f}t", A, v, f * 1e-5))
+        for N in (20, 28, 40):
+            A = S.convection_diffusion_3d(N, 0.0, h=1.0 / 129)
+            v = np.random.default_rng(100 + N).uniform(0, 1, A.n)
+            for t in (2e-3, 6e-3):
+                probs.append((f"diffusion{N}_t{t:g}", A, v, t))
+        return probs
     wide = scale == "wide"
     grids = (20, 28, 40, 52) if wide else ((20, 28, 40) if scale == "small" else (48, 64))
     for N in grids:
@@ -354,13 +373,18 @@ def main(argv=None):
     ap.add_argument("--states", type=int, default=40)
     ap.add_argument("--data-out", default=None, help="also save the raw sweep data (.npz)")
     ap.add_argument("--scale", default="small", choices=["small", "wide", "large"], help="training problem set")
-    ap.add_argument("--out", default=None, help="directory for controller_net.f32 / .json (default: the package)")
+    ap.add_argument("--out", default=None, help="directory for the weights and their .json (default: the package)")
+    ap.add_argument("--kind", default="arnoldi", choices=sorted(CYCLE_COST_MS),
+                    help="cycle cost model: full Gram-Schmidt, or the window-2 short recurrence (symmetric A)")
+    ap.add_argument("--m-set", default=",".join(str(m) for m in M_SET),
+                    help="Krylov dimensions swept per state (the labels' m* is one of them)")
     args = ap.parse_args(argv)
+    m_set = tuple(int(x) for x in args.m_set.split(","))
     t0 = time.time()
     Xs, Ts, ntuples, names = [], [], 0, []
-    for name, A, v, t in training_problems(args.scale):
+    for name, A, v, t in training_problems(args.scale, args.kind):
         with Context(A, m_alloc=max(M_SET)) as ctx:
-            X, T, tup = sweep_problem(ctx, A, v, t, max_states=args.states)
+            X, T, tup = sweep_problem(ctx, A, v, t, max_states=args.states, kind=args.kind, m_set=m_set)
         Xs.append(X)
         Ts.append(T)
         ntuples += len(tup)
@@ -373,11 +397,11 @@ def main(argv=None):
     w, losses = train(X, T, epochs=args.epochs, log=print)
     meta = {"inputs": NET_IN, "hidden": NET_HID, "outputs": NET_OUT, "samples": int(len(X)),
             "tuples": int(ntuples), "problems": names, "epochs": args.epochs, "final_loss": losses[-1],
-            "initial_loss": losses[0], "m_set": list(M_SET), "precision": "mixed",
-            "cost_model": {"target_rows": TARGET_ROWS, "step_fixed_s": 2.0e-5, "cycle_fixed_s": 2.5e-4,
-                           "gbs": 5.5e12},
+            "initial_loss": losses[0], "m_set": list(m_set), "precision": "mixed",
+            "cost_model": {"kind": args.kind, "cycle_ms_F_C_D": list(CYCLE_COST_MS[args.kind])},
             "scale": args.scale, "seconds": round(time.time() - t0, 1)}
-    save(w, meta, os.path.join(args.out, "controller_net.f32") if args.out else WEIGHTS)
+    fname = os.path.basename(WEIGHTS if args.kind == "arnoldi" else WINDOW_WEIGHTS)
+    save(w, meta, os.path.join(args.out, fname) if args.out else os.path.join(HERE, fname))
     print(json.dumps(meta))
 
 
