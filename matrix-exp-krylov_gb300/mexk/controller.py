@@ -234,7 +234,7 @@ def training_problems(scale="small", kind="arnoldi"):
 
     probs = []
     if kind == "window2":
-        for N in (64, 96, 128, 192, 256, 384, 512, 768):
+        for N in (64, 128, 256, 384, 512, 768, 1024, 1536):
             A = S.laplacian_2d(N, h=1.0 / 2049)
             v = np.random.default_rng(N).uniform(0, 1, A.n)
             for f in (1, 3):

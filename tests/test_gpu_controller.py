@@ -235,3 +235,31 @@ def test_learned_controller_against_search():
         for k in tot:
             tot[k] += out[k][1]["spmv_count"]
     assert tot["learned"] <= tot["search"], tot
+
+
+@pytest.mark.parametrize("N", [160, 640])
+def test_learned_window_controller_against_search(N):
+    """Window-2 (Lanczos) solves of held-out heat grids (not among the
+    window network's training grids): the network priced for window-2
+    cycles, whose cost grows about linearly in m, takes larger bases than
+    the search's fixed m and needs no more sparse products."""
+    import time
+
+    from mexk import synthetic as S
+    from mexk.api import Context
+
+    A = S.laplacian_2d(N, h=1.0 / 2049)
+    v = np.random.default_rng(N + 1).uniform(0, 1, A.n)
+    t = 1e-5
+    with Context(A, m_alloc=60) as ctx:
+        y64, _ = ctx.expmv(v, t, 30)
+        out = {}
+        for ctrl in ("search", "learned"):
+            ctx.expmv(v, t, 30, precision="mixed", controller=ctrl, window=2)
+            t0 = time.perf_counter()
+            y, r = ctx.expmv(v, t, 30, precision="mixed", controller=ctrl, window=2)
+            out[ctrl] = (time.perf_counter() - t0, r, np.linalg.norm(y - y64) / np.linalg.norm(y64))
+    print(N, {k: (round(v[0] * 1e3, 2), v[1]["spmv_count"], v[1]["cycles"], f"{v[2]:.2e}") for k, v in out.items()})
+    for ctrl, (_, r, err) in out.items():
+        assert r["converged"] == 1 and err <= 1e-6, (ctrl, err)
+    assert out["learned"][1]["spmv_count"] <= out["search"][1]["spmv_count"]
