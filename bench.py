@@ -916,12 +916,12 @@ def run_batch_once(args):
         print(json.dumps(b.info()), flush=True)
 
 
-def run_solve_once(local_rank, grid=2048, spmv_form=None):
-    """One solve in the headline form (mixed precision, candidate-step
-    controller, window 2: the heat matrix is symmetric) and one plain FP64
-    solve of the heat equation on a grid x grid mesh, untimed: the command
-    ncu captures. spmv_form: run that SpMV form instead of the context's
-    choice (the row-pattern form on this matrix)."""
+def run_solve_once(local_rank, grid=2048, spmv_form=None, controller="learned"):
+    """One solve in the headline form (mixed precision, window 2: the heat
+    matrix is symmetric; the learned controller unless `controller` names
+    another) and one plain FP64 solve of the heat equation on a grid x grid
+    mesh, untimed: the command ncu captures. spmv_form: run that SpMV form
+    instead of the context's choice (the row-pattern form on this matrix)."""
     import torch
 
     from mexk import synthetic as S
@@ -929,11 +929,12 @@ def run_solve_once(local_rank, grid=2048, spmv_form=None):
 
     torch.cuda.set_device(local_rank)
     P = make_problem() if grid == 2048 else S.config1(N=grid)
-    with Context(P.A, m_alloc=P.m, device=local_rank) as ctx:
+    # room for the Krylov dimensions the learned controller may choose (<= 60)
+    with Context(P.A, m_alloc=60, device=local_rank) as ctx:
         if spmv_form is not None:
             for prec in ("mixed", "fp64"):
                 ctx.set_spmv_form(spmv_form, prec)
-        for prec, ctrl, window in (("mixed", "search", 2), ("fp64", "reference", 0)):
+        for prec, ctrl, window in (("mixed", controller, 2), ("fp64", "reference", 0)):
             _, res = ctx.expmv(P.v, P.t, P.m, precision=prec, controller=ctrl, window=window)
             print(prec, ctrl, window, res, flush=True)
 
@@ -1015,7 +1016,8 @@ def main():
         run_batch_once(args)
         return
     if args.solve_once:
-        run_solve_once(int(os.environ.get("LOCAL_RANK", "0")), args.grid, args.spmv_form)
+        run_solve_once(int(os.environ.get("LOCAL_RANK", "0")), args.grid, args.spmv_form,
+                       args.controller if args.precision != "auto" else "learned")
         return
     if args.workload == "batch" and args.impl == "ours":
         run_batch(args)
