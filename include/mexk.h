@@ -270,8 +270,9 @@ int mexk_mlp_gradient(const float* weights, const float* X, const float* T, cons
 int mexk_mlp_adam_step(float* weights, float* adam_state, const float* X, const float* T, const int* idx,
                        int count, int step, float lr, float* loss_parts, float* scratch, void* stream);
 /* The controller's view of a basis: out[0..7] = features of H (device,
- * leading dimension ldh >= k+1), out[8..9] = network outputs (0 if
- * weights is NULL), out[10] = log2 |H_k|_1. */
+ * leading dimension ldh >= k+1, 1 <= k <= MEXK_M_MAX_MIXED, the bases the
+ * learned controller sees), out[8..9] = network outputs (0 if weights is
+ * NULL), out[10] = log2 |H_k|_1. */
 int mexk_controller_predict(const float* weights, const double* H, int ldh, int k, double rem, double tol,
                             double vnorm, double tau_prev, double err_prev, float* out, void* stream);
 

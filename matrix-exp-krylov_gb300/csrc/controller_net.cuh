@@ -48,39 +48,64 @@ __device__ __forceinline__ float gelu_grad(float x) {
 //   f2 subdiagonal log2-decay per column     f6 log2(previous step * |H_k|_1)
 //      over the last half of the basis       f7 log2(previous estimate / tolerance)
 //   f3 log2(tolerance / |v|)
-// Also returns |H_k|_1. Computed by thread 0; deterministic.
+// Every thread of the block calls it (k <= 64): thread j sums column j of
+// H_k in row order (|H_k|_1 is the largest such sum), warp 0 combines the
+// columns (the two squared-norm sums as a fixed xor butterfly: every lane
+// ends with the same bits), lane 0 writes f. FP64 adds take about 64 clocks
+// here, so a single thread's O(k^2) chain cost tens of microseconds. col:
+// 192 doubles of shared scratch; n1: one shared double. Returns |H_k|_1 to
+// every thread; deterministic.
 __device__ inline double basis_features(const double* H, int ldh, int k, double rem, double tol, double vnorm,
-                                        double tau_prev, double err_prev, float* f) {
-    double n1 = 0.0, fro = 0.0, upper = 0.0;
-    for (int j = 0; j < k; ++j) {
-        double cs = 0.0;
-        for (int i = 0; i <= j + 1 && i < k; ++i) {
-            const double h = H[i + static_cast<size_t>(j) * ldh];
-            cs += fabs(h);
-            fro += h * h;
-            if (i < j - 1) upper += h * h;
+                                        double tau_prev, double err_prev, float* f, double* col, double* n1_out) {
+    const int t = threadIdx.x;
+    for (int j = t; j < 64; j += blockDim.x) {
+        double cs = 0.0, fr = 0.0, up = 0.0;
+        if (j < k) {
+            for (int i = 0; i <= j + 1 && i < k; ++i) {
+                const double h = H[i + static_cast<size_t>(j) * ldh];
+                cs += fabs(h);
+                fr += h * h;
+                if (i < j - 1) up += h * h;
+            }
         }
-        n1 = cs > n1 ? cs : n1;
+        col[j] = cs;
+        col[64 + j] = fr;
+        col[128 + j] = up;
     }
-    const double tiny = 1e-300;
-    n1 = n1 > tiny ? n1 : tiny;
-    const double hk = fabs(H[k + static_cast<size_t>(k - 1) * ldh]);
-    const int jm = k / 2;  // column of the mid-basis subdiagonal
-    const double hm = fabs(H[(jm + 1) + static_cast<size_t>(jm) * ldh]);
-    const double span = (k - 1 - jm) > 0 ? static_cast<double>(k - 1 - jm) : 1.0;
-    f[0] = static_cast<float>(log2(n1 * (rem > tiny ? rem : tiny)));
-    f[1] = static_cast<float>(log2(hk / n1 + 1e-30));
-    f[2] = static_cast<float>((log2(hk + tiny) - log2(hm + tiny)) / span);
-    f[3] = static_cast<float>(log2(tol / (vnorm > tiny ? vnorm : tiny)));
-    f[4] = static_cast<float>(k) / 64.0f;
-    f[5] = static_cast<float>(fro > 0.0 ? sqrt(upper / fro) : 0.0);
-    f[6] = tau_prev > 0.0 ? static_cast<float>(log2(tau_prev * n1)) : f[0];
-    f[7] = err_prev > 0.0 ? static_cast<float>(log2(err_prev / tol)) : 0.0f;
-    for (int i = 0; i < IN; ++i) {
-        if (!isfinite(f[i])) f[i] = 0.0f;
-        f[i] = fminf(fmaxf(f[i], -200.0f), 200.0f);
+    __syncthreads();
+    if (t < 32) {
+        double n1 = fmax(col[t], col[t + 32]);
+        double fro = col[64 + t] + col[96 + t];
+        double upper = col[128 + t] + col[160 + t];
+        for (int o = 16; o >= 1; o >>= 1) {
+            n1 = fmax(n1, __shfl_xor_sync(0xffffffffu, n1, o));
+            fro += __shfl_xor_sync(0xffffffffu, fro, o);
+            upper += __shfl_xor_sync(0xffffffffu, upper, o);
+        }
+        if (t == 0) {
+            const double tiny = 1e-300;
+            n1 = n1 > tiny ? n1 : tiny;
+            const double hk = fabs(H[k + static_cast<size_t>(k - 1) * ldh]);
+            const int jm = k / 2;  // column of the mid-basis subdiagonal
+            const double hm = fabs(H[(jm + 1) + static_cast<size_t>(jm) * ldh]);
+            const double span = (k - 1 - jm) > 0 ? static_cast<double>(k - 1 - jm) : 1.0;
+            f[0] = static_cast<float>(log2(n1 * (rem > tiny ? rem : tiny)));
+            f[1] = static_cast<float>(log2(hk / n1 + 1e-30));
+            f[2] = static_cast<float>((log2(hk + tiny) - log2(hm + tiny)) / span);
+            f[3] = static_cast<float>(log2(tol / (vnorm > tiny ? vnorm : tiny)));
+            f[4] = static_cast<float>(k) / 64.0f;
+            f[5] = static_cast<float>(fro > 0.0 ? sqrt(upper / fro) : 0.0);
+            f[6] = tau_prev > 0.0 ? static_cast<float>(log2(tau_prev * n1)) : f[0];
+            f[7] = err_prev > 0.0 ? static_cast<float>(log2(err_prev / tol)) : 0.0f;
+            for (int i = 0; i < IN; ++i) {
+                if (!isfinite(f[i])) f[i] = 0.0f;
+                f[i] = fminf(fmaxf(f[i], -200.0f), 200.0f);
+            }
+            *n1_out = n1;
+        }
     }
-    return n1;
+    __syncthreads();
+    return *n1_out;
 }
 
 // Forward pass by the first HID threads of a block (all threads must call:

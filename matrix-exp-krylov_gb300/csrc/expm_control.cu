@@ -725,9 +725,8 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
     double spacing = 0.25;
     int offset = 24;
     if (a.mlp != nullptr) {
-        if (threadIdx.x == 0)
-            s_n1 = net::basis_features(a.H, a.ldh, k, rem, tol_eff, st->v_norm, st->tau_prev, st->err_prev, s_f);
-        __syncthreads();
+        __shared__ double s_col[192];
+        net::basis_features(a.H, a.ldh, k, rem, tol_eff, st->v_norm, st->tau_prev, st->err_prev, s_f, s_col, &s_n1);
         net::mlp_forward_block(a.mlp, s_f, s_a1, s_a2, s_o);
         if (threadIdx.x == 0) {
             double c = exp2(static_cast<double>(s_o[0])) / s_n1;

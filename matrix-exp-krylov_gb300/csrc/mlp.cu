@@ -164,9 +164,8 @@ __global__ void predict_kernel(const float* __restrict__ w, const double* __rest
                                double rem, double tol, double vnorm, double tau_prev, double err_prev,
                                float* __restrict__ out) {
     __shared__ float f[IN], a1[HID], a2[HID], o[OUT];
-    __shared__ double n1;
-    if (threadIdx.x == 0) n1 = basis_features(H, ldh, k, rem, tol, vnorm, tau_prev, err_prev, f);
-    __syncthreads();
+    __shared__ double col[192], n1s;
+    const double n1 = basis_features(H, ldh, k, rem, tol, vnorm, tau_prev, err_prev, f, col, &n1s);
     if (w != nullptr) mlp_forward_block(w, f, a1, a2, o);
     if (threadIdx.x < IN) out[threadIdx.x] = f[threadIdx.x];
     if (threadIdx.x < OUT) out[IN + threadIdx.x] = (w != nullptr) ? o[threadIdx.x] : 0.f;
@@ -217,7 +216,7 @@ extern "C" int mexk_mlp_adam_step(float* weights, float* adam_state, const float
 
 extern "C" int mexk_controller_predict(const float* weights, const double* H, int ldh, int k, double rem, double tol,
                                        double vnorm, double tau_prev, double err_prev, float* out, void* stream) {
-    if (!H || !out || k < 1 || k > MEXK_M_MAX || ldh < k + 1) return MEXK_ERR_INVALID;
+    if (!H || !out || k < 1 || k > MEXK_M_MAX_MIXED || ldh < k + 1) return MEXK_ERR_INVALID;
     predict_kernel<<<1, net::HID, 0, static_cast<cudaStream_t>(stream)>>>(weights, H, ldh, k, rem, tol, vnorm,
                                                                           tau_prev, err_prev, out);
     MEXK_CK_LAUNCH("predict_kernel");
