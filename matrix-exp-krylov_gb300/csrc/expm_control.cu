@@ -31,7 +31,10 @@ namespace mexk {
 namespace {
 
 constexpr int EXPM_THREADS = 512;
-constexpr int SEARCH_CLUSTER = 4;  // thread blocks (SMs) per candidate exponential: 32 x 4 of the 152 SMs
+constexpr int SEARCH_CLUSTER = 8;  // thread blocks (SMs) per chain of candidate exponentials
+// chains of candidates one octave apart: 12 with a network (96 SMs), 8 without (64)
+constexpr int SEARCH_CHAINS_NET = 12;
+constexpr int SEARCH_CHAINS = 8;
 
 // FP64 adds and FMAs take about 64 cycles of latency on this GPU (FP32: 4),
 // and these k <= 64 matrices leave most of the block idle, so every dot
@@ -359,7 +362,7 @@ __device__ void mm_p(const P& pr, int k, const double* X, const double* Y, doubl
 // thread of the block (of every block of the cluster) must call it, with
 // the same B.A.
 template <typename P>
-__device__ double* expm_taylor(const ExpmBuf& B, int k, const P& pr) {
+__device__ __noinline__ double* expm_taylor(const ExpmBuf& B, int k, const P& pr) {
     __shared__ int s_sq;
     if (threadIdx.x < k) B.red[threadIdx.x] = col_abs_sum(k, B.A, threadIdx.x);
     __syncthreads();
@@ -689,8 +692,9 @@ __device__ void write_log(DevState* st, mexk_step_t* log, double dt, double err,
 
 // Candidate steps tau_g = center * 2^((g - 24)/4), g = 0..31 (1/64 .. 3.4 x the
 // centre), each clamped to the remaining time. Every cluster of
-// SEARCH_CLUSTER blocks evaluates one candidate's exponential (the products
-// shared out over its SMs) and residual estimate; the last block to finish
+// SEARCH_CLUSTER blocks evaluates a chain of candidates an octave apart
+// (their exponentials and residual estimates; the products shared out over
+// its SMs); the last block to finish
 // takes the largest passing step (its exponential is reused for the lift),
 // or, if none passes, continues below the smallest candidate with the
 // reference's shrink rule (on its own).
@@ -738,31 +742,69 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
     }
     ExpmBuf B = carve(smem, k);
     {
-        // With a network: candidates 0..15 on a 1/8-octave grid around its
-        // prediction (2^-1 .. 2^0.875), 16..31 on the quarter-octave grid the
-        // search uses around twice the previous step (2^-4 .. 2^-0.25 of it),
-        // so a poor prediction degrades to a coarser search.
-        const int g = static_cast<int>(blockIdx.x) / SEARCH_CLUSTER;
+        // Candidates one octave apart differ by a squaring: exp(2 tau H) =
+        // exp(tau H)^2, and as |2 tau H|_1 = 2 |tau H|_1 takes one more
+        // halving, both steps reduce to the same scaled matrix whenever
+        // |2 tau H|_1 > 1: the squared result is then bit for bit the
+        // directly computed one (below that, equal to rounding). So each cluster takes
+        // a chain of candidates g0, g0 + P, ... whose steps double, computes
+        // the first exponential and squares its way up; a member clamped to
+        // the remaining time is computed directly, once (later clamped
+        // members are the same step).
+        //   network: candidates 0..15 on a 1/8-octave grid around its
+        //     prediction (2^-1 .. 2^0.875), chains (c, c+8) for c < 8;
+        //     16..31 on the quarter-octave grid the search uses around twice
+        //     the previous step (2^-4 .. 2^-0.25 of it), chains (c, c+4,
+        //     c+8, c+12) for c = 16..19, so a poor prediction degrades to a
+        //     coarser search;
+        //   no network: 0..31 on the quarter-octave grid (2^-6 .. 2^1.75 of
+        //     the centre), chains (c, .., c+12) for c = 0..3 and 16..19.
+        const int chain = static_cast<int>(blockIdx.x) / SEARCH_CLUSTER;
         const bool lead = blockIdx.x % SEARCH_CLUSTER == 0;
-        double tau;
-        if (a.mlp != nullptr && g < SEARCH_CAND / 2) {
-            tau = s_center * exp2(0.125 * (g - 8));
+        int g0, period, len;
+        double tau0;
+        if (a.mlp != nullptr && chain < 8) {
+            g0 = chain;
+            period = 8;
+            len = 2;
+            tau0 = s_center * exp2(0.125 * (g0 - 8));
         } else if (a.mlp != nullptr) {
+            g0 = SEARCH_CAND / 2 + (chain - 8);
+            period = 4;
+            len = 4;
             const double base = st->tau_prev > 0.0 ? 2.0 * st->tau_prev : st->dt;
-            tau = base * exp2(0.25 * (g - SEARCH_CAND / 2 - 15));
+            tau0 = base * exp2(0.25 * (g0 - SEARCH_CAND / 2 - 15));
         } else {
-            tau = s_center * exp2(spacing * (g - offset));
+            g0 = chain < 4 ? chain : SEARCH_CAND / 2 + (chain - 4);
+            period = 4;
+            len = 4;
+            tau0 = s_center * exp2(spacing * (g0 - offset));
         }
-        tau = tau < rem ? tau : rem;
-        for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = tau * a.H[(e % k) + (e / k) * ldh];
-        __syncthreads();
-        double* R = expm_taylor(B, k, ClusterProducts{k});
-        double* c = a.cand + static_cast<size_t>(g) * CAND_STRIDE;
-        if (lead)
-            for (int i = threadIdx.x; i < k; i += blockDim.x) c[2 + i] = R[i];
-        if (lead && threadIdx.x == 0) {
-            c[0] = bd ? 0.0 : fabs(a.H[k + (k - 1) * ldh] * R[k - 1]) * st->v_norm;
-            c[1] = tau;
+        const ClusterProducts pr{k};
+        double* E = nullptr;
+        bool clamped_done = false;
+        double t_i = tau0;
+        for (int i = 0; i < len; ++i, t_i *= 2.0) {
+            const bool clamped = !(t_i < rem);
+            const double tau = clamped ? rem : t_i;
+            if (i == 0 || (clamped && !clamped_done)) {
+                for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = tau * a.H[(e % k) + (e / k) * ldh];
+                __syncthreads();
+                E = expm_taylor(B, k, pr);
+                clamped_done = clamped;
+            } else if (!clamped) {
+                double* W = E == B.T ? B.U : B.T;
+                mm_p(pr, k, E, E, W);
+                E = W;
+            }
+            double* c = a.cand + static_cast<size_t>(g0 + i * period) * CAND_STRIDE;
+            if (lead)
+                for (int r = threadIdx.x; r < k; r += blockDim.x) c[2 + r] = E[r];
+            if (lead && threadIdx.x == 0) {
+                c[0] = bd ? 0.0 : fabs(a.H[k + (k - 1) * ldh] * E[k - 1]) * st->v_norm;
+                c[1] = tau;
+            }
+            pr.sync();  // the lead has read E before the next product writes into the buffers
         }
     }
     if (!grid_last_block(a.counter, &s_flag)) return;
@@ -770,7 +812,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
     if (threadIdx.x < 32) {
         // The largest passing step, the lowest index among equal steps (the
         // serial scan's choice), one lane per candidate and a butterfly.
-        const int ncand = static_cast<int>(gridDim.x) / SEARCH_CLUSTER;
+        const int ncand = SEARCH_CAND;
         int g = static_cast<int>(threadIdx.x);
         double tau = -1.0;
         if (g < ncand) {
@@ -846,7 +888,7 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
 int launch_controller_search(const SearchArgs& a, int m, cudaStream_t s) {
     if (m > EXPM_SMEM_K) return MEXK_ERR_UNSUPPORTED;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(SEARCH_CAND * SEARCH_CLUSTER);
+    cfg.gridDim = dim3((a.mlp != nullptr ? SEARCH_CHAINS_NET : SEARCH_CHAINS) * SEARCH_CLUSTER);
     cfg.blockDim = dim3(EXPM_THREADS);
     cfg.dynamicSmemBytes = expm_smem_bytes(m);
     cfg.stream = s;
