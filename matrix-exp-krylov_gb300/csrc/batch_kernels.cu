@@ -57,17 +57,20 @@ __device__ __forceinline__ const float4* col4(const Layout& L, int c) {
 }
 
 // Arrival of one block of problem p; true in the last of `expected` blocks.
+// One fence per block, by the arriving thread (as in grid_last_block).
 __device__ __forceinline__ bool problem_last(unsigned int* counter, unsigned int expected, int* s_flag) {
-    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) *s_flag = (atomicAdd(counter, 1u) == expected - 1u) ? 1 : 0;
-    __syncthreads();
-    const bool last = *s_flag != 0;
-    if (last) {
+    if (threadIdx.x == 0) {
         __threadfence();
-        if (threadIdx.x == 0) *counter = 0u;
+        const bool last = atomicAdd(counter, 1u) == expected - 1u;
+        if (last) {
+            __threadfence();
+            *counter = 0u;
+        }
+        *s_flag = last ? 1 : 0;
     }
-    return last;
+    __syncthreads();
+    return *s_flag != 0;
 }
 
 // Sum of slot `slot` over the tiles of problem p.

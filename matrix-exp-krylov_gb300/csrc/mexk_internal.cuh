@@ -211,21 +211,24 @@ struct RowIO<4, float> {
 
 // Last-block-done handshake for grid reductions: every block has written its
 // partials; returns true in exactly one block (the last to arrive), which
-// then sees all partials. The counter is reset by that block.
+// then sees all partials. The counter is reset by that block. The block
+// barrier orders every thread's writes before thread 0's fence, and fences
+// are cumulative, so one thread per block fences (as a cooperative grid
+// barrier does) rather than all of them.
 __device__ __forceinline__ bool grid_last_block(unsigned int* counter, int* smem_flag) {
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned int ticket = atomicAdd(counter, 1u);
-        *smem_flag = (ticket == gridDim.x - 1) ? 1 : 0;
+        __threadfence();
+        const unsigned int ticket = atomicAdd(counter, 1u);
+        const bool last = ticket == gridDim.x - 1;
+        if (last) {
+            __threadfence();  // the other blocks' partials before this block reads them
+            *counter = 0u;
+        }
+        *smem_flag = last ? 1 : 0;
     }
     __syncthreads();
-    const bool last = *smem_flag != 0;
-    if (last) {
-        __threadfence();
-        if (threadIdx.x == 0) *counter = 0u;
-    }
-    return last;
+    return *smem_flag != 0;
 }
 
 // Deterministic reduction of partials[b * RED_STRIDE + c] over blocks
