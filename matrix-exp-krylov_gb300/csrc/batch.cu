@@ -189,6 +189,29 @@ Layout layout(mexk_batch_t b, const Wave& w) {
     return L;
 }
 
+// The wave's cycle loop runs on the device: a conditional while node whose
+// body is one cycle followed by wave_loop_next. active[0] = states still
+// stepping (the status kernel's count), active[1] = cycles run.
+__global__ void wave_loop_start(cudaGraphConditionalHandle h, int* active) {
+    active[1] = 0;
+    cudaGraphSetConditional(h, active[0] > 0 ? 1u : 0u);
+}
+__global__ void wave_loop_next(cudaGraphConditionalHandle h, int* active, int limit) {
+    const int c = active[1] + 1;
+    active[1] = c;
+    cudaGraphSetConditional(h, (active[0] > 0 && c < limit) ? 1u : 0u);
+}
+
+// Start of a wave: |v| per state, u_0 = v / |v|, problem status.
+int enqueue_wave_start(mexk_batch_t b, const Wave& w, cudaStream_t s) {
+    const Layout L = layout(b, w);
+    int rc;
+    if ((rc = launch_lift(L, 0, 1, s))) return rc;
+    if ((rc = launch_restart(L, 1, s))) return rc;
+    MEXK_CK(cudaMemsetAsync(b->d_active, 0, sizeof(int), s));
+    return launch_status(L, w.p0, w.p1, s);
+}
+
 // One cycle of a wave (captured into its graph).
 int enqueue_wave_cycle(mexk_batch_t b, const Wave& w, cudaStream_t s) {
     const Layout L = layout(b, w);
@@ -216,29 +239,79 @@ int enqueue_wave_cycle(mexk_batch_t b, const Wave& w, cudaStream_t s) {
     return launch_status(L, w.p0, w.p1, s);
 }
 
+// Every state accepts or finishes once per cycle: at most max_steps cycles.
+int wave_cycle_limit(mexk_batch_t b) { return (b->prm.max_restarts > 0 ? b->prm.max_restarts : 1000) + 2; }
+
+// The whole wave as one graph: its start, then the cycles in a device-side
+// while loop (one launch per wave; the host reads the outcome afterwards).
 int capture_wave(mexk_batch_t b, Wave& w) {
     if (w.exec) {
         cudaGraphExecDestroy(w.exec);
         w.exec = nullptr;
     }
-    cudaGraph_t g = nullptr;
-    MEXK_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    const int rc = enqueue_wave_cycle(b, w, b->stream);
-    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-    if (rc) {
-        if (g) cudaGraphDestroy(g);
-        return rc;
-    }
-    if (e != cudaSuccess) {
-        set_cuda_error(e, "cudaStreamEndCapture (batch)", __FILE__, __LINE__);
+    cudaStream_t s = b->stream;
+    cudaGraph_t g = nullptr, body = nullptr;
+    MEXK_CK(cudaGraphCreate(&g, 0));
+    int rc = MEXK_OK;
+    cudaError_t e = cudaSuccess;
+    std::vector<cudaGraphNode_t> deps;
+    cudaGraphConditionalHandle h = 0;
+    auto fail = [&](cudaError_t err, const char* what) {
+        set_cuda_error(err, what, __FILE__, __LINE__);
         return MEXK_ERR_CUDA;
+    };
+    if ((e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(e, "cudaGraphConditionalHandleCreate (batch)");
     }
-    const cudaError_t ei = cudaGraphInstantiate(&w.exec, g, 0);
+    // the start and the loop's first condition, captured into g
+    if ((e = cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(e, "cudaStreamBeginCaptureToGraph (batch)");
+    }
+    rc = enqueue_wave_start(b, w, s);
+    if (rc == MEXK_OK) {
+        wave_loop_start<<<1, 1, 0, s>>>(h, b->d_active);
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* d = nullptr;
+        size_t nd = 0;
+        e = cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &d, nullptr, &nd);
+        if (e == cudaSuccess) deps.assign(d, d + nd);
+    }
+    cudaGraph_t got = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(s, &got);
+    if (rc != MEXK_OK || e != cudaSuccess || e2 != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return rc != MEXK_OK ? rc : fail(e != cudaSuccess ? e : e2, "wave start capture (batch)");
+    }
+    // the while node after it, its body one cycle and the next condition
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if ((e = cudaGraphAddNode(&node, g, deps.data(), nullptr, deps.size(), &cp)) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(e, "cudaGraphAddNode (batch while)");
+    }
+    body = cp.conditional.phGraph_out[0];
+    if ((e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(e, "cudaStreamBeginCaptureToGraph (batch body)");
+    }
+    rc = enqueue_wave_cycle(b, w, s);
+    if (rc == MEXK_OK) wave_loop_next<<<1, 1, 0, s>>>(h, b->d_active, wave_cycle_limit(b));
+    const cudaError_t e3 = cudaStreamEndCapture(s, &got);
+    if (rc != MEXK_OK || e3 != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return rc != MEXK_OK ? rc : fail(e3, "wave body capture (batch)");
+    }
+    e = cudaGraphInstantiate(&w.exec, g, 0);
     cudaGraphDestroy(g);
-    if (ei != cudaSuccess) {
-        set_cuda_error(ei, "cudaGraphInstantiate (batch)", __FILE__, __LINE__);
-        return MEXK_ERR_CUDA;
-    }
+    if (e != cudaSuccess) return fail(e, "cudaGraphInstantiate (batch)");
     return MEXK_OK;
 }
 
@@ -408,14 +481,14 @@ int mexk_batch_upload(mexk_batch_t b) {
         (rc = dalloc(&b->d_s, S * (BLD + 1))) || (rc = dalloc(&b->d_pre, S * (BLD + 1))) ||
         (rc = dalloc(&b->d_coefl, S * BLD)) || (rc = dalloc(&b->d_coef, S * BLD)) || (rc = dalloc(&b->d_wsc, S)) ||
         (rc = dalloc(&b->d_psc, S)) || (rc = dalloc(&b->d_pcount, P)) || (rc = dalloc(&b->d_pdone, P)) ||
-        (rc = dalloc(&b->d_active, 1)) || (rc = dalloc(&b->d_ptile0, P)) || (rc = dalloc(&b->d_ptiles, P)))
+        (rc = dalloc(&b->d_active, 2)) || (rc = dalloc(&b->d_ptile0, P)) || (rc = dalloc(&b->d_ptiles, P)))
         return rc;
     MEXK_CK(cudaMemset(b->d_H, 0, sizeof(double) * S * BLD * BM_MAX));
     MEXK_CK(cudaMemset(b->d_pcount, 0, sizeof(unsigned int) * P));
     MEXK_CK(cudaMemset(b->d_pdone, 0, sizeof(int) * P));
     MEXK_CK(cudaMemcpy(b->d_prow0, b->prow0.data(), sizeof(long long) * (P + 1), cudaMemcpyHostToDevice));
     {
-        cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&b->h_active), sizeof(int));
+        cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&b->h_active), 2 * sizeof(int));
         if (e != cudaSuccess) {
             set_cuda_error(e, "cudaMallocHost (batch)", __FILE__, __LINE__);
             return MEXK_ERR_ALLOC;
@@ -531,23 +604,12 @@ int mexk_batch_run(mexk_batch_t b) {
     b->have_final = false;
     for (auto& w : b->waves) {
         if (!w.exec && (rc = capture_wave(b, w))) return rc;
-        const Layout L = layout(b, w);
-        // start vectors: |v| per state, u_0 = v / |v|, problem status
-        if ((rc = launch_lift(L, 0, 1, b->stream))) return rc;
-        if ((rc = launch_restart(L, 1, b->stream))) return rc;
-        MEXK_CK(cudaMemsetAsync(b->d_active, 0, sizeof(int), b->stream));
-        if ((rc = launch_status(L, w.p0, w.p1, b->stream))) return rc;
-        MEXK_CK(cudaMemcpyAsync(b->h_active, b->d_active, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+        // one launch: start vectors, then the cycles until every state is done
+        MEXK_CK(cudaGraphLaunch(w.exec, b->stream));
+        MEXK_CK(cudaMemcpyAsync(b->h_active, b->d_active, 2 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
         MEXK_CK(cudaStreamSynchronize(b->stream));
-        // every state accepts or finishes once per cycle: at most max_steps cycles
-        const int limit = (b->prm.max_restarts > 0 ? b->prm.max_restarts : 1000) + 2;
-        for (int c = 0; c < limit && *b->h_active > 0; ++c) {
-            MEXK_CK(cudaGraphLaunch(w.exec, b->stream));
-            MEXK_CK(cudaMemcpyAsync(b->h_active, b->d_active, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
-            MEXK_CK(cudaStreamSynchronize(b->stream));
-            ++b->cycles;
-        }
-        if (*b->h_active > 0) {
+        b->cycles += b->h_active[1];
+        if (b->h_active[0] > 0) {
             set_error_text("batch wave did not finish within the step limit");
             return MEXK_ERR_DEVICE;
         }
