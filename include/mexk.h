@@ -86,10 +86,11 @@ typedef struct {
     int precision;       /* MEXK_PREC_* */
     int controller;      /* MEXK_CTRL_*: step-size control (0 = the reference's) */
     int ortho_window;    /* 0: orthogonalise against the whole basis (Arnoldi, the
-                            reference's method). W >= 2 (mixed precision, symmetric A
-                            only): against the last W basis vectors, the short
-                            recurrence of Lanczos; the context verifies symmetry
-                            (MEXK_ERR_INVALID otherwise). No reference counterpart. */
+                            reference's method). W >= 2 (symmetric A only, either
+                            precision): against the last W basis vectors, the short
+                            recurrence of Lanczos (FP64: CGS2 over the window); the
+                            context verifies symmetry (MEXK_ERR_INVALID otherwise).
+                            No reference counterpart. */
     const mexk_stepping_t* stepping; /* NULL: the defaults above. Otherwise used as
                             given with the reference controller; the candidate-step
                             controllers take dt_min, dt_max, tol_step, max_steps and

@@ -84,20 +84,21 @@ __device__ __forceinline__ void gs_finish(const GsArgs& a, int ncols, double* s_
     const int j = a.j;
     const int c = a.c0 + static_cast<int>(threadIdx.x);
     const size_t ldh = static_cast<size_t>(a.ldh);
+    const size_t hr = static_cast<size_t>(a.h_row0) + c;  // the Hessenberg row of column c of V
     if (MODE == GS_DOT) {
         if (static_cast<int>(threadIdx.x) < ncols) {
             if (a.pass2) {
                 a.h2[c] = s_out[threadIdx.x];
-                if (a.H) a.H[c + j * ldh] = a.h1[c] + s_out[threadIdx.x];
+                if (a.H) a.H[hr + j * ldh] = a.h1[c] + s_out[threadIdx.x];
             } else {
                 a.h1[c] = s_out[threadIdx.x];
-                if (!a.reortho && a.H) a.H[c + j * ldh] = s_out[threadIdx.x];
+                if (!a.reortho && a.H) a.H[hr + j * ldh] = s_out[threadIdx.x];
             }
         }
     } else if (MODE == GS_UPD_DOT) {
         if (static_cast<int>(threadIdx.x) < ncols) {
             a.h2[c] = s_out[threadIdx.x];
-            if (a.H) a.H[c + j * ldh] = a.h1[c] + s_out[threadIdx.x];
+            if (a.H) a.H[hr + j * ldh] = a.h1[c] + s_out[threadIdx.x];
         }
     } else if (threadIdx.x == 0) {
         const double beta = sqrt(s_out[0]);

@@ -354,6 +354,8 @@ struct GsArgs {
     int c0 = 0;       // the dot sweep reduces columns c0 .. c0+kd-1 (kd <= GS_DOT_COLS)
     int kd = 0;       //   (kd = 0: all k columns)
     int pass2 = 0;    // GS_DOT on a chunk of the second pass: results into h2 and H = h1 + h2
+    int h_row0 = 0;   // V's first column is basis column h_row0 (a short-recurrence window):
+                      //   the dots go to H rows h_row0.., the norm to H(j+1, j)
     int j;            // Arnoldi step (column of H)
     int ldv;          // basis leading dimension (elements)
     int ldh;          // H leading dimension

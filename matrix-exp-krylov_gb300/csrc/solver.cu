@@ -218,10 +218,6 @@ int check_params(mexk_context_t ctx, const mexk_params_t* p) {
             set_error_text("ortho_window must be 0 or in 2..m");
             return MEXK_ERR_INVALID;
         }
-        if (p->precision != MEXK_PREC_MIXED) {
-            set_error_text("a short-recurrence window is implemented for the mixed form only");
-            return MEXK_ERR_UNSUPPORTED;
-        }
         int sym = 0;
         const int rc = matrix_symmetric(ctx, &sym);
         if (rc) return rc;
@@ -374,8 +370,16 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
         return launch_gram_update(g, s);
     }
     if ((rc = context_spmv(ctx, j, false, &ctx->d_state->breakdown, s))) return rc;
-    const GsArgs g = gs_args(ctx, j, reortho, false);
-    if ((rc = launch_gs_step(g, gs_grid_size(ctx->n, j + 1), s))) return rc;
+    GsArgs g = gs_args(ctx, j, reortho, false);
+    if (window > 0) {
+        // CGS2 against the window's columns lo..j only (Lanczos for a symmetric A);
+        // H(0:lo-1, j) stays at the zero the cycle starts from
+        const int lo = std::max(0, j + 1 - window);
+        g.V = ctx->d_V + static_cast<size_t>(lo) * ctx->ldv;
+        g.k = j + 1 - lo;
+        g.h_row0 = lo;
+    }
+    if ((rc = launch_gs_step(g, gs_grid_size(ctx->n, g.k), s))) return rc;
     return launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s);
 }
 
@@ -448,6 +452,9 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, 
     const bool fp32 = sizeof(TV) == 4;
     TV* V = fp32 ? reinterpret_cast<TV*>(ctx->d_V32) : reinterpret_cast<TV*>(ctx->d_V);
     int rc;
+    // a window's FP64 steps leave H(0:lo-1, j) alone: the cycle starts from zero
+    if (!fp32 && window > 0)
+        MEXK_CK(cudaMemsetAsync(ctx->d_H, 0, sizeof(double) * static_cast<size_t>(ctx->ldh) * m, s));
     if (use_lanczos_cycle(ctx, m, fp32, window)) {
         // step 0 as two kernels (its update writes step 1's b and a_0 partials), then the rest in one launch
         if ((rc = enqueue_step(ctx, 0, reortho, fp32, s, window, m))) return rc;
@@ -465,7 +472,7 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, 
 
 int enqueue_cycle_any(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, int window, cudaStream_t s) {
     return prec == MEXK_PREC_MIXED ? enqueue_cycle<float>(ctx, m, reortho, ctrl, window, s)
-                                   : enqueue_cycle<double>(ctx, m, reortho, ctrl, 0, s);
+                                   : enqueue_cycle<double>(ctx, m, reortho, ctrl, window, s);
 }
 
 int get_graph(mexk_context_t ctx, int m, int prec, int reortho, int ctrl, int window, cudaGraphExec_t* out) {

@@ -454,6 +454,35 @@ def test_headline_form_vs_reference_fixtures(name, controller, lanczos):
     assert rel(y, d["y"]) <= MIXED_TOL, rel(y, d["y"])
 
 
+FP64_WINDOW_TOL = 1e-9
+
+
+@pytest.mark.parametrize("name", SYMMETRIC)
+def test_fp64_window_vs_reference_fixtures(name):
+    """Plain FP64 with the short-recurrence window of 2 (Lanczos: CGS2 over
+    the last two basis vectors, the reference's controller) against the
+    reference's own full-Arnoldi output on symmetric problems: the same
+    accept/reject decisions and y within FP64_WINDOW_TOL (the Krylov
+    approximation's own error, not rounding, sets the difference)."""
+    from mexk.api import Context
+
+    A, d = load_golden(name)
+    m = int(d["m"])
+    with Context(A, m_alloc=m) as ctx:
+        y, res = ctx.expmv(d["v"], float(d["t"]), m, tol=float(d["tol"]), max_restarts=int(d["max_restarts"]),
+                           precision="fp64", window=2)
+        steps = ctx.steps()
+    ref_steps = [ln.split() for ln in d["step_lines"]]
+    print(name, res["restarts_done"], int(d["restarts_done"]), rel(y, d["y"]) if np.linalg.norm(d["y"]) > 0 else 0.0)
+    assert res["converged"] == int(d["converged"])
+    assert res["restarts_done"] == int(d["restarts_done"])
+    assert len(steps) == len(ref_steps)
+    for st, r in zip(steps, ref_steps):  # the same attempts, accepts and rejects
+        assert f"dt={st[1]:g}" == r[2] and f"accepts={st[4]}" == r[5] and f"rejects={st[5]}" == r[6]
+    if np.linalg.norm(d["y"]) > 0:
+        assert rel(y, d["y"]) <= FP64_WINDOW_TOL, rel(y, d["y"])
+
+
 def test_underflowing_config4_time():
     """Convection-diffusion at Pe = 1000 and t = 1, the config-4 time: the
     exact solution underflows to zero; every form returns |y| within the
@@ -544,8 +573,8 @@ def test_window_refused_for_nonsymmetric_matrix():
     with Context(A, m_alloc=30) as ctx:
         with pytest.raises(MexkError, match="symmetric"):
             ctx.expmv(v, 0.5, 30, precision="mixed", window=2)
-        with pytest.raises(MexkError):
-            ctx.expmv(v, 0.5, 30, precision="fp64", window=2)  # FP64 keeps full Arnoldi
+        with pytest.raises(MexkError, match="symmetric"):
+            ctx.expmv(v, 0.5, 30, precision="fp64", window=2)
         with pytest.raises(MexkError):
             ctx.expmv(v, 0.5, 30, precision="mixed", window=1)
         y, r = ctx.expmv(v, 0.5, 30, precision="mixed")  # the context stays usable
