@@ -240,10 +240,12 @@ def lanczos_fused(ctx, precision, window):
     return precision == "mixed" and window == 2 and ctx.lanczos_form() == "fused"
 
 
-def profile_cycle(ctx, m, n, nnz, precision, iters=2, window=0):
+def profile_cycle(ctx, m, n, nnz, precision, iters=8, window=0):
     """CUDA-event timing of every kernel kind of one Krylov cycle (the sweeps
     as the context's last solve ran them: with its window, if any; a fused
-    Lanczos basis as its one launch for steps 1..m-1)."""
+    Lanczos basis as its one launch for steps 1..m-1), each kind and step
+    as `iters` back-to-back launches after one untimed (a solve's steps
+    follow one another the same way; two launches read about 15 % high)."""
     fp32 = precision == "mixed"
     once = CYCLE_KINDS[precision]
     form = ctx.spmv_form(precision)
