@@ -422,7 +422,7 @@ def run_ours(args, rank, world, local_rank):
     # (precision, controller, window): window 2 = Lanczos' short recurrence,
     # which the library accepts only for a symmetric matrix (refusals skipped).
     candidates = [("mixed", "search", 2), ("mixed", "learned", 2), ("mixed", "learned", 0), ("mixed", "search", 0),
-                  ("mixed", "reference", 0), ("fp64", "search", 0)]
+                  ("mixed", "reference", 0), ("fp64", "search", 0), ("fp64", "reference", 2), ("fp64", "search", 2)]
     if args.precision != "auto":
         candidates = [(args.precision, args.controller, args.window)]
     checked = []
