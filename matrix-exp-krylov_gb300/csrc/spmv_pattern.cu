@@ -173,7 +173,9 @@ constexpr unsigned PAT_FULL = 0xffffffffu;
 // straight to its gathers; any other warp takes each non-major row's
 // offsets and values from the table -- all entries of a row (two rows
 // without DOTS, whose registers allow it) requested together, so a boundary
-// costs a round trip per row, not one per entry. Either way a row's products are formed and added in
+// costs a round trip per row, not one per entry -- unless all its rows share
+// one pattern (a boundary line of a stencil: that pattern's entries are
+// loaded once for the warp and the rows take the major pattern's loop). Either way a row's products are formed and added in
 // entry order from zero. With DOTS (FP32 mixed form, a step j >= 1 over
 // columns j-1 and j; DOTS 2: symmetric A, u_{j-1} w taken from the previous
 // update as w_{j-1} u_j) each row sum also accumulates u_{j-1} w, u_j w, |w|^2
@@ -256,11 +258,49 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
                 }
             }
         };
-        bool all_major = r0 + (PAT_RPT - 1) * 32 < n;
+        const bool all_in = r0 + (PAT_RPT - 1) * 32 < n;
+        bool all_major = all_in;
 #pragma unroll
         for (int i = 0; i < PAT_RPT; ++i) all_major = all_major && cur[i] == major;
+        // one pattern over all of the warp's rows (a boundary line of a stencil)
+        const int p0 = __shfl_sync(PAT_FULL, cur[0], 0);
+        bool uniform = all_in;
+#pragma unroll
+        for (int i = 0; i < PAT_RPT; ++i) uniform = uniform && cur[i] == p0;
         TX s[PAT_RPT];
-        if (__all_sync(PAT_FULL, all_major)) {
+        if (!__all_sync(PAT_FULL, all_major) && __all_sync(PAT_FULL, uniform)) {
+            // that pattern's entries once for the warp (broadcast loads), then
+            // the gathers as for the major pattern, summed in the same order
+            const int plen = __ldg(tlen + p0);
+            int po[LMAX];
+            TX pa[LMAX];
+            int pq0 = -1;
+#pragma unroll
+            for (int q = 0; q < LMAX; ++q) {
+                const bool on = q < plen;
+                po[q] = on ? __ldg(toff + p0 * PAT_LEN + q) : 0;
+                pa[q] = on ? __ldg(tv + p0 * PAT_LEN + q) : TX(0);
+                if (on && po[q] == 0) pq0 = q;
+            }
+            const TX* xb = x + r0;
+            if (pq0 < 0) load_uj();
+#pragma unroll
+            for (int i = 0; i < PAT_RPT; ++i) {
+                TX acc = TX(0);
+#pragma unroll
+                for (int q = 0; q < LMAX; ++q) {
+                    if (q < plen) {
+                        const TX xq = __ldg(xb + (i * 32 + po[q]));
+                        if constexpr (DOTS) {
+                            if (q == pq0) uj[i] = xq;
+                        }
+                        acc += pat_mul(pa[q], xq);
+                    }
+                }
+                s[i] = acc;
+            }
+            emit(s, true);
+        } else if (__all_sync(PAT_FULL, all_major)) {
             const TX* xb = x + r0;
             if (q0 < 0) load_uj();
 #pragma unroll
