@@ -70,31 +70,42 @@ __device__ __forceinline__ int step2_slot(int v, int kw, int lo) {
     return v < kw ? lo + v : (v < 2 * kw ? GRAM_BOFF + lo + (v - kw) : GRAM_NWOFF);
 }
 
-// The scalar chain of a step over at most two columns (kw = 1 or 2; lo =
-// j + 1 - kw) from its sums tot = {a (kw), b (kw), |w|^2}: s_j = 1/|u_j|,
-// H(j, j-1) = |u_j| / p_j with the breakdown test of main.cu:1911, the Gram
-// entry G(j-1, j), c = s s_j a, h = c - (G - I) c, the update coefficients
-// and the pre-scale p of the next column (one rsqrt, a few products, one
-// rsqrt). s0 = s_{lo} (kw = 2), ip_j = 1 / (pre-scale of column j).
 struct Step2Out {
     double sj, beta, hp, hj, g01, p, ip;
     bool bad;
 };
-__device__ __forceinline__ Step2Out step2_chain(const double* tot, int kw, int j, int reortho, double s0,
-                                                double ip_j) {
+
+// The part of the chain that needs only b_{j-1} = u_{j-1}.u_j, b_j = |u_j|^2
+// and a_{j-1} (kw = 2; zeros for kw = 1) with s0 and ip_j: s_j, H(j, j-1)
+// and the breakdown test of main.cu:1911 (the square root runs beside the
+// chain, whose results are used only once the test has passed), s_j^2,
+// G(j-1, j) and c_{j-1}.
+struct Step2Pre {
+    double sj, sj2, beta, g01, cp;
+    bool bad;
+};
+__device__ __forceinline__ Step2Pre step2_chain_pre(double bjm1, double bj, double a0, int j, double s0, double ip_j) {
+    Step2Pre o;
+    o.sj = (bj > 0.0 && !isinf(bj)) ? rsqrt(bj) : 0.0;
+    o.beta = j >= 1 ? sqrt(bj) * ip_j : 1.0;
+    o.bad = !(o.beta >= 1e-14) || isinf(o.beta);
+    o.sj2 = o.sj * o.sj;
+    o.g01 = (s0 * bjm1) * o.sj;  // G(j-1, j)
+    o.cp = (s0 * a0) * o.sj;     // c_{j-1}
+    return o;
+}
+
+// The rest, from a_j, |w|^2 and c_{j-1}: c = s s_j a, h = c - (G - I) c, the
+// update coefficients and the pre-scale p of the next column.
+__device__ __forceinline__ Step2Out step2_chain_rest(const Step2Pre& pr, int kw, double aj, double nw, double cp,
+                                                     int reortho) {
     Step2Out o;
-    const double bj = tot[2 * kw - 1];
-    const double sj = (bj > 0.0 && !isinf(bj)) ? rsqrt(bj) : 0.0;
-    // H(j, j-1) and the breakdown test: the square root runs beside the
-    // chain below, whose results are used only once the test has passed
-    const double beta = j >= 1 ? sqrt(bj) * ip_j : 1.0;
-    o.bad = !(beta >= 1e-14) || isinf(beta);
-    const double sj2 = sj * sj;
-    const double cj = sj2 * tot[kw - 1];
+    o.bad = pr.bad;
+    const double sj2 = pr.sj2;
+    const double cj = sj2 * aj;
     double hj = cj, hp = 0.0, g01 = 0.0, part;
     if (kw == 2) {
-        g01 = (s0 * tot[kw]) * sj;              // G(j-1, j)
-        const double cp = (s0 * tot[0]) * sj;  // c_{j-1}
+        g01 = pr.g01;
         hp = cp;
         if (reortho) {
             hp = cp - __dmul_rn(g01, cj);
@@ -105,7 +116,7 @@ __device__ __forceinline__ Step2Out step2_chain(const double* tot, int kw, int j
     } else {
         part = hj * (hj - 2.0 * cj);
     }
-    const double w2 = sj2 * tot[2 * kw];
+    const double w2 = sj2 * nw;
     const double u2 = w2 + part;
     double p = 1.0, ip = 1.0;
     if (u2 > 1e-8 * w2 && !isinf(u2)) {
@@ -115,14 +126,26 @@ __device__ __forceinline__ Step2Out step2_chain(const double* tot, int kw, int j
         p = rsqrt(w2);
         ip = w2 * p;
     }
-    o.sj = sj;
-    o.beta = beta;
+    o.sj = pr.sj;
+    o.beta = pr.beta;
     o.hp = hp;
     o.hj = hj;
     o.g01 = g01;
     o.p = p;
     o.ip = ip;
     return o;
+}
+
+// The scalar chain of a step over at most two columns (kw = 1 or 2; lo =
+// j + 1 - kw) from its sums tot = {a (kw), b (kw), |w|^2}: s_j = 1/|u_j|,
+// H(j, j-1) = |u_j| / p_j with the breakdown test, the Gram entry G(j-1, j),
+// c = s s_j a, h = c - (G - I) c, the update coefficients and the pre-scale
+// p of the next column (one rsqrt, a few products, one rsqrt). s0 = s_{lo}
+// (kw = 2), ip_j = 1 / (pre-scale of column j).
+__device__ __forceinline__ Step2Out step2_chain(const double* tot, int kw, int j, int reortho, double s0,
+                                                double ip_j) {
+    const Step2Pre pr = step2_chain_pre(kw == 2 ? tot[kw] : 0.0, tot[2 * kw - 1], kw == 2 ? tot[0] : 0.0, j, s0, ip_j);
+    return step2_chain_rest(pr, kw, tot[kw - 1], tot[2 * kw], pr.cp, reortho);
 }
 
 // Writes a step's results (step2_chain) into H, the Gram state and the
@@ -185,6 +208,73 @@ __device__ __forceinline__ void step2_finish(const GramArgs& g, int nrb_a, int n
     if (t != 0) return;
     const Step2Out o = step2_chain(s_tot, kw, j, g.reortho, s0, ip_j);
     step2_store(g, kw, o, s0);
+}
+
+// For a step over two columns whose dots the SpMV takes (kw = 2): the
+// chain's first part (step2_chain_pre) from the previous update's partials,
+// which exist before the SpMV starts -- b_{j-1}, b_j and, with g.sym, a_{j-1}
+// over nrb_b row blocks -- summed as step2_finish<PR> sums them and stored in
+// g.gs->pre. One block calls it (every thread) after its own rows and before
+// it arrives, so that the last block's finish only runs the rest.
+template <int PR>
+__device__ __forceinline__ void step2_precompute(const GramArgs& g, int nrb_b) {
+    const int j = g.j;
+    const int lo = g.lo;  // j - 1
+    __shared__ double s_pb[3];
+    const bool sym = g.sym != 0;
+    step_sum_partials<PR>(
+        g.part, sym ? 3 : 2, [&](int v) { return v == 0 ? GRAM_BOFF + lo : (v == 1 ? GRAM_BOFF + j : lo); },
+        [&](int) { return nrb_b; }, s_pb);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        GramState* gs = g.gs;
+        const Step2Pre pr = step2_chain_pre(s_pb[0], s_pb[1], sym ? s_pb[2] : 0.0, j, __ldcg(&gs->s[lo]),
+                                            __ldcg(&gs->ip[j]));
+        gs->pre[0] = pr.sj;
+        gs->pre[1] = pr.sj2;
+        gs->pre[2] = pr.beta;
+        gs->pre[3] = pr.g01;
+        gs->pre[4] = pr.cp;
+        gs->pre[5] = pr.bad ? 1.0 : 0.0;
+    }
+}
+
+// The finish of such a step in the last block: the SpMV's partials (a_j,
+// |w|^2 and, without g.sym, a_{j-1}), the chain's first part from
+// g.gs->pre, the rest of the chain and the stores. Bit for bit the result of
+// step2_finish<PR>: the same sums and the same operations.
+template <int PR>
+__device__ __forceinline__ void step2_finish_pre(const GramArgs& g, int nrb_a) {
+    const int j = g.j;
+    const int lo = g.lo;
+    __shared__ double s_ta[3];  // a_j, |w|^2, a_{j-1}
+    const int t = threadIdx.x;
+    GramState* gs = g.gs;
+    const size_t ldh = static_cast<size_t>(g.ldh);
+    for (int r = t; r < lo; r += blockDim.x) g.H[r + static_cast<size_t>(j) * ldh] = 0.0;  // outside the window
+    const bool sym = g.sym != 0;
+    // the block's last warp (idle during the sums, which need at most three)
+    // fetches the first part meanwhile, so the two round trips overlap
+    __shared__ double s_pre[7];
+    const int tl = t - (static_cast<int>(blockDim.x) - 32);
+    if (tl >= 0 && tl < 6) s_pre[tl] = __ldcg(&gs->pre[tl]);
+    if (tl == 6) s_pre[6] = __ldcg(&gs->s[lo]);
+    step_sum_partials<PR>(
+        g.part, sym ? 2 : 3, [&](int v) { return v == 0 ? j : (v == 1 ? GRAM_NWOFF : lo); },
+        [&](int) { return nrb_a; }, s_ta);
+    __syncthreads();
+    if (t != 0) return;
+    Step2Pre pr;
+    pr.sj = s_pre[0];
+    pr.sj2 = s_pre[1];
+    pr.beta = s_pre[2];
+    pr.g01 = s_pre[3];
+    pr.cp = s_pre[4];
+    pr.bad = s_pre[5] != 0.0;
+    const double s0 = s_pre[6];
+    const double cp = sym ? pr.cp : (s0 * s_ta[2]) * pr.sj;
+    const Step2Out o = step2_chain_rest(pr, 2, s_ta[0], s_ta[1], cp, g.reortho);
+    step2_store(g, 2, o, s0);
 }
 
 }  // namespace

@@ -212,19 +212,18 @@ struct RowIO<4, float> {
 // Last-block-done handshake for grid reductions: every block has written its
 // partials; returns true in exactly one block (the last to arrive), which
 // then sees all partials. The counter is reset by that block. The block
-// barrier orders every thread's writes before thread 0's fence, and fences
-// are cumulative, so one thread per block fences (as a cooperative grid
-// barrier does) rather than all of them.
+// barrier orders every thread's writes before thread 0's release, and
+// release and acquire are cumulative, so one thread per block synchronises
+// (as a cooperative grid barrier does) rather than all of them.
 __device__ __forceinline__ bool grid_last_block(unsigned int* counter, int* smem_flag) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned int ticket = atomicAdd(counter, 1u);
+        // one acquire-release atomic: releases this block's partials, and in the
+        // last block acquires every other block's
+        unsigned int ticket;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(ticket) : "l"(counter) : "memory");
         const bool last = ticket == gridDim.x - 1;
-        if (last) {
-            __threadfence();  // the other blocks' partials before this block reads them
-            *counter = 0u;
-        }
+        if (last) *counter = 0u;
         *smem_flag = last ? 1 : 0;
     }
     __syncthreads();
@@ -405,6 +404,9 @@ struct GramState {
     double ip[GRAM_M + 2];    // 1 / (pre-scale applied when column c was written)
     float coef[GRAM_M + 8];   // update coefficients s_c h_c of the current step
     float wsc, psc;               // update: u_{j+1} = psc * (wsc * w - sum coef_c u_c)
+    // the part of a step's scalar chain from the previous update's partials
+    // (step2_precompute): s_j, s_j^2, H(j, j-1), G(j-1, j), c_{j-1}, breakdown
+    double pre[6];
 };
 struct GramArgs {
     int n, j, ldv, ldh, reortho;

@@ -571,6 +571,7 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
         // Every block that ran (a timed-out one too, so that the arrival count
         // stays whole) writes its partials; the last one finishes the step.
         if (skipped) return;
+        if (blockIdx.x == 0) step2_precompute<16>(ga, ga.b_blocks);  // the chain's first part, as above
         __shared__ double s_red[8][3];
         const float r0 = warp_sum(da0), r1 = warp_sum(da1), r2 = warp_sum(dw);
         if (lane == 0) {
@@ -582,7 +583,7 @@ __global__ void __launch_bounds__(ST_THREADS, ST_MINB)
         step_write_partials(s_red, ga.part, blockIdx.x, [&](int q) { return q < 2 ? jj - 1 + q : GRAM_NWOFF; });
         __shared__ int s_flag;
         if (!grid_last_block(ga.counter, &s_flag)) return;
-        step2_finish(ga, gridDim.x, ga.b_blocks);
+        step2_finish_pre<16>(ga, gridDim.x);
     }
 }
 

@@ -356,6 +356,9 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
         }
     }
     if constexpr (DOTS) {
+        // block 0: the chain's first part from the previous update's partials,
+        // done while the other blocks finish their rows
+        if (blockIdx.x == 0) step2_precompute<20>(ga, ga.b_blocks);
         __shared__ double s_red[8][3];
         const float r0 = warp_sum(da0), r1 = warp_sum(da1), r2 = warp_sum(dw);
         if (lane == 0) {
@@ -370,7 +373,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
         });
         __shared__ int s_flag;
         if (!grid_last_block(ga.counter, &s_flag)) return;
-        step2_finish<20>(ga, gridDim.x, ga.b_blocks);  // <= 640 blocks: one round of partial loads
+        step2_finish_pre<20>(ga, gridDim.x);  // <= 640 blocks: one round of partial loads
     }
 }
 
