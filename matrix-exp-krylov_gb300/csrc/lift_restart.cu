@@ -21,6 +21,22 @@ namespace {
 constexpr int LIFT_THREADS = 256;
 constexpr int LIFT_BLOCKS_PER_SM = 6;  // a strided multi-column read wants many warps in flight
 
+// The double of a float, exactly (the value F2F produces), by integer
+// operations for normal numbers and zero: the conversion otherwise runs on
+// this GPU's FP64 units, which execute about two lanes per clock per SM.
+// Subnormal, infinite and NaN inputs take the hardware conversion.
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) {
+        if ((u & 0x7fffffffu) == 0u) return __hiloint2double(static_cast<int>(u & 0x80000000u), 0);
+        return static_cast<double>(f);
+    }
+    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu);
+    const unsigned lo = u << 29;
+    return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+}
+
 // RPT rows of y = sum_c coef_c V_c over the columns with nonzero
 // coefficients, loaded 4 at a time (16-byte
 // row groups; 40 registers, so 6 blocks of 256 threads fit an SM). FP64 basis: one DFMA chain per row in column order (the axpy
@@ -71,7 +87,7 @@ __device__ __forceinline__ void lift_rows(const TV* __restrict__ V, size_t ldv, 
                 }
         }
 #pragma unroll
-        for (int i = 0; i < RPT; ++i) y[i] = static_cast<double>(s[i]) - static_cast<double>(comp[i]);
+        for (int i = 0; i < RPT; ++i) y[i] = widen(s[i]) - widen(comp[i]);
     }
 }
 
