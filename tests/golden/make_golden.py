@@ -102,7 +102,7 @@ def cases():
         vd = np.random.default_rng(4).uniform(0, 1, CDd.n)
         out.append((f"decay_convdiff16_pe{int(pe)}", CDd, vd, t, 30, 0, False,
                     f"convection_diffusion_3d(16, {int(pe)})", 1e-8, None))
-    # BASELINE's config-4 time t = 1 at Pe = 1000: the solution underflows to zero.
+    # The 128^3 convection-diffusion workload's time t = 1 at Pe = 1000: the solution underflows to zero.
     CDu = S.convection_diffusion_3d(16, 1000.0)
     vu = np.random.default_rng(4).uniform(0, 1, CDu.n)
     out.append(("convdiff16_pe1000_t1", CDu, vu, 1.0, 30, 0, False, "convection_diffusion_3d(16, 1000)", 1e-6,
