@@ -5,7 +5,7 @@
 // tolerance 1e-6, v = 0.1, OUTPUT_Y_FILE dump and summary lines. It runs on
 // one GPU. Extra flags: --precision fp64|mixed (default fp64, the
 // reference's arithmetic), --controller reference|search|learned (default
-// the reference's heuristic), --window W (mixed precision, symmetric A:
+// the reference's heuristic), --window W (symmetric A, either precision:
 // orthogonalise against the last W basis vectors), --quiet (no
 // [STEP]/[FLOPs] lines), --verbose-h (the reference's per-step
 // "H_m column j stored" lines, main.cu:1951) and --host-load. A .bincsr input is loaded straight
