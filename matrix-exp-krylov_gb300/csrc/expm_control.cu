@@ -698,7 +698,7 @@ __device__ void write_log(DevState* st, mexk_step_t* log, double dt, double err,
 // takes the largest passing step (its exponential is reused for the lift),
 // or, if none passes, continues below the smallest candidate with the
 // reference's shrink rule (on its own).
-__global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchArgs a, int m) {
+__global__ void __launch_bounds__(EXPM_THREADS, 1) controller_search_kernel(SearchArgs a, int m) {
     extern __shared__ double smem[];
     __shared__ int s_k, s_bd, s_flag, s_best, s_dec, s_mnext;
     __shared__ double s_tau, s_center, s_n1;
@@ -761,43 +761,63 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
         //     the centre), chains (c, .., c+12) for c = 0..3 and 16..19.
         const int chain = static_cast<int>(blockIdx.x) / SEARCH_CLUSTER;
         const bool lead = blockIdx.x % SEARCH_CLUSTER == 0;
-        int g0, period, len;
-        double tau0;
-        if (a.mlp != nullptr && chain < 8) {
-            g0 = chain;
-            period = 8;
-            len = 2;
-            tau0 = s_center * exp2(0.125 * (g0 - 8));
-        } else if (a.mlp != nullptr) {
-            g0 = SEARCH_CAND / 2 + (chain - 8);
-            period = 4;
-            len = 4;
-            const double base = st->tau_prev > 0.0 ? 2.0 * st->tau_prev : st->dt;
-            tau0 = base * exp2(0.25 * (g0 - SEARCH_CAND / 2 - 15));
-        } else {
-            g0 = chain < 4 ? chain : SEARCH_CAND / 2 + (chain - 4);
-            period = 4;
-            len = 4;
-            tau0 = s_center * exp2(spacing * (g0 - offset));
-        }
-        const ClusterProducts pr{k};
-        double* E = nullptr;
-        bool clamped_done = false;
-        double t_i = tau0;
-        for (int i = 0; i < len; ++i, t_i *= 2.0) {
-            const bool clamped = !(t_i < rem);
-            const double tau = clamped ? rem : t_i;
-            if (i == 0 || (clamped && !clamped_done)) {
-                for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = tau * a.H[(e % k) + (e / k) * ldh];
-                __syncthreads();
-                E = expm_taylor(B, k, pr);
-                clamped_done = clamped;
-            } else if (!clamped) {
-                double* W = E == B.T ? B.U : B.T;
-                mm_p(pr, k, E, E, W);
-                E = W;
+        const int nch = a.mlp != nullptr ? SEARCH_CHAINS_NET : SEARCH_CHAINS;
+        // chain c: candidates g0, g0 + period, ... (len of them), the first at tau0
+        auto chain_of = [&](int c, int* g0, int* period, int* len) {
+            if (a.mlp != nullptr && c < 8) {
+                *g0 = c;
+                *period = 8;
+                *len = 2;
+            } else if (a.mlp != nullptr) {
+                *g0 = SEARCH_CAND / 2 + (c - 8);
+                *period = 4;
+                *len = 4;
+            } else {
+                *g0 = c < 4 ? c : SEARCH_CAND / 2 + (c - 4);
+                *period = 4;
+                *len = 4;
             }
-            double* c = a.cand + static_cast<size_t>(g0 + i * period) * CAND_STRIDE;
+        };
+        __shared__ double s_tau0[SEARCH_CHAINS_NET];
+        __shared__ int s_grem;
+        if (static_cast<int>(threadIdx.x) < nch) {
+            int g0, period, len;
+            chain_of(threadIdx.x, &g0, &period, &len);
+            double t0;
+            if (a.mlp != nullptr && static_cast<int>(threadIdx.x) < 8) {
+                t0 = s_center * exp2(0.125 * (g0 - 8));
+            } else if (a.mlp != nullptr) {
+                const double base = st->tau_prev > 0.0 ? 2.0 * st->tau_prev : st->dt;
+                t0 = base * exp2(0.25 * (g0 - SEARCH_CAND / 2 - 15));
+            } else {
+                t0 = s_center * exp2(spacing * (g0 - offset));
+            }
+            s_tau0[threadIdx.x] = t0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // The lowest candidate clamped to the remaining time: the extra
+            // cluster evaluates that step once; the other clamped candidates
+            // are the same step at a higher index, which the choice below
+            // never takes, and are marked as failing.
+            int gr = SEARCH_CAND;
+            for (int c = 0; c < nch; ++c) {
+                int g0, period, len;
+                chain_of(c, &g0, &period, &len);
+                double t = s_tau0[c];
+                for (int i = 0; i < len; ++i, t *= 2.0)
+                    if (!(t < rem)) {
+                        gr = g0 + i * period < gr ? g0 + i * period : gr;
+                        break;
+                    }
+            }
+            s_grem = gr;
+        }
+        __syncthreads();
+        const int g_rem = s_grem;
+        const ClusterProducts pr{k};
+        auto write_cand = [&](int g, const double* E, double tau) {
+            double* c = a.cand + static_cast<size_t>(g) * CAND_STRIDE;
             if (lead)
                 for (int r = threadIdx.x; r < k; r += blockDim.x) c[2 + r] = E[r];
             if (lead && threadIdx.x == 0) {
@@ -805,6 +825,39 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
                 c[1] = tau;
             }
             pr.sync();  // the lead has read E before the next product writes into the buffers
+        };
+        if (chain < nch) {
+            int g0, period, len;
+            chain_of(chain, &g0, &period, &len);
+            double* E = nullptr;
+            double t_i = s_tau0[chain];
+            for (int i = 0; i < len; ++i, t_i *= 2.0) {
+                const int g = g0 + i * period;
+                if (!(t_i < rem)) {  // clamped, as every later member
+                    if (g != g_rem && lead && threadIdx.x == 0) {
+                        double* c = a.cand + static_cast<size_t>(g) * CAND_STRIDE;
+                        c[0] = INFINITY;
+                        c[1] = rem;
+                    }
+                    continue;
+                }
+                if (i == 0) {
+                    for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = t_i * a.H[(e % k) + (e / k) * ldh];
+                    __syncthreads();
+                    E = expm_taylor(B, k, pr);
+                } else {
+                    double* W = E == B.T ? B.U : B.T;
+                    mm_p(pr, k, E, E, W);
+                    E = W;
+                }
+                write_cand(g, E, t_i);
+            }
+        } else if (g_rem < SEARCH_CAND) {
+            // the extra cluster: the remaining time as a step
+            for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = rem * a.H[(e % k) + (e / k) * ldh];
+            __syncthreads();
+            double* E = expm_taylor(B, k, pr);
+            write_cand(g_rem, E, rem);
         }
     }
     if (!grid_last_block(a.counter, &s_flag)) return;
@@ -888,7 +941,8 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_search_kernel(SearchA
 int launch_controller_search(const SearchArgs& a, int m, cudaStream_t s) {
     if (m > EXPM_SMEM_K) return MEXK_ERR_UNSUPPORTED;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((a.mlp != nullptr ? SEARCH_CHAINS_NET : SEARCH_CHAINS) * SEARCH_CLUSTER);
+    // the chains and one cluster for the remaining time as a step
+    cfg.gridDim = dim3(((a.mlp != nullptr ? SEARCH_CHAINS_NET : SEARCH_CHAINS) + 1) * SEARCH_CLUSTER);
     cfg.blockDim = dim3(EXPM_THREADS);
     cfg.dynamicSmemBytes = expm_smem_bytes(m);
     cfg.stream = s;
