@@ -196,10 +196,13 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
     const int* __restrict__ toff = T->off;
     const int* __restrict__ tlen = T->len;
     int ids[PAT_RPT];
+    // Addresses: one base pointer per row group or pattern entry, the rows
+    // 32 i apart at constant offsets from it (no 64-bit index arithmetic
+    // per row and entry).
     auto load_ids = [&](int cc, int k) {  // pid is zero-padded to whole chunks
+        const uint8_t* __restrict__ pb = pid + (static_cast<size_t>(cc) * PAT_CHUNK + wrow(k));
 #pragma unroll
-        for (int i = 0; i < PAT_RPT; ++i)
-            ids[i] = cc < nchunk ? __ldg(pid + (static_cast<size_t>(cc) * PAT_CHUNK + wrow(k) + i * 32)) : 0;
+        for (int i = 0; i < PAT_RPT; ++i) ids[i] = cc < nchunk ? __ldg(pb + i * 32) : 0;
     };
     // the matrix is never written by a kernel: the major pattern and the
     // first ids load before the wait
@@ -233,22 +236,25 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
         load_ids(c + gridDim.x, k + 1);
         float up[PAT_RPT], uj[PAT_RPT];
         if constexpr (DOTS == 1) {
+            const float* __restrict__ vb = vlo + r0;
 #pragma unroll
-            for (int i = 0; i < PAT_RPT; ++i) up[i] = r0 + i * 32 < n ? __ldg(vlo + (r0 + i * 32)) : 0.f;
+            for (int i = 0; i < PAT_RPT; ++i) up[i] = r0 + i * 32 < n ? __ldg(vb + i * 32) : 0.f;
         }
         auto load_uj = [&]() {  // u_j = x at the thread's rows
             if constexpr (DOTS) {
+                const float* __restrict__ vb = vj + r0;
 #pragma unroll
-                for (int i = 0; i < PAT_RPT; ++i) uj[i] = r0 + i * 32 < n ? __ldg(vj + (r0 + i * 32)) : 0.f;
+                for (int i = 0; i < PAT_RPT; ++i) uj[i] = r0 + i * 32 < n ? __ldg(vb + i * 32) : 0.f;
             }
         };
         // rows [r0, r0 + 32 i] in range and their sums in s: store, accumulate the dots
         auto emit = [&](const TX (&s)[PAT_RPT], bool all_in) {
+            TX* __restrict__ yb = y + r0;
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i) {
                 const int r = r0 + i * 32;
                 if (all_in || r < n) {
-                    y[r] = s[i];
+                    yb[i * 32] = s[i];
                     if constexpr (DOTS) {
                         const float sf = static_cast<float>(s[i]);
                         if constexpr (DOTS == 1) da0 = fmaf(up[i], sf, da0);
@@ -282,7 +288,9 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
                 pa[q] = on ? __ldg(tv + p0 * PAT_LEN + q) : TX(0);
                 if (on && po[q] == 0) pq0 = q;
             }
-            const TX* xb = x + r0;
+            const TX* xe[LMAX];
+#pragma unroll
+            for (int q = 0; q < LMAX; ++q) xe[q] = x + (r0 + po[q]);
             if (pq0 < 0) load_uj();
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i) {
@@ -290,7 +298,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
 #pragma unroll
                 for (int q = 0; q < LMAX; ++q) {
                     if (q < plen) {
-                        const TX xq = __ldg(xb + (i * 32 + po[q]));
+                        const TX xq = __ldg(xe[q] + i * 32);
                         if constexpr (DOTS) {
                             if (q == pq0) uj[i] = xq;
                         }
@@ -301,7 +309,9 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
             }
             emit(s, true);
         } else if (__all_sync(PAT_FULL, all_major)) {
-            const TX* xb = x + r0;
+            const TX* xe[LMAX];
+#pragma unroll
+            for (int q = 0; q < LMAX; ++q) xe[q] = x + (r0 + mo[q]);
             if (q0 < 0) load_uj();
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i) {
@@ -309,7 +319,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
 #pragma unroll
                 for (int q = 0; q < LMAX; ++q) {
                     if (q < major_len) {
-                        const TX xq = __ldg(xb + (i * 32 + mo[q]));
+                        const TX xq = __ldg(xe[q] + i * 32);
                         if constexpr (DOTS) {
                             if (q == q0) uj[i] = xq;  // the diagonal entry gathers u_j at the row itself
                         }

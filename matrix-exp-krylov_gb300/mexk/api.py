@@ -208,8 +208,9 @@ class Context:
     LANCZOS_FORMS = ("stepwise", "fused")
 
     def lanczos_form(self) -> str:
-        """How window-2 bases run their steps: "fused" (one cooperative
-        launch per basis, the default where it applies) or "stepwise"."""
+        """How window-2 bases run their steps: "stepwise" (two launches per
+        step, the default) or "fused" (one cooperative launch per basis, when
+        selected and the basis's rows fit)."""
         f = C.c_int(0)
         check(lib().mexk_context_get_lanczos_form(self._h, C.byref(f)), "mexk_context_get_lanczos_form")
         return self.LANCZOS_FORMS[f.value]
