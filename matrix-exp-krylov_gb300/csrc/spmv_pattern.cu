@@ -214,10 +214,6 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
         mo[q] = on ? __ldg(toff + major * PAT_LEN + q) : 0;
         ma[q] = on ? __ldg(tv + major * PAT_LEN + q) : TX(0);
     }
-    int q0 = -1;  // the major pattern's entry at offset 0, if any
-#pragma unroll
-    for (int q = 0; q < LMAX; ++q)
-        if (q < major_len && mo[q] == 0) q0 = q;
     int c = blockIdx.x;
     load_ids(c, 0);
     pdl_wait();
@@ -280,18 +276,16 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
             const int plen = __ldg(tlen + p0);
             int po[LMAX];
             TX pa[LMAX];
-            int pq0 = -1;
 #pragma unroll
             for (int q = 0; q < LMAX; ++q) {
                 const bool on = q < plen;
                 po[q] = on ? __ldg(toff + p0 * PAT_LEN + q) : 0;
                 pa[q] = on ? __ldg(tv + p0 * PAT_LEN + q) : TX(0);
-                if (on && po[q] == 0) pq0 = q;
             }
             const TX* xe[LMAX];
 #pragma unroll
             for (int q = 0; q < LMAX; ++q) xe[q] = x + (r0 + po[q]);
-            if (pq0 < 0) load_uj();
+            load_uj();
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i) {
                 TX acc = TX(0);
@@ -299,9 +293,6 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
                 for (int q = 0; q < LMAX; ++q) {
                     if (q < plen) {
                         const TX xq = __ldg(xe[q] + i * 32);
-                        if constexpr (DOTS) {
-                            if (q == pq0) uj[i] = xq;
-                        }
                         acc += pat_mul(pa[q], xq);
                     }
                 }
@@ -312,7 +303,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
             const TX* xe[LMAX];
 #pragma unroll
             for (int q = 0; q < LMAX; ++q) xe[q] = x + (r0 + mo[q]);
-            if (q0 < 0) load_uj();
+            load_uj();  // the rows' own lines, just gathered: L1 hits
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i) {
                 TX acc = TX(0);
@@ -320,9 +311,6 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
                 for (int q = 0; q < LMAX; ++q) {
                     if (q < major_len) {
                         const TX xq = __ldg(xe[q] + i * 32);
-                        if constexpr (DOTS) {
-                            if (q == q0) uj[i] = xq;  // the diagonal entry gathers u_j at the row itself
-                        }
                         acc += pat_mul(ma[q], xq);
                     }
                 }
