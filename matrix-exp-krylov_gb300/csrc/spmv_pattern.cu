@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(PAT_THREADS, 4)
             emit(s, true);
         } else {
             load_uj();
-            constexpr int GP = DOTS ? 1 : 2;  // rows whose entries are in flight together
+            constexpr int GP = DOTS == 1 ? 1 : 2;  // rows whose entries are in flight together (DOTS 1: registers)
             int len[PAT_RPT];
 #pragma unroll
             for (int i = 0; i < PAT_RPT; ++i)
