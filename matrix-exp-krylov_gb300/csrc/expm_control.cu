@@ -52,6 +52,43 @@ __device__ __forceinline__ double dot_k(int k, const double* X, int ldx, const d
     return (s0 + s1) + (s2 + s3);
 }
 
+// Band of a k x k matrix: entry (r, c) may be nonzero only if r - c <= lb
+// and c - r <= ub. A product's band is the sum of its factors' (capped at
+// k - 1); a tridiagonal Lanczos H gives banded powers, and a Hessenberg H a
+// lower bandwidth that grows by one per factor.
+struct Band {
+    int lb, ub;
+};
+__device__ __forceinline__ Band band_mul(Band x, Band y, int k) {
+    return {min(x.lb + y.lb, k - 1), min(x.ub + y.ub, k - 1)};
+}
+__device__ __forceinline__ Band band_max(Band x, Band y) { return {max(x.lb, y.lb), max(x.ub, y.ub)}; }
+
+// dot_k over the terms l in [lo, hi] only (every other product has an exact
+// zero factor): the loop keeps dot_k's groups of four and its tail, so each
+// nonzero product lands in the same accumulation in the same order and the
+// sum is dot_k's.
+__device__ __forceinline__ double dot_k_band(int k, int lo, int hi, const double* X, int ldx, const double* Y) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int l = lo & ~3;
+    const int end = min(k, (hi + 4) & ~3);  // past hi, at a group boundary (or k)
+    for (; l + 3 < end; l += 4) {
+        s0 = fma(X[l * ldx], Y[l], s0);
+        s1 = fma(X[(l + 1) * ldx], Y[l + 1], s1);
+        s2 = fma(X[(l + 2) * ldx], Y[l + 2], s2);
+        s3 = fma(X[(l + 3) * ldx], Y[l + 3], s3);
+    }
+    for (; l < end; ++l) s0 = fma(X[l * ldx], Y[l], s0);
+    return (s0 + s1) + (s2 + s3);
+}
+
+// (X Y)_ij = dot over the l both bands allow.
+__device__ __forceinline__ double dot_banded(int k, int i, int j, const double* X, Band bx, const double* Y, Band by) {
+    const int lo = max(max(i - bx.lb, j - by.ub), 0);
+    const int hi = min(min(i + bx.ub, j + by.lb), k - 1);
+    return dot_k_band(k, lo, hi, X + i, k, Y + j * k);
+}
+
 __device__ void mm(int k, const double* X, const double* Y, double* Z) {
     const int kk = k * k;
     for (int e = threadIdx.x; e < kk; e += blockDim.x) {
@@ -338,17 +375,41 @@ struct ClusterProducts {
     __device__ void sync() const { cooperative_groups::this_cluster().sync(); }
 };
 
-// Z = X Y (k x k), columns shared out as P says.
+// Z = X Y (k x k) for factors within bands bx, by; columns shared out as P
+// says. Returns Z's band.
 template <typename P>
-__device__ void mm_p(const P& pr, int k, const double* X, const double* Y, double* Z) {
+__device__ Band mm_p(const P& pr, int k, const double* X, Band bx, const double* Y, Band by, double* Z) {
     int j0, j1;
     pr.cols(&j0, &j1);
     const int cnt = k * (j1 - j0);
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
         const int i = e % k, j = j0 + e / k;
-        pr.put(Z, i + j * k, dot_k(k, X + i, k, Y + j * k));
+        pr.put(Z, i + j * k, dot_banded(k, i, j, X, bx, Y, by));
     }
     pr.sync();
+    return band_mul(bx, by, k);
+}
+
+// The band of the k x k matrix in A (every thread of the block calls it).
+__device__ Band band_of(int k, const double* A) {
+    __shared__ int s_lb, s_ub;
+    if (threadIdx.x == 0) {
+        s_lb = 0;
+        s_ub = 0;
+    }
+    __syncthreads();
+    int lb = 0, ub = 0;
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        if (A[e] != 0.0) {
+            const int r = e % k, c = e / k;
+            lb = max(lb, r - c);
+            ub = max(ub, c - r);
+        }
+    }
+    if (lb > 0) atomicMax(&s_lb, lb);
+    if (ub > 0) atomicMax(&s_ub, ub);
+    __syncthreads();
+    return {s_lb, s_ub};
 }
 
 // exp of the k-by-k matrix in B.A (ld k) by the degree-18 Taylor polynomial
@@ -362,7 +423,7 @@ __device__ void mm_p(const P& pr, int k, const double* X, const double* Y, doubl
 // thread of the block (of every block of the cluster) must call it, with
 // the same B.A.
 template <typename P>
-__device__ __noinline__ double* expm_taylor(const ExpmBuf& B, int k, const P& pr) {
+__device__ __noinline__ double* expm_taylor(const ExpmBuf& B, int k, const P& pr, Band* band_out) {
     __shared__ int s_sq;
     if (threadIdx.x < k) B.red[threadIdx.x] = col_abs_sum(k, B.A, threadIdx.x);
     __syncthreads();
@@ -385,15 +446,18 @@ __device__ __noinline__ double* expm_taylor(const ExpmBuf& B, int k, const P& pr
     if (sq > 0) {
         for (int e = threadIdx.x; e < kk; e += blockDim.x) B.A[e] = ldexp(B.A[e], -sq);
     }
+    // the band of X (scaling keeps every zero); the products below skip the
+    // terms outside their factors' bands
+    const Band b1 = band_of(k, B.A);
     // every block's copy of X must be final before a product writes into it
     pr.sync();
     const double* X = B.A;
     double* X2 = B.A2;
     double* X3 = B.A4;
     double* X4 = B.A6;
-    mm_p(pr, k, X, X, X2);
-    mm_p(pr, k, X2, X, X3);
-    mm_p(pr, k, X2, X2, X4);
+    const Band b2 = mm_p(pr, k, X, b1, X, b1, X2);
+    const Band b3 = mm_p(pr, k, X2, b2, X, b1, X3);
+    const Band b4 = mm_p(pr, k, X2, b2, X2, b2, X4);
     const double* c = kInvFact;
     // Z = c16 I + c17 X + c18 X^2 (every block its full copy)
     double* Z = B.T;
@@ -408,29 +472,35 @@ __device__ __noinline__ double* expm_taylor(const ExpmBuf& B, int k, const P& pr
     int j0, j1;
     pr.cols(&j0, &j1);
     const int cnt = k * (j1 - j0);
+    Band bz = b2;
     for (int q = 3; q >= 0; --q) {
         for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
             const int i = e % k, j = j0 + e / k;
             const int idx = i + j * k;
             double b = c[4 * q + 1] * X[idx] + c[4 * q + 2] * X2[idx] + c[4 * q + 3] * X3[idx];
             if (i == j) b = b + c[4 * q];
-            pr.put(W, idx, dot_k(k, X4 + i, k, Z + j * k) + b);
+            pr.put(W, idx, dot_banded(k, i, j, X4, b4, Z, bz) + b);
         }
         pr.sync();
+        bz = band_max(band_mul(b4, bz, k), b3);
         double* t = Z;
         Z = W;
         W = t;
     }
     for (int r = 0; r < sq; ++r) {
-        mm_p(pr, k, Z, Z, W);
+        bz = mm_p(pr, k, Z, bz, Z, bz, W);
         double* t = Z;
         Z = W;
         W = t;
     }
+    *band_out = bz;
     return Z;
 }
 
-__device__ double* expm_taylor_block(const ExpmBuf& B, int k) { return expm_taylor(B, k, BlockProducts{k}); }
+__device__ double* expm_taylor_block(const ExpmBuf& B, int k) {
+    Band b;
+    return expm_taylor(B, k, BlockProducts{k}, &b);
+}
 
 __device__ ExpmBuf carve(double* smem, int k) {
     ExpmBuf B;
@@ -830,6 +900,7 @@ __global__ void __launch_bounds__(EXPM_THREADS, 1) controller_search_kernel(Sear
             int g0, period, len;
             chain_of(chain, &g0, &period, &len);
             double* E = nullptr;
+            Band eb{0, 0};
             double t_i = s_tau0[chain];
             for (int i = 0; i < len; ++i, t_i *= 2.0) {
                 const int g = g0 + i * period;
@@ -844,10 +915,10 @@ __global__ void __launch_bounds__(EXPM_THREADS, 1) controller_search_kernel(Sear
                 if (i == 0) {
                     for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = t_i * a.H[(e % k) + (e / k) * ldh];
                     __syncthreads();
-                    E = expm_taylor(B, k, pr);
+                    E = expm_taylor(B, k, pr, &eb);
                 } else {
                     double* W = E == B.T ? B.U : B.T;
-                    mm_p(pr, k, E, E, W);
+                    eb = mm_p(pr, k, E, eb, E, eb, W);
                     E = W;
                 }
                 write_cand(g, E, t_i);
@@ -856,7 +927,8 @@ __global__ void __launch_bounds__(EXPM_THREADS, 1) controller_search_kernel(Sear
             // the extra cluster: the remaining time as a step
             for (int e = threadIdx.x; e < k * k; e += blockDim.x) B.A[e] = rem * a.H[(e % k) + (e / k) * ldh];
             __syncthreads();
-            double* E = expm_taylor(B, k, pr);
+            Band eb;
+            double* E = expm_taylor(B, k, pr, &eb);
             write_cand(g_rem, E, rem);
         }
     }
