@@ -806,7 +806,12 @@ __global__ void __launch_bounds__(EXPM_THREADS, 1) controller_search_kernel(Sear
             double c = exp2(static_cast<double>(s_o[0])) / s_n1;
             c = c > st->dt_min ? c : st->dt_min;
             s_center = c < rem ? c : rem;
-            s_mnext = net::next_m_from(s_o[1], a.m_cap);
+            // the next basis keeps at least half of this one's columns (the
+            // way the step size shrinks by a bounded factor): a network that
+            // asks for a much smaller basis near the end of a solve would
+            // otherwise trade one cycle for several short ones
+            const int m_floor = min((m / 2 + net::M_STEP - 1) / net::M_STEP * net::M_STEP, a.m_cap);
+            s_mnext = max(net::next_m_from(s_o[1], a.m_cap), m_floor);
         }
         __syncthreads();
     }
