@@ -47,7 +47,9 @@ extern "C" {
                                  a solve never add up to more than 5e-7 of the
                                  iterate's norm (beyond what tol itself allows) */
 #define MEXK_CTRL_LEARNED 2   /* SEARCH centred on an MLP's step prediction, with the
-                                 MLP also choosing the next cycle's Krylov dimension */
+                                 MLP also choosing the next cycle's Krylov dimension
+                                 (at least half of the current one, rounded up to a
+                                 multiple of 5, at most the allocation) */
 
 /* Largest Krylov dimension m: MEXK_M_MAX for the plain method (FP64 and the
  * reference controller, the reference's ArnoldiParams default m = 100 among
