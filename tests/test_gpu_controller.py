@@ -263,3 +263,36 @@ def test_learned_window_controller_against_search(N):
     for ctrl, (_, r, err) in out.items():
         assert r["converged"] == 1 and err <= 1e-6, (ctrl, err)
     assert out["learned"][1]["spmv_count"] <= out["search"][1]["spmv_count"]
+
+
+def test_learned_next_basis_keeps_half():
+    """A network whose size output asks for the smallest basis after every
+    cycle: the next basis still keeps at least half of the current one's
+    columns (rounded up to a multiple of 5), so the sizes go 40, 20, 10, ...
+    instead of dropping to 10 at once, and the solve stays within 1e-6 of
+    FP64."""
+    from mexk import controller as K
+    from mexk import synthetic as S
+    from mexk._lib import MEXK_OK, lib
+    from mexk.api import Context
+
+    A = S.laplacian_2d(160, h=1.0 / 2049)
+    v = np.random.default_rng(8).uniform(0, 1, A.n)
+    t = 1e-5
+    w = np.ascontiguousarray(K.load(K.WEIGHTS), dtype=np.float32)
+    omean = K.NET_PARAMS + 2 * K.NET_IN
+    w[omean + 1] = -10.0  # raw size output: far below the smallest basis
+    w[omean + K.NET_OUT + 1] = 0.0
+    with Context(A, m_alloc=60) as ctx:
+        y64, _ = ctx.expmv(v, t, 40)
+        assert lib().mexk_context_set_controller(ctx.handle, w.ctypes.data_as(C.POINTER(C.c_float)), w.size) == MEXK_OK
+        ctx._net_loaded = True
+        y, r = ctx.expmv(v, t, 40, precision="mixed", controller="learned")
+        ms = [int(s[3]) for s in ctx.steps()]
+    # one attempt per cycle (the search takes a candidate every time), so
+    # the step log's basis sizes are the cycles'
+    assert r["converged"] == 1 and r["cycles"] >= 3 and r["attempts"] == r["cycles"], (r, ms)
+    assert ms[0] == 40 and ms[1] == 20 and ms[2] == 10, ms
+    for a, b in zip(ms, ms[1:]):
+        assert b >= max(10, min(60, -(-(a // 2) // 5) * 5)), ms
+    assert np.linalg.norm(y - y64) / np.linalg.norm(y64) <= 1e-6
