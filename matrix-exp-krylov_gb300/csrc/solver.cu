@@ -565,8 +565,10 @@ void init_state(DevState* st, const mexk_params_t* p, int log_cap) {
     st->log_cap = log_cap;
 }
 
+// y_host (optional): y is also copied there, ahead of the final
+// synchronisation (one host round trip for the result and the state).
 int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, double* y_dev, cudaStream_t s,
-          mexk_result_t* result) {
+          mexk_result_t* result, double* y_host = nullptr) {
     NvtxRange total_range("total_compute_expmv");
     int rc = check_params(ctx, p);
     if (rc) return rc;
@@ -629,6 +631,8 @@ int solve(mexk_context_t ctx, const mexk_params_t* p, const double* v_dev, doubl
     }
     if (y_dev != ctx->d_y)
         MEXK_CK(cudaMemcpyAsync(y_dev, ctx->d_y, sizeof(double) * ctx->n, cudaMemcpyDeviceToDevice, s));
+    if (y_host != nullptr)
+        MEXK_CK(cudaMemcpyAsync(y_host, y_dev, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, s));
     MEXK_CK(cudaMemcpyAsync(ctx->h_state, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, s));
     MEXK_CK(cudaStreamSynchronize(s));
     const DevState* st = ctx->h_state;
@@ -905,12 +909,9 @@ int mexk_expmv(mexk_context_t ctx, const mexk_params_t* p, const double* v_host,
     const size_t bytes = sizeof(double) * ctx->n;
     // v goes through the work vector slot w (FP64, length >= n) as staging.
     MEXK_CK(cudaMemcpyAsync(ctx->d_w, v_host, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    // The start-vector kernels read v before any cycle overwrites w.
-    rc = solve(ctx, p, ctx->d_w, ctx->d_y, ctx->stream, result);
-    if (rc) return rc;
-    MEXK_CK(cudaMemcpyAsync(y_host, ctx->d_y, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    MEXK_CK(cudaStreamSynchronize(ctx->stream));
-    return MEXK_OK;
+    // The start-vector kernels read v before any cycle overwrites w; y
+    // comes back with the solve's final state.
+    return solve(ctx, p, ctx->d_w, ctx->d_y, ctx->stream, result, y_host);
 }
 
 int mexk_get_steps(mexk_context_t ctx, mexk_step_t* steps, int cap, int* count) {
