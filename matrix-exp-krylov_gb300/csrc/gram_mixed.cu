@@ -494,6 +494,23 @@ __global__ void __launch_bounds__(GT, 4) gram_update2_kernel(GramArgs g) {
     }
 }
 
+// From b = |u_{j+1}|^2 (one thread): H(j+1, j), s_{j+1} and the breakdown
+// flag (main.cu:1911).
+__device__ __forceinline__ void last_norm_store(const GramArgs& g, double b) {
+    DevState* st = g.st;
+    GramState* gs = g.gs;
+    const int jn = g.j + 1;
+    const double beta = sqrt(b) * gs->ip[jn];
+    const bool bad = !(beta >= 1e-14) || isinf(beta);
+    if (jn < g.ldh) g.H[jn + static_cast<size_t>(g.j) * g.ldh] = bad ? 0.0 : beta;
+    gs->s[jn] = (b > 0.0 && !isinf(b)) ? rsqrt(b) : 0.0;
+    gs->G[jn + static_cast<size_t>(jn) * GRAM_LD] = 1.0;
+    if (bad) {
+        st->breakdown = 1;
+        st->k_used = jn;
+    }
+}
+
 // |u_{j+1}|^2 by grid reduction; the last block sets H(j+1, j), s_{j+1} and
 // the breakdown flag (main.cu:1911).
 __global__ void __launch_bounds__(GT) gram_norm_kernel(GramArgs g) {
@@ -516,19 +533,21 @@ __global__ void __launch_bounds__(GT) gram_norm_kernel(GramArgs g) {
     __shared__ double s_tot[1];
     step_sum_partials<20>(g.part, 1, [](int) { return 0; }, [&](int) { return static_cast<int>(gridDim.x); }, s_tot);
     __syncthreads();
-    if (threadIdx.x == 0) {
-        GramState* gs = g.gs;
-        const double b = s_tot[0];
-        const double beta = sqrt(b) * gs->ip[jn];
-        const bool bad = !(beta >= 1e-14) || isinf(beta);
-        if (jn < g.ldh) g.H[jn + static_cast<size_t>(g.j) * g.ldh] = bad ? 0.0 : beta;
-        gs->s[jn] = (b > 0.0 && !isinf(b)) ? rsqrt(b) : 0.0;
-        gs->G[jn + static_cast<size_t>(jn) * GRAM_LD] = 1.0;
-        if (bad) {
-            st->breakdown = 1;
-            st->k_used = jn;
-        }
-    }
+    if (threadIdx.x == 0) last_norm_store(g, s_tot[0]);
+}
+
+// The same from the |u_{j+1}|^2 partials the last two-column update wrote
+// into column j+1's b slot (over g.b_blocks row blocks): one block sums
+// them, no sweep of u_{j+1}.
+__global__ void __launch_bounds__(GT) gram_norm_partials_kernel(GramArgs g) {
+    pdl_wait();
+    DevState* st = g.st;
+    if (st->breakdown || st->done) return;
+    const int jn = g.j + 1;
+    __shared__ double s_tot[1];
+    step_sum_partials<20>(g.part, 1, [&](int) { return GRAM_BOFF + jn; }, [&](int) { return g.b_blocks; }, s_tot);
+    __syncthreads();
+    if (threadIdx.x == 0) last_norm_store(g, s_tot[0]);
 }
 
 int row_blocks(int n, int per_sm) {
@@ -595,6 +614,16 @@ int launch_gram_norm(const GramArgs& a, cudaStream_t s) {
     if (a.j < 0 || a.j >= GRAM_M) return MEXK_ERR_INVALID;
     gram_norm_kernel<<<row_blocks(a.n, 4), GT, 0, s>>>(a);
     MEXK_CK_LAUNCH("gram_norm_kernel");
+    return MEXK_OK;
+}
+
+int launch_gram_norm_partials(const GramArgs& a, cudaStream_t s) {
+    if (a.j < 0 || a.j + 1 >= GRAM_M || a.b_blocks < 1 || a.b_blocks > GRAM_MAX_ROW_BLOCKS) return MEXK_ERR_INVALID;
+    const cudaError_t e = launch_dependent(gram_norm_partials_kernel, 1, GT, 0, s, a);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "gram_norm_partials_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
     return MEXK_OK;
 }
 

@@ -437,6 +437,9 @@ int launch_gram_update(const GramArgs& a, cudaStream_t s);
 int gram_update2_blocks(int n);
 // |u_{j+1}| -> H(j+1, j) and s[j+1] (the last step of a basis, or a single step).
 int launch_gram_norm(const GramArgs& a, cudaStream_t s);
+// The same from the |u_{j+1}|^2 partials of the last two-column update
+// (write_b; a.b_blocks row blocks): one block, no sweep.
+int launch_gram_norm_partials(const GramArgs& a, cudaStream_t s);
 
 // Steps j0..m-1 of a Lanczos basis (window 2, symmetric A in the row-pattern
 // form, FP32 basis) in one cooperative launch (lanczos_cycle.cu): per step

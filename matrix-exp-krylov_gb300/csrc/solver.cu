@@ -327,6 +327,15 @@ bool fused_step(int j, int window) {
     return j >= 1 && j + 1 - lo <= 2;
 }
 
+// Whether the last update of an m-column mixed basis (step m - 1) leaves
+// |u_m|^2 as partials in column m's b slot: a two-column update sweep, and a
+// slot below the |w|^2 one. The basis's last norm then needs no sweep.
+bool norm_from_update(int m, int window) {
+    if (m < 1 || m >= GRAM_M) return false;
+    const int lo = window > 0 ? std::max(0, m - window) : 0;
+    return m - lo <= 2;
+}
+
 // The context SpMV in its form for the precision: w = A u_j (dots: FP32, as
 // for launch_spmv; not with the direct form).
 int context_spmv(mexk_context_t ctx, int j, bool fp32, const int* skip, cudaStream_t s,
@@ -367,6 +376,7 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
         if ((rc = context_spmv(ctx, j, true, &ctx->d_state->breakdown, s, fuse ? &g : nullptr))) return rc;
         if (!fuse && (rc = launch_gram_dot(g, s))) return rc;
         g.write_b = (fusable && j + 1 < m && fused_step(j + 1, window)) ? 1 : 0;
+        if (m > 0 && j + 1 == m && norm_from_update(m, window)) g.write_b = 1;  // for finish_basis
         return launch_gram_update(g, s);
     }
     if ((rc = context_spmv(ctx, j, false, &ctx->d_state->breakdown, s))) return rc;
@@ -383,9 +393,17 @@ int enqueue_step(mexk_context_t ctx, int j, int reortho, bool fp32, cudaStream_t
     return launch_normalize<double>(ctx->n, j, ctx->ldv, ctx->d_w, ctx->d_V, ctx->d_state, nullptr, s);
 }
 
-// After the last step j of a basis: H(j+1, j) of the mixed form.
-int finish_basis(mexk_context_t ctx, int j, bool fp32, cudaStream_t s) {
-    return fp32 ? launch_gram_norm(gram_args(ctx, j, 1), s) : MEXK_OK;
+// After the last step j of a basis: H(j+1, j) of the mixed form. partials:
+// the basis was built by enqueue_step with m = j + 1 and its window, whose
+// last update left |u_{j+1}|^2 as partials (norm_from_update).
+int finish_basis(mexk_context_t ctx, int j, bool fp32, cudaStream_t s, bool partials = false) {
+    if (!fp32) return MEXK_OK;
+    GramArgs g = gram_args(ctx, j, 1);
+    if (partials) {
+        g.b_blocks = gram_update2_blocks(ctx->n);
+        return launch_gram_norm_partials(g, s);
+    }
+    return launch_gram_norm(g, s);
 }
 
 // The cycle's step controller over the k x k Hessenberg (k = m, or the
@@ -455,7 +473,8 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, 
     // a window's FP64 steps leave H(0:lo-1, j) alone: the cycle starts from zero
     if (!fp32 && window > 0)
         MEXK_CK(cudaMemsetAsync(ctx->d_H, 0, sizeof(double) * static_cast<size_t>(ctx->ldh) * m, s));
-    if (use_lanczos_cycle(ctx, m, fp32, window)) {
+    const bool fused = use_lanczos_cycle(ctx, m, fp32, window);
+    if (fused) {
         // step 0 as two kernels (its update writes step 1's b and a_0 partials), then the rest in one launch
         if ((rc = enqueue_step(ctx, 0, reortho, fp32, s, window, m))) return rc;
         if ((rc = enqueue_lanczos_cycle(ctx, m, reortho, s))) return rc;
@@ -463,7 +482,8 @@ int enqueue_cycle(mexk_context_t ctx, int m, int reortho, int ctrl, int window, 
         for (int j = 0; j < m; ++j)
             if ((rc = enqueue_step(ctx, j, reortho, fp32, s, window, m))) return rc;
     }
-    if ((rc = finish_basis(ctx, m - 1, fp32, s))) return rc;
+    // the stepwise basis's last update left |u_m|^2 as partials where it could
+    if ((rc = finish_basis(ctx, m - 1, fp32, s, !fused && fp32 && norm_from_update(m, window)))) return rc;
     if ((rc = enqueue_controller(ctx, m, ctrl, ctx->d_log, s, window))) return rc;
     const LiftArgs l = lift_args(ctx, fp32);
     if ((rc = launch_lift<TV>(l, gs_grid_size(ctx->n, 1), s))) return rc;
