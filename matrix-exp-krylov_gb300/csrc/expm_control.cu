@@ -773,6 +773,11 @@ __global__ void __launch_bounds__(EXPM_THREADS, 1) controller_search_kernel(Sear
     __shared__ int s_k, s_bd, s_flag, s_best, s_dec, s_mnext;
     __shared__ double s_tau, s_center, s_n1;
     __shared__ float s_f[net::IN], s_a1[net::HID], s_a2[net::HID], s_o[net::OUT];
+    // a programmatic dependent of the basis's last kernel: the state and H
+    // are read after the wait; the lift may then launch onto the SMs the
+    // clusters leave idle (it waits for this grid before reading)
+    pdl_wait();
+    pdl_trigger();
     DevState* st = a.st;
     if (st->done) return;
     if (threadIdx.x == 0) {
@@ -1023,13 +1028,15 @@ int launch_controller_search(const SearchArgs& a, int m, cudaStream_t s) {
     cfg.blockDim = dim3(EXPM_THREADS);
     cfg.dynamicSmemBytes = expm_smem_bytes(m);
     cfg.stream = s;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = SEARCH_CLUSTER;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     const cudaError_t e = cudaLaunchKernelEx(&cfg, controller_search_kernel, a, m);
     if (e != cudaSuccess) {
         set_cuda_error(e, "controller_search_kernel", __FILE__, __LINE__);

@@ -541,6 +541,7 @@ __global__ void __launch_bounds__(GT) gram_norm_kernel(GramArgs g) {
 // them, no sweep of u_{j+1}.
 __global__ void __launch_bounds__(GT) gram_norm_partials_kernel(GramArgs g) {
     pdl_wait();
+    pdl_trigger();  // the controller may take the idle SMs meanwhile
     DevState* st = g.st;
     if (st->breakdown || st->done) return;
     const int jn = g.j + 1;

@@ -100,6 +100,10 @@ __global__ void __launch_bounds__(LIFT_THREADS, LIFT_BLOCKS_PER_SM) lift_kernel(
     __shared__ double s_out[1];
     __shared__ double s_scratch[LIFT_THREADS];
     __shared__ int s_flag;
+    // launched as a dependent of the controller: its state and coefficients
+    // are read after the wait; the restart may launch meanwhile
+    pdl_wait();
+    pdl_trigger();
     DevState* st = a.st;
     if (!st->lift) return;
     const int k = st->k_lift;
@@ -189,6 +193,8 @@ __global__ void __launch_bounds__(LIFT_THREADS)
 template <typename TV>
 __global__ void __launch_bounds__(256) restart_kernel(int n, const double* __restrict__ x, TV* __restrict__ V0,
                                                       const DevState* st, int force) {
+    pdl_wait();  // a dependent of the lift (no-op after a plain launch)
+    pdl_trigger();
     if (!force && !st->restart) return;
     const TV sc = static_cast<TV>(st->restart_scale);
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
@@ -209,16 +215,22 @@ int launch_lift(const LiftArgs& a, int /*grid*/, cudaStream_t s) {
     const long long need = (static_cast<long long>(a.n) + RPT * LIFT_THREADS - 1) / (RPT * LIFT_THREADS);
     const long long cap = static_cast<long long>(device_sm_count()) * LIFT_BLOCKS_PER_SM;
     const int grid = static_cast<int>(need < cap ? (need < 1 ? 1 : need) : cap);
-    lift_kernel<TV><<<grid, LIFT_THREADS, 0, s>>>(a);
-    MEXK_CK_LAUNCH("lift_kernel");
+    const cudaError_t e = launch_dependent(lift_kernel<TV>, grid, LIFT_THREADS, 0, s, a);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "lift_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
     return MEXK_OK;
 }
 
 template <typename TV>
 int launch_restart(int n, int ldv, const double* y, TV* V, const DevState* st, cudaStream_t s) {
     (void)ldv;
-    restart_kernel<TV><<<elementwise_grid(n), 256, 0, s>>>(n, y, V, st, 0);
-    MEXK_CK_LAUNCH("restart_kernel");
+    const cudaError_t e = launch_dependent(restart_kernel<TV>, elementwise_grid(n), 256, 0, s, n, y, V, st, 0);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "restart_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
     return MEXK_OK;
 }
 
