@@ -541,6 +541,8 @@ __global__ void __launch_bounds__(EXPM_THREADS) controller_kernel(ControlArgs a,
     extern __shared__ double smem[];
     __shared__ int s_k, s_bd, s_dec, s_mcur, s_cyc_bd, s_cyc_k;
     __shared__ double s_dt;
+    pdl_wait();  // launched as a dependent of the basis's last kernel
+    pdl_trigger();
     // One block per state: block b drives state b (a batch), or the only one.
     DevState* st = a.st + blockIdx.x;
     const double* Hb = a.H + blockIdx.x * a.h_stride;
@@ -1069,8 +1071,11 @@ int launch_expm_standalone(int k, const double* A, int lda, double* E, int lde, 
 int launch_controller(const ControlArgs& a, int m, cudaStream_t s, int nstates) {
     if (m > EXPM_SMEM_K && (a.ws == nullptr || nstates != 1)) return MEXK_ERR_INVALID;
     const size_t smem = expm_launch_smem(m);
-    controller_kernel<<<nstates, EXPM_THREADS, smem, s>>>(a, m);
-    MEXK_CK_LAUNCH("controller_kernel");
+    const cudaError_t e = launch_dependent(controller_kernel, nstates, EXPM_THREADS, smem, s, a, m);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "controller_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
     return MEXK_OK;
 }
 

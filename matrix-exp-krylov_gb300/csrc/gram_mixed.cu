@@ -514,6 +514,8 @@ __device__ __forceinline__ void last_norm_store(const GramArgs& g, double b) {
 // |u_{j+1}|^2 by grid reduction; the last block sets H(j+1, j), s_{j+1} and
 // the breakdown flag (main.cu:1911).
 __global__ void __launch_bounds__(GT) gram_norm_kernel(GramArgs g) {
+    pdl_wait();
+    pdl_trigger();
     DevState* st = g.st;
     if (st->breakdown || st->done) return;
     const int jn = g.j + 1;
@@ -613,8 +615,11 @@ int launch_gram_update(const GramArgs& a, cudaStream_t s) {
 
 int launch_gram_norm(const GramArgs& a, cudaStream_t s) {
     if (a.j < 0 || a.j >= GRAM_M) return MEXK_ERR_INVALID;
-    gram_norm_kernel<<<row_blocks(a.n, 4), GT, 0, s>>>(a);
-    MEXK_CK_LAUNCH("gram_norm_kernel");
+    const cudaError_t e = launch_dependent(gram_norm_kernel, row_blocks(a.n, 4), GT, 0, s, a);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "gram_norm_kernel", __FILE__, __LINE__);
+        return MEXK_ERR_CUDA;
+    }
     return MEXK_OK;
 }
 
